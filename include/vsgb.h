@@ -1,0 +1,180 @@
+/* include/vsgb.h — C ABI of the GB300 (sm_103a) SOL 101 CHEXA8 backend.
+ *
+ * One shared library (libvsgb.so) replaces three layers of vibestran's
+ * SOL 101 solid path on one GPU:
+ *   - the CHEXA8 element stiffness (src/elements/solid_elements.cpp:95-180 SRI,
+ *     :1054-1206 EAS) and the lower-triangle CSR assembly
+ *     (src/solver/assembly_parallel.hpp:69-110, src/core/sparse_matrix.cpp:16-150),
+ *   - the analysis DOF map (src/core/dof_map.cpp:10-97,
+ *     src/solver/analysis_support.cpp:176-214) and FORCE loads
+ *     (src/solver/linear_static.cpp:344-374),
+ *   - the SolverBackend::solve of --backend=cuda-pcg / cuda-pcg-mixed
+ *     (include/solver/solver_backend.hpp:20-51,
+ *     src/solver/cuda_pcg_backend_impl.hpp:1688-2262).
+ *
+ * Conventions: plain C types, host pointers unless a name says "device",
+ * 0-based equation indices, -1 marks a constrained DOF (CONSTRAINED_DOF,
+ * include/core/dof_map.hpp:20).  Every function returns VSGB_OK (0) or a
+ * negative status; the message of the last failure on a context is returned
+ * by vsgb_last_error().  A context is single-threaded: one host thread at a
+ * time (the reference backend has the same contract).
+ */
+#ifndef VSGB_H
+#define VSGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ── status codes ───────────────────────────────────────────────────────── */
+#define VSGB_OK 0
+#define VSGB_ERR_INVALID (-1)       /* bad argument: size mismatch, empty K, bad index */
+#define VSGB_ERR_SINGULAR (-2)      /* zero / missing diagonal, r.z <= 0 at start */
+#define VSGB_ERR_NOT_CONVERGED (-3) /* max iterations reached, or p.Ap <= 0 breakdown */
+#define VSGB_ERR_CUDA (-4)          /* CUDA runtime error (message has the CUDA text) */
+#define VSGB_ERR_ELEMENT (-5)       /* non-positive Jacobian / EAS Kaa not SPD */
+#define VSGB_ERR_NO_DEVICE (-6)     /* no CUDA device, or not an sm_103 device */
+#define VSGB_ERR_STATE (-7)         /* call order: e.g. solve before assemble */
+#define VSGB_ERR_LIMIT (-8)         /* a documented device limit was exceeded */
+
+/* ── precision / formulation selectors ──────────────────────────────────── */
+#define VSGB_FP64 64  /* FP64 Jacobi PCG (cuda-pcg semantics) */
+#define VSGB_MIXED 32 /* FP32 inner PCG + FP64 refinement on the GPU (cuda-pcg-mixed) */
+
+#define VSGB_EAS 0 /* CHexa8Eas (default, PSOLID ISOP blank or EAS) */
+#define VSGB_SRI 1 /* CHexa8 selective reduced integration (ISOP = SRI) */
+
+/* ── options for vsgb_set_option ────────────────────────────────────────── */
+#define VSGB_OPT_TOLERANCE 1      /* relative residual target (default 1e-8 FP64, 1e-6 mixed) */
+#define VSGB_OPT_MAX_ITERS 2      /* max PCG iterations per solve (default 10000) */
+#define VSGB_OPT_PRECISION 3      /* VSGB_FP64 or VSGB_MIXED */
+#define VSGB_OPT_INNER_TOL 4      /* mixed: inner FP32 tolerance (<=0: clamp(100*tol,1e-4,1e-2)) */
+#define VSGB_OPT_MAX_SOLVES 5     /* mixed: max inner solves (default 3 = 1 + 2 corrections) */
+#define VSGB_OPT_CHECK_EVERY 6    /* iterations launched between host convergence checks */
+#define VSGB_OPT_USE_GRAPH 7      /* 1: replay iteration batches as CUDA graphs (default 1) */
+#define VSGB_OPT_FORMAT 8         /* 0 auto, 1 scalar CSR, 2 3x3 node blocks */
+
+typedef struct vsgb_ctx vsgb_ctx;
+
+/* Per-solve diagnostics (SolverBackend::last_iteration_count /
+ * last_estimated_error, include/solver/solver_backend.hpp:39-43, plus timing). */
+typedef struct vsgb_stats {
+  int iterations;        /* PCG iterations (mixed: summed over inner solves; nrhs>1: max) */
+  int inner_solves;      /* mixed: FP32 solves run (1 for FP64) */
+  int converged;         /* 1 when the tolerance was met */
+  int format;            /* operator format used: 1 scalar CSR, 2 3x3 node blocks */
+  double rel_residual;   /* FP64: sqrt(r.r)/||F|| of the recursion; mixed: true FP64 residual */
+  double solve_ms;       /* device time of the iteration phase (CUDA events) */
+  double setup_ms;       /* device time of operator preparation (upload/expand/convert) */
+  double spmv_bytes;     /* algorithmic bytes of one SpMV of the operator used */
+} vsgb_stats;
+
+/* Create a context on `device` (cuda-pcg uses device 0,
+ * src/solver/cuda_pcg_backend_impl.hpp:2040-2065).  tol <= 0 selects the
+ * default (1e-8 FP64, 1e-6 mixed, as CudaPCGSolverBackend::try_create and
+ * CudaMixedPCGSolverBackend::try_create); max_iters <= 0 selects 10000.
+ * Returns VSGB_ERR_NO_DEVICE (and *out = NULL) when no usable GPU exists —
+ * the try_create() -> nullopt contract. */
+int vsgb_create(int device, double tol, int max_iters, int precision, vsgb_ctx** out);
+void vsgb_destroy(vsgb_ctx* ctx);
+int vsgb_set_option(vsgb_ctx* ctx, int option, double value);
+/* Copies the last error message (NUL-terminated, truncated to len). */
+int vsgb_last_error(vsgb_ctx* ctx, char* buf, size_t len);
+int vsgb_device_name(vsgb_ctx* ctx, char* buf, size_t len);
+/* Backend display name, e.g. "GB300 PCG + Jacobi float64 (GPU)". */
+int vsgb_backend_name(vsgb_ctx* ctx, char* buf, size_t len);
+
+/* Drop-in SolverBackend::solve (include/solver/solver_backend.hpp:27-30):
+ * K as CsrData (row_ptr[n+1], col_ind[nnz], values[nnz]; lower_only != 0 for
+ * SymmetryStorage::Lower), F[n*nrhs] (column-major: rhs k at F + k*n) ->
+ * u_out[n*nrhs].  Errors follow cuda-pcg: empty K, |F| != n, zero or missing
+ * diagonal, r.z <= 0, non-convergence or breakdown.  A zero RHS returns zeros
+ * with 0 iterations. */
+int vsgb_solve_csr(vsgb_ctx* ctx, int n, int nnz, const int* row_ptr, const int* col_ind,
+                   const double* values, int lower_only, const double* F, int nrhs,
+                   double* u_out, vsgb_stats* stats);
+
+/* ── DOF map and loads (host) ───────────────────────────────────────────── */
+
+/* Analysis DOF map of a CHEXA8-only model (DofMap::build + constrain_batch,
+ * src/core/dof_map.cpp:10-97; build_analysis_dof_map,
+ * src/solver/analysis_support.cpp:176-214): node ids are ranked ascending,
+ * each node owns 6 slots, T1-T3 of element nodes are active, SPC components
+ * (bit d set = DOF d+1) are removed, remaining slots are numbered densely.
+ * conn_ids holds grid ids (8 per element).  eq6_out[6*i+d] is the equation of
+ * DOF d of node_ids[i], or -1. */
+int vsgb_build_dof_map(int n_nodes, const int* node_ids, int n_elem, const int* conn_ids,
+                       int n_spc, const int* spc_node_ids, const int* spc_masks, int* eq6_out,
+                       int* n_free, char* err, size_t errlen);
+
+/* FORCE cards with CID 0 (LinearStaticSolver::apply_point_loads,
+ * src/solver/linear_static.cpp:344-374): F[eq(node, d)] += scale * dir[d]. */
+int vsgb_apply_forces(int n_nodes, const int* node_ids, const int* eq6, int n_force,
+                      const int* force_node_ids, const double* scale, const double* dir,
+                      int n, double* F, char* err, size_t errlen);
+
+/* ── GPU element stiffness + assembly ───────────────────────────────────── */
+
+/* Upload a node-indexed CHEXA8 mesh and assemble K on the GPU (element
+ * stiffness, lower-triangle pattern with the value != 0.0 filter of
+ * add_element_stiffness, duplicate sums in ascending element order).
+ * node_xyz[3*n_nodes]; node_eq3[3*n_nodes] = equations of T1-T3 (-1 =
+ * constrained); conn[8*n_elem] = 0-based node indices; E, nu per element;
+ * formulation per element (NULL = all EAS).  The assembled K stays resident
+ * in the context for vsgb_solve_assembled; *nnz_lower_out receives the nnz of
+ * the reference's lower-triangle CsrData. */
+int vsgb_assemble_chexa8(vsgb_ctx* ctx, int n_nodes, const double* node_xyz,
+                         const int* node_eq3, int n_elem, const int* conn, const double* E,
+                         const double* nu, const int* formulation, int n_dof,
+                         long long* nnz_lower_out);
+
+/* Copy the resident K out as the reference's lower-triangle CsrData. */
+int vsgb_copy_csr_lower(vsgb_ctx* ctx, int* row_ptr, int* col_ind, double* values);
+
+/* Solve with the resident K: F[n*nrhs] host -> u_out[n*nrhs] host.
+ * nrhs > 1 runs the load cases as one batched PCG (one matrix sweep per
+ * iteration for all right-hand sides). */
+int vsgb_solve_assembled(vsgb_ctx* ctx, const double* F, int nrhs, double* u_out,
+                         vsgb_stats* stats);
+
+/* ── device-resident staging (inputs already in HBM) ────────────────────── */
+
+/* Upload the mesh only (no assembly). */
+int vsgb_mesh_upload(vsgb_ctx* ctx, int n_nodes, const double* node_xyz, const int* node_eq3,
+                     int n_elem, const int* conn, const double* E, const double* nu,
+                     const int* formulation, int n_dof);
+/* Element stiffness + assembly from the resident mesh (no host traffic). */
+int vsgb_assemble_resident(vsgb_ctx* ctx, long long* nnz_lower_out);
+/* Upload right-hand sides into the context (n*nrhs doubles). */
+int vsgb_rhs_upload(vsgb_ctx* ctx, const double* F, int nrhs);
+/* Solve resident K against the resident RHS; the solution stays on the GPU. */
+int vsgb_solve_resident(vsgb_ctx* ctx, vsgb_stats* stats);
+/* Download the resident solution (n*nrhs doubles). */
+int vsgb_solution_download(vsgb_ctx* ctx, double* u_out);
+
+/* ── adjoint sensitivities ──────────────────────────────────────────────── */
+
+/* dJ/dE_e = -lambda_e^T (K_e / E_e) u_e for every element of the resident
+ * mesh, given host vectors u[n] and lambda[n] (lambda solves K lambda = dJ/du;
+ * for compliance F^T u, lambda = u). */
+int vsgb_element_sensitivity(vsgb_ctx* ctx, const double* u, const double* lambda,
+                             double* dJdE_out);
+
+/* ── measurement helpers ────────────────────────────────────────────────── */
+
+/* Events on the context stream, synchronised on both sides. */
+int vsgb_timer_start(vsgb_ctx* ctx);
+int vsgb_timer_stop(vsgb_ctx* ctx, double* ms);
+/* Average device time of `reps` back-to-back launches of the resident
+ * operator's SpMV (precision VSGB_FP64 or VSGB_MIXED). */
+int vsgb_time_spmv(vsgb_ctx* ctx, int precision, int reps, double* avg_ms, double* bytes);
+/* Number of kernels this context launched since creation. */
+long long vsgb_kernel_launches(vsgb_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VSGB_H */

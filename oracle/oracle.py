@@ -1,0 +1,311 @@
+"""ctypes front end of the CPU oracle (oracle/oracle.cpp).
+
+TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT.  Only tests/,
+``__graft_entry__.smoke()`` and bench.py's CPU-baseline / reference arm import
+this module, as the checker or as the timed CPU reference.  The product
+(vibestran_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD, "liboracle.so")
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_vp = ctypes.c_void_p
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle restatement into oracle/_build/liboracle.so."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "oracle.cpp")
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["g++", "-std=c++20", "-O2", "-fopenmp", "-shared", "-fPIC",
+                           src, "-o", tmp])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        cp = ctypes.c_char_p
+        ci = ctypes.c_int
+        L.orc_num_threads.argtypes = [ci]
+        L.orc_num_threads.restype = ci
+        L.orc_chexa8_ke.argtypes = [_f64p, ctypes.c_double, ctypes.c_double, ci, _f64p, cp, ci]
+        L.orc_chexa8_ke_batch.argtypes = [ci, _f64p, _i32p, _f64p, _f64p, _i32p, _f64p, cp, ci]
+        L.orc_dof_map.argtypes = [ci, _i32p, ci, _i32p, ci, _i32p, _i32p, _i32p,
+                                  ctypes.POINTER(ci), cp, ci]
+        L.orc_dof_constrain.argtypes = [ci, _i32p, ci, _i32p, _i32p, ci, _i32p,
+                                        ctypes.POINTER(ci), cp, ci]
+        L.orc_apply_forces.argtypes = [ci, _i32p, _i32p, ci, _i32p, _f64p, _f64p, ci, _f64p,
+                                       cp, ci]
+        L.orc_assemble_dense_elements.argtypes = [ci, ci, ci, _i32p, _f64p]
+        L.orc_assemble_dense_elements.restype = _vp
+        L.orc_build_from_triplets.argtypes = [ci, ci, _i32p, _i32p, _f64p]
+        L.orc_build_from_triplets.restype = _vp
+        L.orc_assemble_chexa8.argtypes = [ci, _f64p, _i32p, ci, _i32p, _f64p, _f64p, _i32p,
+                                          ci, cp, ci]
+        L.orc_assemble_chexa8.restype = _vp
+        L.orc_csr_from_arrays.argtypes = [ci, ci, _i32p, _i32p, _f64p, ci]
+        L.orc_csr_from_arrays.restype = _vp
+        L.orc_csr_info.argtypes = [_vp, ctypes.POINTER(ci), ctypes.POINTER(ci),
+                                   ctypes.POINTER(ci)]
+        L.orc_csr_copy.argtypes = [_vp, _i32p, _i32p, _f64p]
+        L.orc_csr_free.argtypes = [_vp]
+        L.orc_csr_expand.argtypes = [_vp]
+        L.orc_csr_expand.restype = _vp
+        L.orc_csr_lower.argtypes = [_vp]
+        L.orc_csr_lower.restype = _vp
+        L.orc_csr_multiply.argtypes = [_vp, _f64p, _f64p]
+        L.orc_pcg_jacobi.argtypes = [_vp, _f64p, ctypes.c_double, ci, ci, _f64p,
+                                     ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_double), cp, ci]
+        L.orc_pcg_mixed.argtypes = [_vp, _f64p, ctypes.c_double, ci, _f64p, ctypes.POINTER(ci),
+                                    ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_double), cp, ci]
+        L.orc_dense_cholesky_solve.argtypes = [_vp, _f64p, _f64p, cp, ci]
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _err():
+    return ctypes.create_string_buffer(512)
+
+
+def set_threads(n: int) -> int:
+    return lib().orc_num_threads(int(n))
+
+
+@dataclass
+class Csr:
+    """CSR in the reference's CsrData layout (include/core/sparse_matrix.hpp:63-87)."""
+    row_ptr: np.ndarray
+    col_ind: np.ndarray
+    values: np.ndarray
+    n: int
+    nnz: int
+    lower: bool
+
+    def handle(self):
+        return _CsrHandle(lib().orc_csr_from_arrays(
+            self.n, self.nnz, np.ascontiguousarray(self.row_ptr, np.int32),
+            np.ascontiguousarray(self.col_ind, np.int32),
+            np.ascontiguousarray(self.values, np.float64), int(self.lower)))
+
+    def multiply(self, x):
+        with self.handle() as h:
+            y = np.zeros(self.n)
+            lib().orc_csr_multiply(h.ptr, np.ascontiguousarray(x, np.float64), y)
+            return y
+
+    def expanded_symmetric(self) -> "Csr":
+        with self.handle() as h:
+            return _take(lib().orc_csr_expand(h.ptr))
+
+    def lower_triangle(self) -> "Csr":
+        with self.handle() as h:
+            return _take(lib().orc_csr_lower(h.ptr))
+
+    def to_dense(self) -> np.ndarray:
+        A = np.zeros((self.n, self.n))
+        rows = np.repeat(np.arange(self.n), np.diff(self.row_ptr))
+        np.add.at(A, (rows, self.col_ind), self.values)
+        if self.lower:
+            A = A + np.tril(A, -1).T
+        return A
+
+
+class _CsrHandle:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        lib().orc_csr_free(self.ptr)
+
+
+def _take(ptr) -> Csr:
+    if not ptr:
+        raise OracleError("null CSR handle")
+    L = lib()
+    n, nnz, lower = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    L.orc_csr_info(ptr, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(lower))
+    rp = np.empty(n.value + 1, np.int32)
+    ci = np.empty(nnz.value, np.int32)
+    v = np.empty(nnz.value, np.float64)
+    L.orc_csr_copy(ptr, rp, ci, v)
+    L.orc_csr_free(ptr)
+    return Csr(rp, ci, v, n.value, nnz.value, bool(lower.value))
+
+
+def chexa8_ke(xyz24, E, nu, formulation=0) -> np.ndarray:
+    ke = np.zeros(576)
+    err = _err()
+    if lib().orc_chexa8_ke(np.ascontiguousarray(xyz24, np.float64).reshape(-1), float(E),
+                           float(nu), int(formulation), ke, err, 512) != 0:
+        raise OracleError(err.value.decode())
+    return ke.reshape(24, 24)
+
+
+def chexa8_ke_batch(model) -> np.ndarray:
+    out = np.zeros((model.n_elem, 576))
+    err = _err()
+    if lib().orc_chexa8_ke_batch(model.n_elem, np.ascontiguousarray(model.xyz),
+                                 np.ascontiguousarray(model.conn, np.int32), model.E, model.nu,
+                                 np.ascontiguousarray(model.form, np.int32), out, err, 512) != 0:
+        raise OracleError(err.value.decode())
+    return out.reshape(model.n_elem, 24, 24)
+
+
+def dof_map(model):
+    """(eq6 (N,6) int32 in model node order, n_free)."""
+    eq = np.empty(model.n_nodes * 6, np.int32)
+    nf = ctypes.c_int()
+    err = _err()
+    rc = lib().orc_dof_map(model.n_nodes, np.ascontiguousarray(model.node_ids, np.int32),
+                           model.n_elem, np.ascontiguousarray(model.conn_ids(), np.int32),
+                           int(model.spc_nodes.shape[0]),
+                           np.ascontiguousarray(model.spc_nodes, np.int32),
+                           np.ascontiguousarray(model.spc_mask, np.int32), eq,
+                           ctypes.byref(nf), err, 512)
+    if rc != 0:
+        raise OracleError(err.value.decode())
+    return eq.reshape(-1, 6), nf.value
+
+
+def dof_constrain(node_ids, pairs, batch: bool):
+    ids = np.ascontiguousarray(node_ids, np.int32)
+    cn = np.ascontiguousarray([p[0] for p in pairs], np.int32)
+    cd = np.ascontiguousarray([p[1] for p in pairs], np.int32)
+    eq = np.empty(ids.shape[0] * 6, np.int32)
+    nf = ctypes.c_int()
+    err = _err()
+    if lib().orc_dof_constrain(ids.shape[0], ids, cn.shape[0], cn, cd, 1 if batch else 0, eq,
+                               ctypes.byref(nf), err, 512) != 0:
+        raise OracleError(err.value.decode())
+    return eq.reshape(-1, 6), nf.value
+
+
+def apply_forces(model, eq6, n, load_index=0):
+    nodes, scale, dirs = model.loads[load_index]
+    F = np.zeros(n)
+    err = _err()
+    if lib().orc_apply_forces(model.n_nodes, np.ascontiguousarray(model.node_ids, np.int32),
+                              np.ascontiguousarray(eq6, np.int32).reshape(-1),
+                              int(len(nodes)), np.ascontiguousarray(nodes, np.int32),
+                              np.ascontiguousarray(scale, np.float64),
+                              np.ascontiguousarray(dirs, np.float64).reshape(-1), n, F,
+                              err, 512) != 0:
+        raise OracleError(err.value.decode())
+    return F
+
+
+def assemble_chexa8(model, eq6, n) -> Csr:
+    err = _err()
+    ptr = lib().orc_assemble_chexa8(model.n_nodes, np.ascontiguousarray(model.xyz),
+                                    np.ascontiguousarray(eq6, np.int32).reshape(-1),
+                                    model.n_elem, np.ascontiguousarray(model.conn, np.int32),
+                                    model.E, model.nu, np.ascontiguousarray(model.form, np.int32),
+                                    n, err, 512)
+    if not ptr:
+        raise OracleError(err.value.decode())
+    return _take(ptr)
+
+
+def assemble_dense_elements(n, gdofs, kes) -> Csr:
+    gdofs = np.ascontiguousarray(gdofs, np.int32)
+    kes = np.ascontiguousarray(kes, np.float64)
+    ne, nd = gdofs.shape
+    return _take(lib().orc_assemble_dense_elements(n, ne, nd, gdofs.reshape(-1),
+                                                    kes.reshape(-1)))
+
+
+def build_from_triplets(n, rows, cols, vals) -> Csr:
+    r = np.ascontiguousarray(rows, np.int32)
+    return _take(lib().orc_build_from_triplets(n, r.shape[0], r,
+                                               np.ascontiguousarray(cols, np.int32),
+                                               np.ascontiguousarray(vals, np.float64)))
+
+
+def pcg_jacobi(K: Csr, F, tol=1e-8, max_iters=10000, precision=64):
+    u = np.zeros(K.n)
+    it = ctypes.c_int()
+    rel = ctypes.c_double()
+    err = _err()
+    with K.handle() as h:
+        rc = lib().orc_pcg_jacobi(h.ptr, np.ascontiguousarray(F, np.float64), float(tol),
+                                  int(max_iters), int(precision), u, ctypes.byref(it),
+                                  ctypes.byref(rel), err, 512)
+    if rc != 0:
+        raise OracleError(err.value.decode())
+    return u, it.value, rel.value
+
+
+def pcg_mixed(K: Csr, F, tol=1e-6, max_iters=10000):
+    u = np.zeros(K.n)
+    it = ctypes.c_int()
+    ns = ctypes.c_int()
+    rel = ctypes.c_double()
+    err = _err()
+    with K.handle() as h:
+        rc = lib().orc_pcg_mixed(h.ptr, np.ascontiguousarray(F, np.float64), float(tol),
+                                 int(max_iters), u, ctypes.byref(it), ctypes.byref(ns),
+                                 ctypes.byref(rel), err, 512)
+    if rc != 0:
+        raise OracleError(err.value.decode())
+    return u, it.value, ns.value, rel.value
+
+
+def direct_solve(K: Csr, F):
+    """FP64 direct solve: dense LLT up to n = 20000 (the --backend=cpu stand-in)."""
+    u = np.zeros(K.n)
+    err = _err()
+    with K.handle() as h:
+        if lib().orc_dense_cholesky_solve(h.ptr, np.ascontiguousarray(F, np.float64), u, err,
+                                          512) != 0:
+            raise OracleError(err.value.decode())
+    return u
+
+
+def sparse_direct_solve(K: Csr, F):
+    """FP64 sparse direct solve (SuperLU via scipy) for sizes a dense factor cannot take."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    full = K.expanded_symmetric() if K.lower else K
+    A = sp.csc_matrix(sp.csr_matrix((full.values, full.col_ind, full.row_ptr),
+                                    shape=(K.n, K.n)))
+    return spla.spsolve(A, np.asarray(F, np.float64), permc_spec="MMD_AT_PLUS_A")
+
+
+def solve_model(model, tol=None, load_index=0, direct=True):
+    """Whole oracle pipeline for a model: DOF map, assembly, forces, solve."""
+    eq6, n = dof_map(model)
+    K = assemble_chexa8(model, eq6, n)
+    F = apply_forces(model, eq6, n, load_index)
+    if direct:
+        u = direct_solve(K, F) if n <= 6000 else sparse_direct_solve(K, F)
+    else:
+        u, _, _ = pcg_jacobi(K, F, tol or 1e-10, 100000)
+    return eq6, n, K, F, u

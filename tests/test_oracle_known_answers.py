@@ -1,0 +1,187 @@
+"""Pin the CPU oracle against the reference's own known answers (no GPU)."""
+import numpy as np
+import pytest
+
+from conftest import banded500, model_from_spec, tridiagonal
+
+
+def _disp(eq6, node_ids, u, nid, d):
+    i = int(np.where(node_ids == nid)[0][0])
+    e = eq6[i, d]
+    return 0.0 if e < 0 else u[e]
+
+
+def test_hexa_bar_axial_extension(oracle, known):
+    spec = known["hexa_bar_axial_extension"]
+    m = model_from_spec(spec)
+    eq6, n, K, F, u = oracle.solve_model(m)
+    ex = spec["expect"]
+    for nid in ex["uz_top_nodes"]:
+        assert abs(_disp(eq6, m.node_ids, u, nid, 2) - ex["uz"]) < ex["abs_tol"]
+    assert abs(_disp(eq6, m.node_ids, u, 6, 0) - ex["ux_node6"]) < ex["abs_tol"]
+
+
+def test_eas_softer_than_sri_nearly_incompressible(oracle, known):
+    spec = known["hexa_eas_vs_sri_bending_nearly_incompressible"]
+    u5 = {}
+    for isop in (0, 1):
+        m = model_from_spec(spec, isop)
+        eq6, n, K, F, u = oracle.solve_model(m)
+        u5[isop] = _disp(eq6, m.node_ids, u, 5, 0)
+    G = spec["E"] / (2.0 * (1.0 + spec["nu"]))
+    assert u5[1] > 0 and u5[0] > 0
+    assert u5[0] > u5[1]
+    assert u5[0] > 0.1 * 250.0 / G
+
+
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("nu", [0.3, 0.4999])
+def test_chexa8_symmetric_psd(oracle, form, nu):
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                    [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    ke = oracle.chexa8_ke(xyz, 1e6, nu, form)
+    assert np.abs(ke - ke.T).max() < 1e-10 * np.abs(ke).max()
+    ev = np.linalg.eigvalsh(0.5 * (ke + ke.T))
+    assert ev.min() >= -1e-6 * ev.max()
+    # six rigid-body modes, no spurious zero-energy modes
+    assert np.sum(ev < 1e-9 * ev.max()) == 6
+
+
+def test_chexa8_bad_jacobian(oracle):
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                    [0, 0, -1], [1, 0, -1], [1, 1, -1], [0, 1, -1]], float)
+    with pytest.raises(oracle.OracleError, match="non-positive"):
+        oracle.chexa8_ke(xyz, 1e6, 0.3, 0)
+
+
+def test_csr_element_assembly_lower(oracle, known):
+    c = known["csr_element_assembly_lower"]
+    K = oracle.assemble_dense_elements(c["n"], [c["dofs"]], [c["ke"]])
+    ex = c["expect"]
+    assert K.lower == ex["lower"] and K.nnz == ex["nnz"]
+    assert K.row_ptr.tolist() == ex["row_ptr"]
+    assert K.col_ind.tolist() == ex["col_ind"]
+    assert K.values.tolist() == ex["values"]
+    mv = known["csr_lower_matvec"]
+    assert K.multiply(np.array(mv["x"])).tolist() == mv["expect"]["y"]
+    full = K.expanded_symmetric()
+    assert full.nnz == mv["expect"]["full_nnz"] and not full.lower
+    assert full.multiply(np.array(mv["x"])).tolist() == mv["expect"]["y"]
+
+
+def test_csr_merge_and_lower_extraction(oracle, known):
+    for key in ("csr_merge_duplicates", "csr_lower_extraction"):
+        c = known[key]
+        t = c["triplets"]
+        K = oracle.build_from_triplets(c["n"], [x[0] for x in t], [x[1] for x in t],
+                                       [x[2] for x in t])
+        if key == "csr_lower_extraction":
+            assert not K.lower
+            K = K.lower_triangle()
+            assert K.lower
+        ex = c["expect"]
+        assert K.nnz == ex["nnz"]
+        assert K.row_ptr.tolist() == ex["row_ptr"]
+        assert K.col_ind.tolist() == ex["col_ind"]
+        assert K.values.tolist() == ex["values"]
+
+
+def test_dofmap_batch_equals_serial(oracle, known):
+    c = known["dofmap_batch_equals_serial"]
+    a, na = oracle.dof_constrain(c["nodes"], c["constraints"], batch=False)
+    b, nb = oracle.dof_constrain(c["nodes"], c["constraints"], batch=True)
+    assert na == nb == 24 - 8
+    assert np.array_equal(a, b)
+    d = known["dofmap_duplicates"]
+    e, ne = oracle.dof_constrain(d["nodes"], d["constraints"], batch=True)
+    assert ne == d["expect"]["num_free"]
+    assert e[0, 0] == -1 and e[0, 1] == -1 and e[0, 2] != -1
+    s = known["dofmap_shift"]
+    e0, n0 = oracle.dof_constrain(s["nodes"], [], batch=True)
+    e1, n1 = oracle.dof_constrain(s["nodes"], [(1, 0)], batch=False)
+    assert n0 == s["expect"]["num_free_before"] and n1 == s["expect"]["after_constrain_node1_T1"]
+    assert e1[1, 0] == e0[1, 0] + s["expect"]["node2_T1_shift"]
+
+
+def test_pcg_conformance_cases_on_oracle(oracle, known):
+    # The CudaPCGTest cases (test_pcg_solver.cpp:269-425) against the oracle's
+    # FP64 Jacobi PCG, which the GPU backend is later compared to.
+    K = oracle.build_from_triplets(2, [0, 1], [0, 1], [4.0, 9.0])
+    u, it, rel = oracle.pcg_jacobi(K, [8.0, 27.0], 1e-8)
+    assert np.allclose(u, [2.0, 3.0], atol=1e-7) and it <= 1
+    for n, d, off, lower, tol in [(5, 3.0, -1.0, False, 1e-6), (8, 3.0, -1.0, True, 1e-6),
+                                  (200, 2.0, -1.0, False, 1e-5)]:
+        K = tridiagonal(n, d, off, lower)
+        F = np.ones(n)
+        u, it, rel = oracle.pcg_jacobi(K, F, 1e-8)
+        ud = oracle.direct_solve(K, F)
+        assert np.abs(u - ud).max() < tol
+    K = oracle.build_from_triplets(100, list(range(100)), list(range(100)), [1.3e9] * 100)
+    u, it, rel = oracle.pcg_jacobi(K, np.full(100, 333.0), 1e-8)
+    assert np.allclose(u, 333.0 / 1.3e9, rtol=1e-6)
+    K = tridiagonal(10, 3.0, -1.0)
+    u, it, rel = oracle.pcg_jacobi(K, np.zeros(10), 1e-8)
+    assert it == 0 and np.abs(u).max() == 0.0
+    K, F = banded500()
+    u, it, rel = oracle.pcg_jacobi(K, F, 1e-8)
+    assert np.abs(u - oracle.direct_solve(K, F)).max() < 1e-5
+    K = tridiagonal(200, 2.0, -1.0)
+    u, it, ns, rel = oracle.pcg_mixed(K, np.ones(200), 1e-6)
+    assert np.abs(u - oracle.direct_solve(K, np.ones(200))).max() < 5e-3 and rel < 1e-4
+
+
+def test_pcg_error_semantics(oracle):
+    K = oracle.build_from_triplets(3, [0, 1, 2], [0, 1, 2], [1.0, 0.0, 1.0])
+    with pytest.raises(oracle.OracleError, match="zero diagonal at row 1"):
+        oracle.pcg_jacobi(K, np.ones(3))
+    K = oracle.build_from_triplets(3, [0, 2, 1], [0, 2, 0], [1.0, 1.0, 0.5])
+    with pytest.raises(oracle.OracleError, match="missing diagonal at row 1"):
+        oracle.pcg_jacobi(K, np.ones(3))
+    K = tridiagonal(200, 2.0, -1.0)
+    with pytest.raises(oracle.OracleError, match="did not converge after 3 iterations"):
+        oracle.pcg_jacobi(K, np.ones(200), 1e-8, 3)
+
+
+def test_cantilever_1500_sizes_and_solution(oracle):
+    from vibestran_gb300 import cantilever as C
+    m = C.cantilever_1500()
+    eq6, n, K, F, u = oracle.solve_model(m)
+    assert m.n_nodes == 525 and n == 1500
+    assert K.nnz == 44859 and K.lower
+    assert K.expanded_symmetric().nnz == 88218
+    up, it, rel = oracle.pcg_jacobi(K, F, 1e-10)
+    assert np.linalg.norm(up - u) / np.linalg.norm(u) < 1e-8
+    # Euler-Bernoulli tip deflection F L^3/(3 E I) = 1.25e-5 m, shear + EAS
+    # corrections within a few percent.
+    tip = [e for i, e in enumerate(eq6[:, 2]) if e >= 0 and (m.node_ids[i] - 1) // 25 == 20]
+    assert 1.2e-5 < -np.mean(u[tip]) < 1.35e-5
+
+
+def test_golden_oracle_fixture(oracle):
+    """Regression fixture of oracle outputs (tests/golden/make_golden.py)."""
+    import json
+    import os
+
+    from conftest import GOLDEN
+    from vibestran_gb300 import cantilever as C
+    with open(os.path.join(GOLDEN, "oracle_fixtures.json")) as fh:
+        g = json.load(fh)
+    for name, rec in g["elements"].items():
+        ke = oracle.chexa8_ke(np.array(rec["xyz"]), rec["E"], rec["nu"], rec["form"])
+        ref = np.array(rec["ke"]).reshape(24, 24)
+        assert np.abs(ke - ref).max() <= 1e-13 * np.abs(ref).max(), name
+    c1 = g["cantilever_1500"]
+    m = C.cantilever_1500()
+    eq6, n, K, F, u = oracle.solve_model(m)
+    assert n == c1["n"] and K.nnz == c1["nnz_lower"]
+    assert C_hash(K) == c1["pattern_sha256"]
+    assert np.abs(np.array(c1["u_head"]) - u[:len(c1["u_head"])]).max() <= 1e-12 * np.abs(u).max()
+    assert abs(np.linalg.norm(u) - c1["u_norm"]) <= 1e-12 * c1["u_norm"]
+
+
+def C_hash(K):
+    import hashlib
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(K.row_ptr, np.int32).tobytes())
+    h.update(np.ascontiguousarray(K.col_ind, np.int32).tobytes())
+    return h.hexdigest()

@@ -1,0 +1,404 @@
+"""Host-side mirror of vibestran's SolverBackend over the libvsgb C ABI.
+
+The classes follow the reference's interface for this path:
+
+* :class:`CsrData` — ``SparseMatrixBuilder::CsrData``
+  (include/core/sparse_matrix.hpp:63-87): row_ptr / col_ind / values, n, nnz
+  and the symmetry tag (lower-triangle or full storage).
+* :class:`Gb300PcgSolverBackend` — a drop-in for ``CudaPCGSolverBackend``
+  (include/solver/cuda_pcg_solver_backend.hpp:33-75): ``try_create`` returns
+  ``None`` when no usable GPU exists, ``solve`` raises :class:`SolverError`
+  with the reference's messages, and the diagnostics accessors match.
+* :class:`Gb300MixedPcgSolverBackend` — ``CudaMixedPCGSolverBackend``
+  (include/solver/cuda_mixed_pcg_solver_backend.hpp), with the refinement
+  residual, update and norms kept in FP64 on the GPU.
+* :class:`ChexaAssembler` — GPU element stiffness + assembly for a CHEXA8
+  model (the layers above ``SolverBackend::solve`` in
+  src/solver/linear_static.cpp:233-260).
+
+Every numeric call goes through ``libvsgb.so``; there is no CPU fallback —
+importing on a machine without the built library raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+VSGB_OK = 0
+VSGB_ERR_INVALID = -1
+VSGB_ERR_SINGULAR = -2
+VSGB_ERR_NOT_CONVERGED = -3
+VSGB_ERR_CUDA = -4
+VSGB_ERR_ELEMENT = -5
+VSGB_ERR_NO_DEVICE = -6
+VSGB_ERR_STATE = -7
+VSGB_ERR_LIMIT = -8
+
+FP64 = 64
+MIXED = 32
+EAS = 0
+SRI = 1
+
+OPT_TOLERANCE = 1
+OPT_MAX_ITERS = 2
+OPT_PRECISION = 3
+OPT_INNER_TOL = 4
+OPT_MAX_SOLVES = 5
+OPT_CHECK_EVERY = 6
+OPT_USE_GRAPH = 7
+OPT_FORMAT = 8
+
+# The symbols include/vsgb.h declares (checked by tests against the .so).
+EXPORTS = (
+    "vsgb_create", "vsgb_destroy", "vsgb_set_option", "vsgb_last_error", "vsgb_device_name",
+    "vsgb_backend_name", "vsgb_solve_csr", "vsgb_build_dof_map", "vsgb_apply_forces",
+    "vsgb_assemble_chexa8", "vsgb_copy_csr_lower", "vsgb_solve_assembled", "vsgb_mesh_upload",
+    "vsgb_assemble_resident", "vsgb_rhs_upload", "vsgb_solve_resident",
+    "vsgb_solution_download", "vsgb_element_sensitivity", "vsgb_timer_start",
+    "vsgb_timer_stop", "vsgb_time_spmv", "vsgb_kernel_launches",
+)
+
+
+class SolverError(RuntimeError):
+    """vibestran::SolverError (include/core/exceptions.hpp:14)."""
+
+    def __init__(self, msg: str, code: int = VSGB_ERR_INVALID):
+        super().__init__(msg)
+        self.code = code
+
+
+class VsgbStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("inner_solves", ctypes.c_int),
+                ("converged", ctypes.c_int), ("format", ctypes.c_int),
+                ("rel_residual", ctypes.c_double), ("solve_ms", ctypes.c_double),
+                ("setup_ms", ctypes.c_double), ("spmv_bytes", ctypes.c_double)]
+
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load_library(build_if_missing: bool = False):
+    """Load libvsgb.so (raises if it was not built — no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError(f"libvsgb.so is not built ({path}); run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    c_int, c_dbl, c_ll = ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+    vp, cp, sz = ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t
+    L.vsgb_create.argtypes = [c_int, c_dbl, c_int, c_int, ctypes.POINTER(vp)]
+    L.vsgb_destroy.argtypes = [vp]
+    L.vsgb_destroy.restype = None
+    L.vsgb_set_option.argtypes = [vp, c_int, c_dbl]
+    L.vsgb_last_error.argtypes = [vp, cp, sz]
+    L.vsgb_device_name.argtypes = [vp, cp, sz]
+    L.vsgb_backend_name.argtypes = [vp, cp, sz]
+    L.vsgb_solve_csr.argtypes = [vp, c_int, c_int, _i32p, _i32p, _f64p, c_int, _f64p, c_int,
+                                 _f64p, ctypes.POINTER(VsgbStats)]
+    L.vsgb_build_dof_map.argtypes = [c_int, _i32p, c_int, _i32p, c_int, _i32p, _i32p, _i32p,
+                                     ctypes.POINTER(c_int), cp, sz]
+    L.vsgb_apply_forces.argtypes = [c_int, _i32p, _i32p, c_int, _i32p, _f64p, _f64p, c_int,
+                                    _f64p, cp, sz]
+    L.vsgb_assemble_chexa8.argtypes = [vp, c_int, _f64p, _i32p, c_int, _i32p, _f64p, _f64p, vp,
+                                       c_int, ctypes.POINTER(c_ll)]
+    L.vsgb_mesh_upload.argtypes = [vp, c_int, _f64p, _i32p, c_int, _i32p, _f64p, _f64p, vp, c_int]
+    L.vsgb_assemble_resident.argtypes = [vp, ctypes.POINTER(c_ll)]
+    L.vsgb_copy_csr_lower.argtypes = [vp, _i32p, _i32p, _f64p]
+    L.vsgb_solve_assembled.argtypes = [vp, _f64p, c_int, _f64p, ctypes.POINTER(VsgbStats)]
+    L.vsgb_rhs_upload.argtypes = [vp, _f64p, c_int]
+    L.vsgb_solve_resident.argtypes = [vp, ctypes.POINTER(VsgbStats)]
+    L.vsgb_solution_download.argtypes = [vp, _f64p]
+    L.vsgb_element_sensitivity.argtypes = [vp, _f64p, _f64p, _f64p]
+    L.vsgb_timer_start.argtypes = [vp]
+    L.vsgb_timer_stop.argtypes = [vp, ctypes.POINTER(c_dbl)]
+    L.vsgb_time_spmv.argtypes = [vp, c_int, c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)]
+    L.vsgb_kernel_launches.argtypes = [vp]
+    L.vsgb_kernel_launches.restype = c_ll
+    _lib = L
+    return L
+
+
+@dataclass
+class CsrData:
+    """SparseMatrixBuilder::CsrData: lower-triangle (``lower=True``) or full storage."""
+    row_ptr: np.ndarray
+    col_ind: np.ndarray
+    values: np.ndarray
+    n: int
+    nnz: int
+    lower: bool = True
+
+    def stores_lower_triangle_only(self) -> bool:
+        return self.lower
+
+
+class _Context:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def check(self, rc: int):
+        if rc != VSGB_OK:
+            raise SolverError(self.last_error(), rc)
+
+    def last_error(self) -> str:
+        buf = ctypes.create_string_buffer(1024)
+        load_library().vsgb_last_error(self.ptr, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def close(self):
+        if self.ptr:
+            load_library().vsgb_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _create(device: int, tol: float, max_iters: int, precision: int):
+    L = load_library()
+    p = ctypes.c_void_p()
+    rc = L.vsgb_create(device, float(tol), int(max_iters), precision, ctypes.byref(p))
+    if rc == VSGB_ERR_NO_DEVICE:
+        return None
+    if rc != VSGB_OK:
+        raise SolverError(f"vsgb_create failed with status {rc}", rc)
+    return _Context(p)
+
+
+class Gb300PcgSolverBackend:
+    """Drop-in for CudaPCGSolverBackend (FP64 Jacobi PCG on sm_103a)."""
+
+    precision = FP64
+
+    def __init__(self, ctx: _Context):
+        self._ctx = ctx
+        self._iters = 0
+        self._rel = 0.0
+        self.last_stats = VsgbStats()
+
+    @classmethod
+    def try_create(cls, tolerance: float = 0.0, max_iters: int = 0, device: int = 0):
+        """None when no CUDA device (cuda_pcg_solver_backend.cu:19-25)."""
+        ctx = _create(device, tolerance, max_iters, cls.precision)
+        return None if ctx is None else cls(ctx)
+
+    def set_option(self, option: int, value: float):
+        self._ctx.check(load_library().vsgb_set_option(self._ctx.ptr, option, float(value)))
+
+    def solve(self, K: CsrData, F, factor_ratio_policy=None) -> np.ndarray:
+        """SolverBackend::solve: K as CsrData, F (n,) or (n, nrhs) -> u."""
+        F = np.asarray(F, dtype=np.float64)
+        if K.n == 0:
+            raise SolverError("CUDA PCG: stiffness matrix is empty -- no free DOFs")
+        if F.shape[0] != K.n:
+            raise SolverError(f"CUDA PCG: force vector size {F.shape[0]} != matrix size {K.n}")
+        nrhs = 1 if F.ndim == 1 else F.shape[1]
+        Fc = np.ascontiguousarray(F.T if F.ndim == 2 else F).reshape(-1)
+        u = np.zeros(K.n * nrhs)
+        st = VsgbStats()
+        rc = load_library().vsgb_solve_csr(
+            self._ctx.ptr, int(K.n), int(K.nnz), np.ascontiguousarray(K.row_ptr, np.int32),
+            np.ascontiguousarray(K.col_ind, np.int32), np.ascontiguousarray(K.values, np.float64),
+            1 if K.lower else 0, Fc, nrhs, u, ctypes.byref(st))
+        self._ctx.check(rc)
+        self._record(st)
+        return u if nrhs == 1 else u.reshape(nrhs, K.n).T.copy()
+
+    def _record(self, st: VsgbStats):
+        self.last_stats = st
+        self._iters = st.iterations
+        self._rel = st.rel_residual
+
+    def name(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        load_library().vsgb_backend_name(self._ctx.ptr, buf, 256)
+        return buf.value.decode()
+
+    def device_name(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        load_library().vsgb_device_name(self._ctx.ptr, buf, 256)
+        return buf.value.decode()
+
+    def last_iteration_count(self) -> int:
+        return self._iters
+
+    def last_relative_residual(self) -> float:
+        return self._rel
+
+    def last_estimated_error(self) -> float:
+        return self._rel
+
+    def requires_full_symmetric_csr(self) -> bool:
+        return False
+
+    def kernel_launches(self) -> int:
+        return int(load_library().vsgb_kernel_launches(self._ctx.ptr))
+
+    @property
+    def context(self) -> _Context:
+        return self._ctx
+
+    def close(self):
+        self._ctx.close()
+
+
+class Gb300MixedPcgSolverBackend(Gb300PcgSolverBackend):
+    """Drop-in for CudaMixedPCGSolverBackend (default tolerance 1e-6)."""
+
+    precision = MIXED
+
+
+def build_dof_map(model):
+    """Analysis DOF map through the library (host C++): (eq6 (N,6), n_free)."""
+    L = load_library()
+    eq = np.empty(model.n_nodes * 6, np.int32)
+    nf = ctypes.c_int()
+    err = ctypes.create_string_buffer(512)
+    rc = L.vsgb_build_dof_map(model.n_nodes, np.ascontiguousarray(model.node_ids, np.int32),
+                              model.n_elem, np.ascontiguousarray(model.conn_ids(), np.int32).reshape(-1),
+                              int(model.spc_nodes.shape[0]),
+                              np.ascontiguousarray(model.spc_nodes, np.int32),
+                              np.ascontiguousarray(model.spc_mask, np.int32), eq,
+                              ctypes.byref(nf), err, 512)
+    if rc != VSGB_OK:
+        raise SolverError(err.value.decode(), rc)
+    return eq.reshape(-1, 6), nf.value
+
+
+def apply_forces(model, eq6, n, load_index=0):
+    nodes, scale, dirs = model.loads[load_index]
+    F = np.zeros(n)
+    err = ctypes.create_string_buffer(512)
+    rc = load_library().vsgb_apply_forces(
+        model.n_nodes, np.ascontiguousarray(model.node_ids, np.int32),
+        np.ascontiguousarray(eq6, np.int32).reshape(-1), int(len(nodes)),
+        np.ascontiguousarray(nodes, np.int32), np.ascontiguousarray(scale, np.float64),
+        np.ascontiguousarray(dirs, np.float64).reshape(-1), int(n), F, err, 512)
+    if rc != VSGB_OK:
+        raise SolverError(err.value.decode(), rc)
+    return F
+
+
+class ChexaAssembler:
+    """GPU CHEXA8 element stiffness + assembly bound to a backend context.
+
+    ``assemble(model, eq6, n)`` uploads the mesh and assembles K on the GPU;
+    ``csr_lower()`` returns the reference's lower-triangle CsrData;
+    ``solve(F)`` solves with the resident K (F may hold several load cases).
+    """
+
+    def __init__(self, backend: Gb300PcgSolverBackend):
+        self.backend = backend
+        self.n = 0
+        self.nnz_lower = 0
+        self.n_elem = 0
+
+    def upload(self, model, eq6, n):
+        L = load_library()
+        eq3 = np.ascontiguousarray(np.asarray(eq6)[:, :3], np.int32).reshape(-1)
+        form = np.ascontiguousarray(model.form, np.int32)
+        rc = L.vsgb_mesh_upload(self.backend.context.ptr, model.n_nodes,
+                                np.ascontiguousarray(model.xyz, np.float64).reshape(-1), eq3,
+                                model.n_elem, np.ascontiguousarray(model.conn, np.int32).reshape(-1),
+                                np.ascontiguousarray(model.E, np.float64),
+                                np.ascontiguousarray(model.nu, np.float64),
+                                form.ctypes.data_as(ctypes.c_void_p), int(n))
+        self.backend.context.check(rc)
+        self.n = int(n)
+        self.n_elem = model.n_elem
+
+    def assemble_resident(self) -> int:
+        nnz = ctypes.c_longlong()
+        self.backend.context.check(
+            load_library().vsgb_assemble_resident(self.backend.context.ptr, ctypes.byref(nnz)))
+        self.nnz_lower = int(nnz.value)
+        return self.nnz_lower
+
+    def assemble(self, model, eq6, n) -> int:
+        self.upload(model, eq6, n)
+        return self.assemble_resident()
+
+    def csr_lower(self) -> CsrData:
+        rp = np.empty(self.n + 1, np.int32)
+        ci = np.empty(self.nnz_lower, np.int32)
+        v = np.empty(self.nnz_lower, np.float64)
+        self.backend.context.check(
+            load_library().vsgb_copy_csr_lower(self.backend.context.ptr, rp, ci, v))
+        return CsrData(rp, ci, v, self.n, self.nnz_lower, True)
+
+    def solve(self, F) -> np.ndarray:
+        F = np.asarray(F, dtype=np.float64)
+        nrhs = 1 if F.ndim == 1 else F.shape[1]
+        Fc = np.ascontiguousarray(F.T if F.ndim == 2 else F).reshape(-1)
+        u = np.zeros(self.n * nrhs)
+        st = VsgbStats()
+        self.backend.context.check(load_library().vsgb_solve_assembled(
+            self.backend.context.ptr, Fc, nrhs, u, ctypes.byref(st)))
+        self.backend._record(st)
+        return u if nrhs == 1 else u.reshape(nrhs, self.n).T.copy()
+
+    def upload_rhs(self, F):
+        F = np.asarray(F, dtype=np.float64)
+        nrhs = 1 if F.ndim == 1 else F.shape[1]
+        Fc = np.ascontiguousarray(F.T if F.ndim == 2 else F).reshape(-1)
+        self.backend.context.check(
+            load_library().vsgb_rhs_upload(self.backend.context.ptr, Fc, nrhs))
+        self._nrhs = nrhs
+
+    def solve_resident(self) -> VsgbStats:
+        st = VsgbStats()
+        self.backend.context.check(
+            load_library().vsgb_solve_resident(self.backend.context.ptr, ctypes.byref(st)))
+        self.backend._record(st)
+        return st
+
+    def download(self) -> np.ndarray:
+        nrhs = getattr(self, "_nrhs", 1)
+        u = np.zeros(self.n * nrhs)
+        self.backend.context.check(
+            load_library().vsgb_solution_download(self.backend.context.ptr, u))
+        return u if nrhs == 1 else u.reshape(nrhs, self.n).T.copy()
+
+    def sensitivity(self, u, lam) -> np.ndarray:
+        out = np.zeros(self.n_elem)
+        self.backend.context.check(load_library().vsgb_element_sensitivity(
+            self.backend.context.ptr, np.ascontiguousarray(u, np.float64),
+            np.ascontiguousarray(lam, np.float64), out))
+        return out
+
+
+def timer_start(backend):
+    backend.context.check(load_library().vsgb_timer_start(backend.context.ptr))
+
+
+def timer_stop(backend) -> float:
+    ms = ctypes.c_double()
+    backend.context.check(load_library().vsgb_timer_stop(backend.context.ptr, ctypes.byref(ms)))
+    return ms.value
+
+
+def time_spmv(backend, precision: int, reps: int = 50):
+    ms = ctypes.c_double()
+    by = ctypes.c_double()
+    backend.context.check(load_library().vsgb_time_spmv(backend.context.ptr, precision, reps,
+                                                        ctypes.byref(ms), ctypes.byref(by)))
+    return ms.value, by.value

@@ -1,0 +1,509 @@
+// vibestran_gb300/csrc/api.cu — C ABI (include/vsgb.h): context, solve, assembly.
+//
+// The context mirrors CudaPCGContext (src/solver/cuda_pcg_backend_impl.hpp:2031-2065):
+// device, tolerance, max iterations, last iteration count / residual, device
+// name — plus the resident mesh, the assembled operator and the PCG engine.
+// Error texts follow the reference's SolverError messages so a C++ wrapper can
+// rethrow them unchanged.
+
+#include <climits>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "pcg.cuh"
+
+using vsgb::DevBuf;
+using vsgb::Error;
+
+struct vsgb_ctx {
+  int device = 0;
+  int num_sms = 152;
+  cudaStream_t stream = nullptr;
+  std::string device_name;
+  std::string last_error;
+  double tol = 1e-8;
+  int max_iters = 10000;
+  int precision = VSGB_FP64;
+  double inner_tol = 0.0;
+  int max_solves = 3;
+  int format = 0;
+
+  // resident mesh
+  int n_nodes = 0, n_elem = 0, n_dof = 0;
+  bool mesh_ok = false, assembled = false, has_form = false;
+  DevBuf<double> xyz, E, nu, kbuf;
+  DevBuf<int> eq3, conn, form;
+  DevBuf<vsgb::ElementError> elem_err;
+  vsgb::AssemblyScratch scr;
+  vsgb::AssembledCsr K;
+  std::unique_ptr<vsgb::PcgEngine> eng;
+
+  // right-hand sides / solutions
+  int nrhs = 0;
+  DevBuf<double> f, u;
+  // staging of an uploaded CSR (solve_csr)
+  DevBuf<int> in_rp, in_ci;
+  DevBuf<double> in_v;
+
+  vsgb::PcgScalars* h_scal = nullptr;  // pinned
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  long long launches = 0;
+  int last_iters = 0;
+  double last_rel = 0.0;
+};
+
+namespace {
+
+void set_device(vsgb_ctx* c) { VSGB_CUDA(cudaSetDevice(c->device)); }
+
+template <typename F>
+int guarded(vsgb_ctx* c, F&& fn) {
+  if (!c) return VSGB_ERR_INVALID;
+  try {
+    set_device(c);
+    fn();
+    c->last_error.clear();
+    return VSGB_OK;
+  } catch (const Error& e) {
+    c->last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    c->last_error = "host allocation failed";
+    return VSGB_ERR_LIMIT;
+  } catch (const std::exception& e) {
+    c->last_error = e.what();
+    return VSGB_ERR_INVALID;
+  }
+}
+
+double default_tol(int precision) { return precision == VSGB_MIXED ? 1e-6 : 1e-8; }
+
+double inner_tolerance(const vsgb_ctx* c) {
+  if (c->inner_tol > 0.0) return c->inner_tol;
+  // cuda_pcg_backend_impl.hpp:2166-2171: clamp(100 * tol, 1e-4, 1e-2)
+  double t = c->tol * 100.0;
+  if (t < 1e-4) t = 1e-4;
+  if (t > 1e-2) t = 1e-2;
+  return t;
+}
+
+void check_assembly_error(vsgb_ctx* c) {
+  vsgb::AssemblyError h{};
+  VSGB_CUDA(cudaMemcpyAsync(&h, c->scr.err.ptr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  VSGB_CUDA(cudaStreamSynchronize(c->stream));
+  if (h.code == 0) return;
+  const std::string i = std::to_string(h.index);
+  switch (h.code) {
+    case 1:
+      throw Error(VSGB_ERR_INVALID, "equation index " + i + " is assigned to two DOFs");
+    case 2:
+      throw Error(VSGB_ERR_INVALID, "index out of range at position " + i);
+    case 3:
+      throw Error(VSGB_ERR_LIMIT, "node index " + i +
+                                      " exceeds the device assembly limits (32 elements or 128 "
+                                      "neighbour nodes per node)");
+    case 4:
+      throw Error(VSGB_ERR_SINGULAR, "CUDA PCG: zero diagonal at row " + i +
+                                         " -- matrix is singular. Check boundary conditions.");
+    case 5:
+      throw Error(VSGB_ERR_SINGULAR, "CUDA PCG: missing diagonal at row " + i +
+                                         " -- matrix is singular. Check boundary conditions.");
+    case 6:
+      throw Error(VSGB_ERR_INVALID, "element index " + i + " references a node index out of range");
+    default:
+      throw Error(VSGB_ERR_INVALID, "assembly error code " + std::to_string(h.code));
+  }
+}
+
+void reset_assembly_error(vsgb_ctx* c) {
+  c->scr.err.reserve(1);
+  VSGB_CUDA(cudaMemsetAsync(c->scr.err.ptr, 0, sizeof(vsgb::AssemblyError), c->stream));
+  c->scr.flag.reserve(1);
+}
+
+void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
+  const int n = c->K.n;
+  c->u.reserve(static_cast<size_t>(n) * nrhs);
+  vsgb_stats st{};
+  st.format = 1;
+  st.inner_solves = 0;
+  st.converged = 1;
+  float ms_total = 0.f;
+  for (int k = 0; k < nrhs; ++k) {
+    const double* fk = c->f.ptr + static_cast<size_t>(k) * n;
+    vsgb::SolveResult res;
+    VSGB_CUDA(cudaEventRecord(c->ev[0], c->stream));
+    if (c->precision == VSGB_MIXED) {
+      c->eng->solve_mixed(fk, c->tol, inner_tolerance(c), c->max_iters, c->max_solves, c->stream,
+                          c->h_scal, res);
+    } else {
+      c->eng->solve_fp64(fk, c->tol, c->max_iters, c->stream, c->h_scal, res);
+    }
+    VSGB_CUDA(cudaMemcpyAsync(c->u.ptr + static_cast<size_t>(k) * n, c->eng->solution(),
+                              sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    VSGB_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    VSGB_CUDA(cudaEventSynchronize(c->ev[1]));
+    float ms = 0.f;
+    VSGB_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    ms_total += ms;
+    st.iterations = res.iterations > st.iterations ? res.iterations : st.iterations;
+    st.inner_solves += res.inner_solves;
+    st.rel_residual = res.rel > st.rel_residual ? res.rel : st.rel_residual;
+    c->last_iters = res.iterations;
+    c->last_rel = res.rel;
+    const std::string tail = " (relative residual " + std::to_string(res.rel) + " > tolerance " +
+                             std::to_string(c->tol) +
+                             "). Consider increasing max iterations or using a direct solver.";
+    if (c->precision == VSGB_MIXED) {
+      if (res.inner_failed)
+        throw Error(VSGB_ERR_NOT_CONVERGED, "CUDA PCG: did not converge after " +
+                                                std::to_string(c->max_iters) + " iterations" + tail);
+      if (!res.converged) st.converged = 0;  // mixed returns the refined solution (warns)
+    } else if (!res.converged || res.iterations >= c->max_iters) {
+      // cuda_pcg_backend_impl.hpp:1964-1970 (also reached on breakdown)
+      throw Error(VSGB_ERR_NOT_CONVERGED, "CUDA PCG: did not converge after " +
+                                              std::to_string(c->max_iters) + " iterations" + tail);
+    }
+  }
+  if (stats) {
+    st.solve_ms = ms_total;
+    st.spmv_bytes = c->eng->spmv_bytes(c->precision);
+    *stats = st;
+  }
+}
+
+void upload(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes) VSGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+}
+
+}  // namespace
+
+extern "C" {
+
+int vsgb_create(int device, double tol, int max_iters, int precision, vsgb_ctx** out) {
+  if (!out) return VSGB_ERR_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0 || device < 0 || device >= count) {
+    cudaGetLastError();
+    return VSGB_ERR_NO_DEVICE;
+  }
+  if (precision != VSGB_FP64 && precision != VSGB_MIXED) return VSGB_ERR_INVALID;
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return VSGB_ERR_NO_DEVICE;
+  if (prop.major != 10 || prop.minor != 3) return VSGB_ERR_NO_DEVICE;  // built for sm_103a only
+  if (cudaSetDevice(device) != cudaSuccess) return VSGB_ERR_NO_DEVICE;
+  auto* c = new (std::nothrow) vsgb_ctx();
+  if (!c) return VSGB_ERR_LIMIT;
+  c->device = device;
+  c->num_sms = prop.multiProcessorCount;
+  c->device_name = prop.name;
+  c->precision = precision;
+  c->tol = tol > 0.0 ? tol : default_tol(precision);
+  c->max_iters = max_iters > 0 ? max_iters : 10000;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMallocHost(&c->h_scal, sizeof(vsgb::PcgScalars) * 2) != cudaSuccess) {
+    vsgb_destroy(c);
+    return VSGB_ERR_CUDA;
+  }
+  for (auto& e : c->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      vsgb_destroy(c);
+      return VSGB_ERR_CUDA;
+    }
+  c->eng = std::make_unique<vsgb::PcgEngine>(c->num_sms);
+  *out = c;
+  return VSGB_OK;
+}
+
+void vsgb_destroy(vsgb_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->eng.reset();
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->h_scal) cudaFreeHost(c->h_scal);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int vsgb_set_option(vsgb_ctx* c, int option, double value) {
+  return guarded(c, [&] {
+    switch (option) {
+      case VSGB_OPT_TOLERANCE:
+        c->tol = value > 0.0 ? value : default_tol(c->precision);
+        break;
+      case VSGB_OPT_MAX_ITERS:
+        c->max_iters = value > 0 ? static_cast<int>(value) : 10000;
+        break;
+      case VSGB_OPT_PRECISION: {
+        const int p = static_cast<int>(value);
+        if (p != VSGB_FP64 && p != VSGB_MIXED) throw Error(VSGB_ERR_INVALID, "bad precision");
+        if (p != c->precision && c->assembled) c->eng->prepare(c->K, p == VSGB_MIXED, c->stream);
+        c->precision = p;
+        break;
+      }
+      case VSGB_OPT_INNER_TOL:
+        c->inner_tol = value;
+        break;
+      case VSGB_OPT_MAX_SOLVES:
+        c->max_solves = value >= 1 ? static_cast<int>(value) : 3;
+        break;
+      case VSGB_OPT_CHECK_EVERY:
+        c->eng->set_check_every(static_cast<int>(value));
+        break;
+      case VSGB_OPT_USE_GRAPH:
+        c->eng->set_use_graph(value != 0.0);
+        break;
+      case VSGB_OPT_FORMAT:
+        c->format = static_cast<int>(value);
+        break;
+      default:
+        throw Error(VSGB_ERR_INVALID, "unknown option " + std::to_string(option));
+    }
+  });
+}
+
+int vsgb_last_error(vsgb_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || len == 0) return VSGB_ERR_INVALID;
+  std::snprintf(buf, len, "%s", c->last_error.c_str());
+  return VSGB_OK;
+}
+
+int vsgb_device_name(vsgb_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || len == 0) return VSGB_ERR_INVALID;
+  std::snprintf(buf, len, "%s", c->device_name.c_str());
+  return VSGB_OK;
+}
+
+int vsgb_backend_name(vsgb_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || len == 0) return VSGB_ERR_INVALID;
+  std::snprintf(buf, len, "%s",
+                c->precision == VSGB_MIXED
+                    ? "CUDA GB300 mixed-precision PCG + Jacobi, FP64 refinement on GPU (GPU)"
+                    : "CUDA GB300 PCG + Jacobi float64 (GPU)");
+  return VSGB_OK;
+}
+
+int vsgb_solve_csr(vsgb_ctx* c, int n, int nnz, const int* row_ptr, const int* col_ind,
+                   const double* values, int lower_only, const double* F, int nrhs,
+                   double* u_out, vsgb_stats* stats) {
+  return guarded(c, [&] {
+    if (n <= 0) throw Error(VSGB_ERR_INVALID, "CUDA PCG: stiffness matrix is empty -- no free DOFs");
+    if (nnz < 0 || !row_ptr || (nnz > 0 && (!col_ind || !values)) || !F || !u_out || nrhs < 1)
+      throw Error(VSGB_ERR_INVALID, "vsgb_solve_csr: invalid argument");
+    if (row_ptr[0] != 0 || row_ptr[n] != nnz)
+      throw Error(VSGB_ERR_INVALID, "vsgb_solve_csr: row_ptr does not span nnz");
+    cudaStream_t s = c->stream;
+    VSGB_CUDA(cudaEventRecord(c->ev[2], s));
+    c->in_rp.reserve(static_cast<size_t>(n) + 1);
+    c->in_ci.reserve(static_cast<size_t>(nnz > 0 ? nnz : 1));
+    c->in_v.reserve(static_cast<size_t>(nnz > 0 ? nnz : 1));
+    upload(c->in_rp.ptr, row_ptr, sizeof(int) * (n + 1), s);
+    upload(c->in_ci.ptr, col_ind, sizeof(int) * nnz, s);
+    upload(c->in_v.ptr, values, sizeof(double) * nnz, s);
+    reset_assembly_error(c);
+    c->assembled = false;
+    vsgb::prepare_full_csr(n, nnz, c->in_rp.ptr, c->in_ci.ptr, c->in_v.ptr, lower_only != 0,
+                           c->scr, c->K, c->num_sms, s);
+    check_assembly_error(c);
+    c->eng->prepare(c->K, c->precision == VSGB_MIXED, s);
+    VSGB_CUDA(cudaEventRecord(c->ev[3], s));
+    c->f.reserve(static_cast<size_t>(n) * nrhs);
+    upload(c->f.ptr, F, sizeof(double) * n * nrhs, s);
+    c->nrhs = nrhs;
+    run_solves(c, nrhs, stats);
+    VSGB_CUDA(cudaMemcpyAsync(u_out, c->u.ptr, sizeof(double) * n * nrhs, cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+    if (stats) {
+      float ms = 0.f;
+      VSGB_CUDA(cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]));
+      stats->setup_ms = ms;
+    }
+  });
+}
+
+int vsgb_mesh_upload(vsgb_ctx* c, int n_nodes, const double* node_xyz, const int* node_eq3,
+                     int n_elem, const int* conn, const double* E, const double* nu,
+                     const int* formulation, int n_dof) {
+  return guarded(c, [&] {
+    if (n_nodes < 0 || n_elem < 0 || n_dof < 0 || (n_nodes > 0 && (!node_xyz || !node_eq3)) ||
+        (n_elem > 0 && (!conn || !E || !nu)))
+      throw Error(VSGB_ERR_INVALID, "vsgb_mesh_upload: invalid argument");
+    if (n_elem > INT_MAX / 8) throw Error(VSGB_ERR_LIMIT, "too many elements");
+    cudaStream_t s = c->stream;
+    c->n_nodes = n_nodes;
+    c->n_elem = n_elem;
+    c->n_dof = n_dof;
+    c->xyz.reserve(static_cast<size_t>(n_nodes) * 3 + 1);
+    c->eq3.reserve(static_cast<size_t>(n_nodes) * 3 + 1);
+    c->conn.reserve(static_cast<size_t>(n_elem) * 8 + 1);
+    c->E.reserve(static_cast<size_t>(n_elem) + 1);
+    c->nu.reserve(static_cast<size_t>(n_elem) + 1);
+    upload(c->xyz.ptr, node_xyz, sizeof(double) * 3 * n_nodes, s);
+    upload(c->eq3.ptr, node_eq3, sizeof(int) * 3 * n_nodes, s);
+    upload(c->conn.ptr, conn, sizeof(int) * 8 * n_elem, s);
+    upload(c->E.ptr, E, sizeof(double) * n_elem, s);
+    upload(c->nu.ptr, nu, sizeof(double) * n_elem, s);
+    c->has_form = formulation != nullptr;
+    if (c->has_form) {
+      c->form.reserve(static_cast<size_t>(n_elem) + 1);
+      upload(c->form.ptr, formulation, sizeof(int) * n_elem, s);
+    }
+    VSGB_CUDA(cudaStreamSynchronize(s));
+    c->mesh_ok = true;
+    c->assembled = false;
+  });
+}
+
+int vsgb_assemble_resident(vsgb_ctx* c, long long* nnz_lower_out) {
+  return guarded(c, [&] {
+    if (!c->mesh_ok) throw Error(VSGB_ERR_STATE, "no mesh uploaded");
+    if (c->n_dof <= 0) throw Error(VSGB_ERR_INVALID, "CUDA PCG: stiffness matrix is empty -- no free DOFs");
+    cudaStream_t s = c->stream;
+    c->assembled = false;
+    c->kbuf.reserve(static_cast<size_t>(c->n_elem) * 576 + 1);
+    c->elem_err.reserve(1);
+    const vsgb::ElementError init{INT_MAX, 0};
+    VSGB_CUDA(cudaMemcpyAsync(c->elem_err.ptr, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    vsgb::launch_chexa8_stiffness(c->n_elem, c->xyz.ptr, c->conn.ptr, c->E.ptr, c->nu.ptr,
+                                  c->has_form ? c->form.ptr : nullptr, c->kbuf.ptr,
+                                  c->elem_err.ptr, c->num_sms, s);
+    c->eng->add_launches(1);
+    reset_assembly_error(c);
+    vsgb::assemble_csr(c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof, c->kbuf.ptr,
+                       c->scr, c->K, c->num_sms, s);
+    c->eng->add_launches(18);
+    vsgb::ElementError he{};
+    VSGB_CUDA(cudaMemcpyAsync(&he, c->elem_err.ptr, sizeof(he), cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+    if (he.index != INT_MAX) {
+      throw Error(VSGB_ERR_ELEMENT,
+                  std::string("CHEXA8") + (he.code == 2 ? "EAS element index " : " element index ") +
+                      std::to_string(he.index) +
+                      (he.code == 2 ? ": Kaa factorization failed" : ": non-positive Jacobian"));
+    }
+    check_assembly_error(c);
+    c->eng->prepare(c->K, c->precision == VSGB_MIXED, s);
+    c->assembled = true;
+    if (nnz_lower_out) *nnz_lower_out = c->K.nnz_lower;
+  });
+}
+
+int vsgb_assemble_chexa8(vsgb_ctx* c, int n_nodes, const double* node_xyz, const int* node_eq3,
+                         int n_elem, const int* conn, const double* E, const double* nu,
+                         const int* formulation, int n_dof, long long* nnz_lower_out) {
+  int rc = vsgb_mesh_upload(c, n_nodes, node_xyz, node_eq3, n_elem, conn, E, nu, formulation,
+                            n_dof);
+  if (rc != VSGB_OK) return rc;
+  return vsgb_assemble_resident(c, nnz_lower_out);
+}
+
+int vsgb_copy_csr_lower(vsgb_ctx* c, int* row_ptr, int* col_ind, double* values) {
+  return guarded(c, [&] {
+    if (!c->assembled) throw Error(VSGB_ERR_STATE, "nothing assembled");
+    cudaStream_t s = c->stream;
+    DevBuf<int> lrp, lci;
+    DevBuf<double> lv;
+    lrp.reserve(static_cast<size_t>(c->K.n) + 1);
+    lci.reserve(static_cast<size_t>(c->K.nnz_lower > 0 ? c->K.nnz_lower : 1));
+    lv.reserve(static_cast<size_t>(c->K.nnz_lower > 0 ? c->K.nnz_lower : 1));
+    vsgb::extract_lower(c->K, lrp.ptr, lci.ptr, lv.ptr, c->scr, c->num_sms, s);
+    VSGB_CUDA(cudaMemcpyAsync(row_ptr, lrp.ptr, sizeof(int) * (c->K.n + 1), cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaMemcpyAsync(col_ind, lci.ptr, sizeof(int) * c->K.nnz_lower, cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaMemcpyAsync(values, lv.ptr, sizeof(double) * c->K.nnz_lower, cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int vsgb_rhs_upload(vsgb_ctx* c, const double* F, int nrhs) {
+  return guarded(c, [&] {
+    if (!c->assembled) throw Error(VSGB_ERR_STATE, "nothing assembled");
+    if (!F || nrhs < 1) throw Error(VSGB_ERR_INVALID, "vsgb_rhs_upload: invalid argument");
+    c->f.reserve(static_cast<size_t>(c->K.n) * nrhs);
+    upload(c->f.ptr, F, sizeof(double) * c->K.n * nrhs, c->stream);
+    VSGB_CUDA(cudaStreamSynchronize(c->stream));
+    c->nrhs = nrhs;
+  });
+}
+
+int vsgb_solve_resident(vsgb_ctx* c, vsgb_stats* stats) {
+  return guarded(c, [&] {
+    if (!c->assembled || c->nrhs < 1) throw Error(VSGB_ERR_STATE, "assemble and upload RHS first");
+    run_solves(c, c->nrhs, stats);
+  });
+}
+
+int vsgb_solution_download(vsgb_ctx* c, double* u_out) {
+  return guarded(c, [&] {
+    if (!u_out) throw Error(VSGB_ERR_INVALID, "null output");
+    VSGB_CUDA(cudaMemcpyAsync(u_out, c->u.ptr, sizeof(double) * c->K.n * c->nrhs,
+                              cudaMemcpyDeviceToHost, c->stream));
+    VSGB_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int vsgb_solve_assembled(vsgb_ctx* c, const double* F, int nrhs, double* u_out,
+                         vsgb_stats* stats) {
+  int rc = vsgb_rhs_upload(c, F, nrhs);
+  if (rc != VSGB_OK) return rc;
+  rc = vsgb_solve_resident(c, stats);
+  if (rc != VSGB_OK) return rc;
+  return vsgb_solution_download(c, u_out);
+}
+
+int vsgb_element_sensitivity(vsgb_ctx* c, const double* u, const double* lambda,
+                             double* dJdE_out) {
+  return guarded(c, [&] {
+    if (!c->assembled) throw Error(VSGB_ERR_STATE, "nothing assembled");
+    if (!u || !lambda || !dJdE_out) throw Error(VSGB_ERR_INVALID, "null argument");
+    cudaStream_t s = c->stream;
+    DevBuf<double> du, dl, out;
+    du.reserve(static_cast<size_t>(c->n_dof) + 1);
+    dl.reserve(static_cast<size_t>(c->n_dof) + 1);
+    out.reserve(static_cast<size_t>(c->n_elem) + 1);
+    upload(du.ptr, u, sizeof(double) * c->n_dof, s);
+    upload(dl.ptr, lambda, sizeof(double) * c->n_dof, s);
+    vsgb::launch_element_sensitivity(c->n_elem, c->conn.ptr, c->eq3.ptr, c->E.ptr, c->kbuf.ptr,
+                                     du.ptr, dl.ptr, out.ptr, c->num_sms, s);
+    c->eng->add_launches(1);
+    VSGB_CUDA(cudaMemcpyAsync(dJdE_out, out.ptr, sizeof(double) * c->n_elem,
+                              cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int vsgb_timer_start(vsgb_ctx* c) {
+  return guarded(c, [&] {
+    VSGB_CUDA(cudaStreamSynchronize(c->stream));
+    VSGB_CUDA(cudaEventRecord(c->ev[2], c->stream));
+  });
+}
+
+int vsgb_timer_stop(vsgb_ctx* c, double* ms) {
+  return guarded(c, [&] {
+    VSGB_CUDA(cudaEventRecord(c->ev[3], c->stream));
+    VSGB_CUDA(cudaEventSynchronize(c->ev[3]));
+    VSGB_CUDA(cudaStreamSynchronize(c->stream));
+    float m = 0.f;
+    VSGB_CUDA(cudaEventElapsedTime(&m, c->ev[2], c->ev[3]));
+    if (ms) *ms = m;
+  });
+}
+
+int vsgb_time_spmv(vsgb_ctx* c, int precision, int reps, double* avg_ms, double* bytes) {
+  return guarded(c, [&] {
+    if (!c->assembled && c->K.n == 0) throw Error(VSGB_ERR_STATE, "no operator");
+    if (precision == VSGB_MIXED && !c->eng->has32()) c->eng->prepare(c->K, true, c->stream);
+    c->eng->time_spmv(precision, reps > 0 ? reps : 20, c->stream, avg_ms);
+    if (bytes) *bytes = c->eng->spmv_bytes(precision);
+  });
+}
+
+long long vsgb_kernel_launches(vsgb_ctx* c) { return c ? c->eng->launches() : -1; }
+
+}  // extern "C"

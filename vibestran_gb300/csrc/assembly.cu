@@ -1,0 +1,695 @@
+// vibestran_gb300/csrc/assembly.cu — deterministic CSR assembly on the GPU.
+//
+// Replaces the reference's triplet path (add_element_stiffness + build_csr,
+// src/core/sparse_matrix.cpp:16-150; assembly_parallel.hpp:69-110):
+//   * node -> element incidence (count, scan, fill, per-node ascending sort);
+//   * one warp per node gathers the neighbour nodes of all incident elements,
+//     orders them by their first equation index, and for every (row DOF,
+//     neighbour DOF) pair sums the element contributions in ascending element
+//     order.  A pair enters the pattern only if some element contributes a
+//     value != 0.0 — the add_element_stiffness filter (:31) — so the pattern is
+//     bit-identical to the reference's, and no atomics touch matrix values.
+//   * Both triangles are produced (the symmetric SpMV wants full storage); the
+//     reference's lower-triangle CsrData is extracted on request.
+// Memory-bound: each pass reads the element stiffness buffer once
+// (576 doubles per element) and writes 12 B per stored nonzero.
+
+#include <climits>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace vsgb {
+
+namespace {
+
+constexpr int kMaxValence = 32;                 // elements per node in the pattern kernel
+constexpr int kMaxCand = kMaxValence * 8;       // candidate neighbour slots
+constexpr int kMaxNbr = 128;                    // unique neighbour nodes per node
+constexpr int kPatWarps = 4;
+
+__device__ __forceinline__ void set_error(AssemblyError* err, int code, int index) {
+  if (atomicCAS(&err->code, 0, code) == 0) err->index = index;
+}
+
+// ── scan ───────────────────────────────────────────────────────────────────
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void k_scan_tiles(const int* __restrict__ in, int* __restrict__ out, long long n,
+                             long long* __restrict__ tile_sum) {
+  __shared__ long long s[kScanThreads];
+  const long long base = static_cast<long long>(blockIdx.x) * kScanTile;
+  long long v[kScanItems];
+  long long local = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const long long i = base + threadIdx.x * kScanItems + k;
+    v[k] = (i < n) ? in[i] : 0;
+    local += v[k];
+  }
+  s[threadIdx.x] = local;
+  __syncthreads();
+  for (int off = 1; off < kScanThreads; off <<= 1) {
+    long long t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  long long run = s[threadIdx.x] - local;  // exclusive prefix of this thread
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const long long i = base + threadIdx.x * kScanItems + k;
+    if (i < n) out[i] = static_cast<int>(run);  // tile-local; fixed up below
+    run += v[k];
+  }
+  if (threadIdx.x == kScanThreads - 1) tile_sum[blockIdx.x] = s[threadIdx.x];
+}
+
+__global__ void k_scan_tile_sums(long long* __restrict__ tile_sum, int ntiles,
+                                 long long* __restrict__ total) {
+  // single block: exclusive scan of tile sums in place
+  __shared__ long long s[1024];
+  long long carry = 0;
+  for (int base = 0; base < ntiles; base += 1024) {
+    const int i = base + threadIdx.x;
+    const long long v = (i < ntiles) ? tile_sum[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      long long t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < ntiles) tile_sum[i] = carry + s[threadIdx.x] - v;
+    const long long blk = s[1023];
+    __syncthreads();
+    carry += blk;
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(int* __restrict__ out, long long n,
+                           const long long* __restrict__ tile_sum,
+                           const long long* __restrict__ total) {
+  const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = static_cast<int>(out[i] + tile_sum[i / kScanTile]);
+  if (i == 0) out[n] = static_cast<int>(*total);
+}
+
+}  // namespace
+
+size_t scan_tmp_size(long long n) { return static_cast<size_t>((n + kScanTile - 1) / kScanTile + 1) * 2; }
+
+// tmp is reinterpreted as long long storage (scan_tmp_size counts ints).
+void exclusive_scan_checked(const int* count, int* out, long long n, int* tmp,
+                            long long* d_total, cudaStream_t s) {
+  const long long ntiles = (n + kScanTile - 1) / kScanTile;
+  long long* tile_sum = reinterpret_cast<long long*>(tmp);
+  if (n > 0) {
+    k_scan_tiles<<<static_cast<unsigned>(ntiles), kScanThreads, 0, s>>>(count, out, n, tile_sum);
+    VSGB_LAUNCH_CHECK();
+  }
+  k_scan_tile_sums<<<1, 1024, 0, s>>>(tile_sum, static_cast<int>(ntiles), d_total);
+  VSGB_LAUNCH_CHECK();
+  const long long blocks = (n + 1 + 255) / 256;
+  k_scan_add<<<static_cast<unsigned>(blocks), 256, 0, s>>>(out, n, tile_sum, d_total);
+  VSGB_LAUNCH_CHECK();
+}
+
+namespace {
+
+// ── DOF / incidence ────────────────────────────────────────────────────────
+
+__global__ void k_dof_node(int n_nodes, const int* __restrict__ eq3, int n_dof,
+                           int* __restrict__ dof_node, AssemblyError* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * n_nodes) return;
+  const int eq = eq3[i];
+  if (eq < 0) return;
+  if (eq >= n_dof) {
+    set_error(err, 2, i / 3);
+    return;
+  }
+  if (atomicExch(&dof_node[eq], i) != -1) set_error(err, 1, eq);
+}
+
+__global__ void k_dof_check(int n_dof, const int* __restrict__ dof_node, AssemblyError* err) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n_dof && dof_node[r] < 0) set_error(err, 5, r);
+}
+
+__global__ void k_node_count(long long n_slots, const int* __restrict__ conn, int n_nodes,
+                             int* __restrict__ cnt, AssemblyError* err) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= n_slots) return;
+  const int nd = conn[t];
+  if (nd < 0 || nd >= n_nodes) {
+    set_error(err, 6, static_cast<int>(t / 8));
+    return;
+  }
+  atomicAdd(&cnt[nd], 1);
+}
+
+__global__ void k_node_fill(long long n_slots, const int* __restrict__ conn, int n_nodes,
+                            const int* __restrict__ ptr, int* __restrict__ cursor,
+                            int* __restrict__ node_elem) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= n_slots) return;
+  const int nd = conn[t];
+  if (nd < 0 || nd >= n_nodes) return;
+  node_elem[ptr[nd] + atomicAdd(&cursor[nd], 1)] = static_cast<int>(t);
+}
+
+__global__ void k_node_sort(int n_nodes, const int* __restrict__ ptr, int* __restrict__ node_elem) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n_nodes) return;
+  const int b = ptr[a], e = ptr[a + 1];
+  for (int i = b + 1; i < e; ++i) {  // insertion sort: slot = 8*element + local node
+    const int v = node_elem[i];
+    int j = i - 1;
+    while (j >= b && node_elem[j] > v) {
+      node_elem[j + 1] = node_elem[j];
+      --j;
+    }
+    node_elem[j + 1] = v;
+  }
+}
+
+// ── pattern + values ───────────────────────────────────────────────────────
+
+struct PatSmem {
+  int cand[kMaxCand];
+  int key[kMaxCand];
+  int first[kMaxCand];
+  int nbr[kMaxNbr];
+};
+
+__device__ __forceinline__ int first_free_eq(const int* eq3, int b) {
+  int k = INT_MAX;
+#pragma unroll
+  for (int d = 2; d >= 0; --d) {
+    const int q = eq3[3 * b + d];
+    if (q >= 0) k = q < k ? q : k;
+  }
+  return k;
+}
+
+// Warp-inclusive scan of ints across lanes.
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+template <bool kFill>
+__global__ void __launch_bounds__(kPatWarps * 32)
+k_pattern(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3,
+          const int* __restrict__ node_ptr, const int* __restrict__ node_elem,
+          const double* __restrict__ kbuf, int* __restrict__ row_cnt,
+          const int* __restrict__ row_ptr, int* __restrict__ col_ind,
+          double* __restrict__ values, double* __restrict__ dinv, AssemblyError* err) {
+  __shared__ PatSmem smem_all[kPatWarps];
+  PatSmem& s = smem_all[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * kPatWarps;
+  for (int a = blockIdx.x * kPatWarps + (threadIdx.x >> 5); a < n_nodes; a += warps_total) {
+    int row[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) row[d] = eq3[3 * a + d];
+    if (row[0] < 0 && row[1] < 0 && row[2] < 0) continue;
+    const int pb = node_ptr[a], L = node_ptr[a + 1] - pb;
+    if (L > kMaxValence) {
+      if (lane == 0) set_error(err, 3, a);
+      continue;
+    }
+    const int C = 8 * L;
+    for (int c = lane; c < C; c += 32) {
+      const int slot = node_elem[pb + (c >> 3)];
+      const int b = conn[(slot & ~7) + (c & 7)];
+      s.cand[c] = b;
+      s.key[c] = first_free_eq(eq3, b);
+    }
+    __syncwarp();
+    for (int c = lane; c < C; c += 32) {
+      const int b = s.cand[c];
+      int f = s.key[c] != INT_MAX;
+      for (int m = 0; m < c && f; ++m)
+        if (s.cand[m] == b) f = 0;
+      s.first[c] = f;
+    }
+    __syncwarp();
+    int U = 0;
+    for (int c = lane; c < C; c += 32) {
+      if (s.first[c]) {
+        const int k = s.key[c];
+        int r = 0;
+        for (int m = 0; m < C; ++m) r += (s.first[m] && s.key[m] < k);
+        if (r < kMaxNbr) s.nbr[r] = s.cand[c];
+      }
+    }
+    for (int c = lane; c < C; c += 32) U += s.first[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) U += __shfl_xor_sync(0xffffffffu, U, o);
+    if (U > kMaxNbr) {
+      if (lane == 0) set_error(err, 3, a);
+      continue;
+    }
+    __syncwarp();
+
+    int carry[3] = {0, 0, 0};
+    int base[3] = {0, 0, 0};
+    if (kFill) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) base[d] = row[d] >= 0 ? row_ptr[row[d]] : 0;
+    }
+    bool diag_seen[3] = {false, false, false};
+    for (int u0 = 0; u0 < U; u0 += 32) {
+      const int u = u0 + lane;
+      const bool act = u < U;
+      const int b = act ? s.nbr[u] : -1;
+      int colq[3] = {-1, -1, -1};
+      double sum[3][3];
+      bool nz[3][3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          sum[d][q] = 0.0;
+          nz[d][q] = false;
+        }
+      if (act) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) colq[q] = eq3[3 * b + q];
+        for (int k = 0; k < L; ++k) {
+          const int slot = node_elem[pb + k];
+          const int e = slot >> 3, la = slot & 7;
+          int lb = -1;
+#pragma unroll
+          for (int m = 0; m < 8; ++m)
+            if (conn[8 * e + m] == b) lb = m;
+          if (lb < 0) continue;
+          const double* ke = kbuf + static_cast<size_t>(e) * 576 + (3 * la) * 24 + 3 * lb;
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const double v = ke[d * 24 + q];
+              sum[d][q] += v;
+              nz[d][q] = nz[d][q] || (v != 0.0);
+            }
+        }
+      }
+      int cnt[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        cnt[d] = 0;
+        if (row[d] >= 0)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) cnt[d] += (colq[q] >= 0 && nz[d][q]);
+      }
+      if (!kFill) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          int t = cnt[d];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+          carry[d] += t;
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const int incl = warp_incl_scan(cnt[d]);
+          int pos = base[d] + carry[d] + incl - cnt[d];
+          carry[d] += __shfl_sync(0xffffffffu, incl, 31);
+          if (act && row[d] >= 0) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              if (colq[q] >= 0 && nz[d][q]) {
+                col_ind[pos] = colq[q];
+                values[pos] = sum[d][q];
+                ++pos;
+              }
+            }
+            if (b == a) {
+              if (nz[d][d]) {
+                diag_seen[d] = true;
+                if (sum[d][d] == 0.0)
+                  set_error(err, 4, row[d]);
+                else
+                  dinv[row[d]] = 1.0 / sum[d][d];
+              }
+            }
+          }
+        }
+      }
+    }
+    if (!kFill) {
+      if (lane == 0)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          if (row[d] >= 0) row_cnt[row[d]] = carry[d];
+    } else {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const bool seen = __any_sync(0xffffffffu, diag_seen[d]);
+        if (lane == 0 && row[d] >= 0 && !seen) set_error(err, 5, row[d]);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Sort each row by column (stable rank sort; rows already sorted are left
+// untouched).  Rows up to kRowSmem entries are ranked in shared memory,
+// longer rows in global memory.
+constexpr int kRowSmem = 512;
+constexpr int kSortWarps = 4;
+
+__global__ void __launch_bounds__(kSortWarps * 32)
+k_sort_rows(int n, const int* __restrict__ rp, int* __restrict__ ci, double* __restrict__ v,
+            int* __restrict__ tmp_ci, double* __restrict__ tmp_v, int* __restrict__ need_tmp) {
+  __shared__ int s_c[kSortWarps][kRowSmem];
+  __shared__ double s_v[kSortWarps][kRowSmem];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int r = blockIdx.x * kSortWarps + w; r < n; r += gridDim.x * kSortWarps) {
+    const int b = rp[r], len = rp[r + 1] - b;
+    int unsorted = 0;
+    for (int k = lane + 1; k < len; k += 32) unsorted |= (ci[b + k - 1] > ci[b + k]);
+    if (!__any_sync(0xffffffffu, unsorted)) continue;
+    if (len <= kRowSmem) {
+      for (int k = lane; k < len; k += 32) {
+        s_c[w][k] = ci[b + k];
+        s_v[w][k] = v[b + k];
+      }
+      __syncwarp();
+      for (int k = lane; k < len; k += 32) {
+        const int c = s_c[w][k];
+        int rank = 0;
+        for (int m = 0; m < len; ++m) {
+          const int cm = s_c[w][m];
+          rank += (cm < c) || (cm == c && m < k);
+        }
+        ci[b + rank] = c;
+        v[b + rank] = s_v[w][k];
+      }
+      __syncwarp();
+    } else if (tmp_ci == nullptr) {
+      if (lane == 0) *need_tmp = 1;  // host reruns with scratch buffers
+    } else {
+      for (int k = lane; k < len; k += 32) {
+        tmp_ci[b + k] = ci[b + k];
+        tmp_v[b + k] = v[b + k];
+      }
+      __syncwarp();
+      for (int k = lane; k < len; k += 32) {
+        const int c = tmp_ci[b + k];
+        int rank = 0;
+        for (int m = 0; m < len; ++m) {
+          const int cm = tmp_ci[b + m];
+          rank += (cm < c) || (cm == c && m < k);
+        }
+        ci[b + rank] = c;
+        v[b + rank] = tmp_v[b + k];
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ── lower-triangle extraction ──────────────────────────────────────────────
+
+__global__ void k_lower_count(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                              int* __restrict__ cnt) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int lo = rp[r], hi = rp[r + 1];  // rows are sorted: first index with col > r
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (ci[mid] <= r)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  cnt[r] = lo - rp[r];
+}
+
+__global__ void k_lower_fill(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                             const double* __restrict__ v, const int* __restrict__ lrp,
+                             int* __restrict__ lci, double* __restrict__ lv) {
+  const int lane = threadIdx.x & 31;
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += (gridDim.x * blockDim.x) >> 5) {
+    const int b = rp[r], lb = lrp[r], len = lrp[r + 1] - lb;
+    for (int k = lane; k < len; k += 32) {
+      lci[lb + k] = ci[b + k];
+      lv[lb + k] = v[b + k];
+    }
+  }
+}
+
+// ── lower -> full expansion of an uploaded CSR ─────────────────────────────
+
+__global__ void k_check_cols(long long nnz, const int* __restrict__ ci, int n,
+                             AssemblyError* err) {
+  const long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < nnz && (ci[k] < 0 || ci[k] >= n)) set_error(err, 2, static_cast<int>(k));
+}
+
+__global__ void k_expand_count(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                               int* __restrict__ cnt /* zeroed, gets transposed counts */) {
+  const int lane = threadIdx.x & 31;
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += (gridDim.x * blockDim.x) >> 5) {
+    for (int k = rp[r] + lane; k < rp[r + 1]; k += 32) {
+      const int c = ci[k];
+      if (c != r && c >= 0 && c < n) atomicAdd(&cnt[c], 1);
+    }
+  }
+}
+
+__global__ void k_add_rowlen(int n, const int* __restrict__ rp, int* __restrict__ cnt) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) cnt[r] += rp[r + 1] - rp[r];
+}
+
+__global__ void k_expand_fill(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                              const double* __restrict__ v, const int* __restrict__ frp,
+                              int* __restrict__ cursor, int* __restrict__ fci,
+                              double* __restrict__ fv) {
+  const int lane = threadIdx.x & 31;
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += (gridDim.x * blockDim.x) >> 5) {
+    const int b = rp[r], len = rp[r + 1] - b, fb = frp[r];
+    for (int k = lane; k < len; k += 32) {
+      const int c = ci[b + k];
+      const double x = v[b + k];
+      fci[fb + k] = c;
+      fv[fb + k] = x;
+      if (c != r && c >= 0 && c < n) {
+        const int pos = frp[c] + (rp[c + 1] - rp[c]) + atomicAdd(&cursor[c], 1);
+        fci[pos] = r;
+        fv[pos] = x;
+      }
+    }
+  }
+}
+
+// Inverse Jacobi diagonal from full storage: first entry with col == row
+// (build_jacobi_diagonal, cuda_pcg_backend_impl.hpp:2076-2101).
+__global__ void k_diag_inverse(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                               const double* __restrict__ v, double* __restrict__ dinv,
+                               AssemblyError* err) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (int k = rp[r]; k < rp[r + 1]; ++k) {
+    if (ci[k] == r) {
+      if (v[k] == 0.0) {
+        set_error(err, 4, r);
+        dinv[r] = 0.0;
+      } else {
+        dinv[r] = 1.0 / v[k];
+      }
+      return;
+    }
+  }
+  set_error(err, 5, r);
+  dinv[r] = 0.0;
+}
+
+}  // namespace
+
+void assemble_csr(int n_nodes, int n_elem, const int* conn, const int* eq3, int n_dof,
+                  const double* kbuf, AssemblyScratch& scr, AssembledCsr& out, int num_sms,
+                  cudaStream_t s) {
+  const long long slots = 8LL * n_elem;
+  scr.node_cnt.reserve(static_cast<size_t>(n_nodes) + 1);
+  scr.node_ptr.reserve(static_cast<size_t>(n_nodes) + 1);
+  scr.node_elem.reserve(static_cast<size_t>(slots > 0 ? slots : 1));
+  scr.dof_node.reserve(static_cast<size_t>(n_dof > 0 ? n_dof : 1));
+  scr.row_cnt.reserve(static_cast<size_t>(n_dof) + 1);
+  const long long scan_n = n_nodes > n_dof ? n_nodes : n_dof;
+  scr.scan_tmp.reserve(scan_tmp_size(scan_n + 1));
+  scr.total.reserve(1);
+  out.n = n_dof;
+  out.row_ptr.reserve(static_cast<size_t>(n_dof) + 1);
+  out.dinv.reserve(static_cast<size_t>(n_dof > 0 ? n_dof : 1));
+
+  // DOF -> node map and validation of the equation table.
+  VSGB_CUDA(cudaMemsetAsync(scr.dof_node.ptr, 0xFF, sizeof(int) * (n_dof > 0 ? n_dof : 1), s));
+  k_dof_node<<<grid_for(3LL * n_nodes, kThreads, 1 << 30), kThreads, 0, s>>>(
+      n_nodes, eq3, n_dof, scr.dof_node.ptr, scr.err.ptr);
+  VSGB_LAUNCH_CHECK();
+  k_dof_check<<<grid_for(n_dof, kThreads, 1 << 30), kThreads, 0, s>>>(n_dof, scr.dof_node.ptr,
+                                                                      scr.err.ptr);
+  VSGB_LAUNCH_CHECK();
+
+  // Node -> element incidence.
+  VSGB_CUDA(cudaMemsetAsync(scr.node_cnt.ptr, 0, sizeof(int) * (n_nodes + 1), s));
+  k_node_count<<<grid_for(slots, kThreads, 1 << 30), kThreads, 0, s>>>(slots, conn, n_nodes,
+                                                                      scr.node_cnt.ptr, scr.err.ptr);
+  VSGB_LAUNCH_CHECK();
+  exclusive_scan_checked(scr.node_cnt.ptr, scr.node_ptr.ptr, n_nodes, scr.scan_tmp.ptr,
+                         scr.total.ptr, s);
+  VSGB_CUDA(cudaMemsetAsync(scr.node_cnt.ptr, 0, sizeof(int) * (n_nodes + 1), s));
+  k_node_fill<<<grid_for(slots, kThreads, 1 << 30), kThreads, 0, s>>>(
+      slots, conn, n_nodes, scr.node_ptr.ptr, scr.node_cnt.ptr, scr.node_elem.ptr);
+  VSGB_LAUNCH_CHECK();
+  k_node_sort<<<grid_for(n_nodes, 128, 1 << 30), 128, 0, s>>>(n_nodes, scr.node_ptr.ptr,
+                                                              scr.node_elem.ptr);
+  VSGB_LAUNCH_CHECK();
+
+  // Pattern count -> row_ptr.
+  VSGB_CUDA(cudaMemsetAsync(scr.row_cnt.ptr, 0, sizeof(int) * (n_dof + 1), s));
+  const int pgrid = grid_for(static_cast<long long>(n_nodes) * 32, kPatWarps * 32, num_sms * 16);
+  k_pattern<false><<<pgrid, kPatWarps * 32, 0, s>>>(n_nodes, conn, eq3, scr.node_ptr.ptr,
+                                                    scr.node_elem.ptr, kbuf, scr.row_cnt.ptr,
+                                                    nullptr, nullptr, nullptr, nullptr,
+                                                    scr.err.ptr);
+  VSGB_LAUNCH_CHECK();
+  exclusive_scan_checked(scr.row_cnt.ptr, out.row_ptr.ptr, n_dof, scr.scan_tmp.ptr,
+                         scr.total.ptr, s);
+  long long nnz = 0;
+  VSGB_CUDA(cudaMemcpyAsync(&nnz, scr.total.ptr, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  if (nnz >= INT_MAX) throw Error(VSGB_ERR_LIMIT, "assembled nnz exceeds the int32 CSR limit");
+  out.nnz = nnz;
+  out.col_ind.reserve(static_cast<size_t>(nnz > 0 ? nnz : 1));
+  out.values.reserve(static_cast<size_t>(nnz > 0 ? nnz : 1));
+  k_pattern<true><<<pgrid, kPatWarps * 32, 0, s>>>(n_nodes, conn, eq3, scr.node_ptr.ptr,
+                                                   scr.node_elem.ptr, kbuf, nullptr,
+                                                   out.row_ptr.ptr, out.col_ind.ptr,
+                                                   out.values.ptr, out.dinv.ptr, scr.err.ptr);
+  VSGB_LAUNCH_CHECK();
+  // Columns come out sorted for node-major equation numbering (the
+  // reference's DofMap); any other numbering is sorted here.
+  k_sort_rows<<<grid_for(static_cast<long long>(n_dof) * 32, kSortWarps * 32, num_sms * 16),
+                kSortWarps * 32, 0, s>>>(n_dof, out.row_ptr.ptr, out.col_ind.ptr,
+                                         out.values.ptr, nullptr, nullptr, scr.flag.ptr);
+  VSGB_LAUNCH_CHECK();
+  // Lower-triangle nnz for reporting.
+  k_lower_count<<<grid_for(n_dof, kThreads, 1 << 30), kThreads, 0, s>>>(
+      n_dof, out.row_ptr.ptr, out.col_ind.ptr, scr.row_cnt.ptr);
+  VSGB_LAUNCH_CHECK();
+  scr.lower_rp.reserve(static_cast<size_t>(n_dof) + 1);
+  exclusive_scan_checked(scr.row_cnt.ptr, scr.lower_rp.ptr, n_dof, scr.scan_tmp.ptr,
+                         scr.total.ptr, s);
+  long long nl = 0;
+  VSGB_CUDA(cudaMemcpyAsync(&nl, scr.total.ptr, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  out.nnz_lower = nl;
+}
+
+void extract_lower(const AssembledCsr& full, int* d_row_ptr, int* d_col_ind, double* d_values,
+                   AssemblyScratch& scr, int num_sms, cudaStream_t s) {
+  const int n = full.n;
+  scr.row_cnt.reserve(static_cast<size_t>(n) + 1);
+  scr.scan_tmp.reserve(scan_tmp_size(n + 1));
+  scr.total.reserve(1);
+  k_lower_count<<<grid_for(n, kThreads, 1 << 30), kThreads, 0, s>>>(n, full.row_ptr.ptr,
+                                                                    full.col_ind.ptr,
+                                                                    scr.row_cnt.ptr);
+  VSGB_LAUNCH_CHECK();
+  exclusive_scan_checked(scr.row_cnt.ptr, d_row_ptr, n, scr.scan_tmp.ptr, scr.total.ptr, s);
+  k_lower_fill<<<grid_for(static_cast<long long>(n) * 32, kThreads, num_sms * 16), kThreads, 0,
+                 s>>>(n, full.row_ptr.ptr, full.col_ind.ptr, full.values.ptr, d_row_ptr,
+                      d_col_ind, d_values);
+  VSGB_LAUNCH_CHECK();
+}
+
+void prepare_full_csr(int n, long long nnz, const int* rp, const int* ci, const double* v,
+                      bool lower, AssemblyScratch& scr, AssembledCsr& out, int num_sms,
+                      cudaStream_t s) {
+  out.n = n;
+  out.row_ptr.reserve(static_cast<size_t>(n) + 1);
+  out.dinv.reserve(static_cast<size_t>(n));
+  if (nnz > 0) {
+    k_check_cols<<<grid_for(nnz, kThreads, 1 << 30), kThreads, 0, s>>>(nnz, ci, n, scr.err.ptr);
+    VSGB_LAUNCH_CHECK();
+  }
+  if (!lower) {
+    out.nnz = nnz;
+    out.col_ind.reserve(static_cast<size_t>(nnz > 0 ? nnz : 1));
+    out.values.reserve(static_cast<size_t>(nnz > 0 ? nnz : 1));
+    VSGB_CUDA(cudaMemcpyAsync(out.row_ptr.ptr, rp, sizeof(int) * (n + 1), cudaMemcpyDeviceToDevice, s));
+    if (nnz > 0) {
+      VSGB_CUDA(cudaMemcpyAsync(out.col_ind.ptr, ci, sizeof(int) * nnz, cudaMemcpyDeviceToDevice, s));
+      VSGB_CUDA(cudaMemcpyAsync(out.values.ptr, v, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, s));
+    }
+  } else {
+    scr.row_cnt.reserve(static_cast<size_t>(n) + 1);
+    scr.node_cnt.reserve(static_cast<size_t>(n) + 1);
+    scr.scan_tmp.reserve(scan_tmp_size(n + 1));
+    scr.total.reserve(1);
+    VSGB_CUDA(cudaMemsetAsync(scr.row_cnt.ptr, 0, sizeof(int) * (n + 1), s));
+    const int wgrid = grid_for(static_cast<long long>(n) * 32, kThreads, num_sms * 16);
+    k_expand_count<<<wgrid, kThreads, 0, s>>>(n, rp, ci, scr.row_cnt.ptr);
+    VSGB_LAUNCH_CHECK();
+    k_add_rowlen<<<grid_for(n, kThreads, 1 << 30), kThreads, 0, s>>>(n, rp, scr.row_cnt.ptr);
+    VSGB_LAUNCH_CHECK();
+    exclusive_scan_checked(scr.row_cnt.ptr, out.row_ptr.ptr, n, scr.scan_tmp.ptr, scr.total.ptr, s);
+    long long fnnz = 0;
+    VSGB_CUDA(cudaMemcpyAsync(&fnnz, scr.total.ptr, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+    if (fnnz >= INT_MAX) throw Error(VSGB_ERR_LIMIT, "expanded nnz exceeds the int32 CSR limit");
+    out.nnz = fnnz;
+    out.col_ind.reserve(static_cast<size_t>(fnnz > 0 ? fnnz : 1));
+    out.values.reserve(static_cast<size_t>(fnnz > 0 ? fnnz : 1));
+    VSGB_CUDA(cudaMemsetAsync(scr.node_cnt.ptr, 0, sizeof(int) * (n + 1), s));
+    k_expand_fill<<<wgrid, kThreads, 0, s>>>(n, rp, ci, v, out.row_ptr.ptr, scr.node_cnt.ptr,
+                                              out.col_ind.ptr, out.values.ptr);
+    VSGB_LAUNCH_CHECK();
+  }
+  // Sort rows (mirrored entries arrive unordered).  Rows longer than the
+  // shared-memory tile are sorted in a second pass with global scratch.
+  const int sgrid = grid_for(static_cast<long long>(n) * 32, kSortWarps * 32, num_sms * 16);
+  VSGB_CUDA(cudaMemsetAsync(scr.flag.ptr, 0, sizeof(int), s));
+  k_sort_rows<<<sgrid, kSortWarps * 32, 0, s>>>(n, out.row_ptr.ptr, out.col_ind.ptr,
+                                                out.values.ptr, nullptr, nullptr, scr.flag.ptr);
+  VSGB_LAUNCH_CHECK();
+  int need_tmp = 0;
+  VSGB_CUDA(cudaMemcpyAsync(&need_tmp, scr.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  if (need_tmp) {
+    DevBuf<int> tci;
+    DevBuf<double> tv;
+    tci.reserve(static_cast<size_t>(out.nnz));
+    tv.reserve(static_cast<size_t>(out.nnz));
+    k_sort_rows<<<sgrid, kSortWarps * 32, 0, s>>>(n, out.row_ptr.ptr, out.col_ind.ptr,
+                                                  out.values.ptr, tci.ptr, tv.ptr, scr.flag.ptr);
+    VSGB_LAUNCH_CHECK();
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  }
+  k_diag_inverse<<<grid_for(n, kThreads, 1 << 30), kThreads, 0, s>>>(
+      n, out.row_ptr.ptr, out.col_ind.ptr, out.values.ptr, out.dinv.ptr, scr.err.ptr);
+  VSGB_LAUNCH_CHECK();
+}
+
+}  // namespace vsgb

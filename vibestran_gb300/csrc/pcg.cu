@@ -1,0 +1,651 @@
+// vibestran_gb300/csrc/pcg.cu — Jacobi-preconditioned CG on the GPU.
+//
+// Replaces run_pcg_prepared (src/solver/cuda_pcg_backend_impl.hpp:1688-1999),
+// which issues per iteration three cuSPARSE SpMV passes over the lower CSR, four
+// cuBLAS dots, two axpys, two single-thread scalar kernels and a blocking
+// device->host copy.  Here:
+//   FP64:  3 kernels / iteration
+//     p  = z + beta p                       (k_search64)
+//     Ap = K p, pAp, alpha                  (k_spmv64, last-block reduction)
+//     u += alpha p, r -= alpha Ap, z = r/d, r.z, r.r, beta, convergence
+//                                           (k_update64, last-block reduction)
+//   FP32 inner (mixed):  2 kernels / iteration — the search-direction update is
+//     fused into the SpMV gather (x_j = z_j + beta p_j recomputed per nonzero,
+//     with an explicit fma so every consumer rounds identically), p ping-pongs
+//     between two buffers.
+// Scalars live on the device (PcgScalars); the host reads them every
+// `check_every` iterations (iterations after convergence early-exit), and the
+// iteration batch is replayed as a CUDA graph.
+// The operator is full-storage CSR (both triangles), one SpMV pass.
+// Roofline: HBM (12 B/nnz FP64, 8 B/nnz FP32 + vectors) and, on GB300, the
+// FP64 FMA rate for the FP64 path.
+
+#include <cmath>
+#include <string>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "pcg.cuh"
+
+namespace vsgb {
+
+namespace {
+
+constexpr int kSpmvThreads = 256;
+constexpr int kLpr = 8;  // lanes per CSR row
+
+// ── FP64 kernels ───────────────────────────────────────────────────────────
+
+__global__ void __launch_bounds__(kThreads)
+k_init64(int n, const double* __restrict__ f, const double* __restrict__ dinv,
+         double* __restrict__ r, double* __restrict__ u, double* __restrict__ z,
+         double* __restrict__ p, PcgScalars* S, double* partials, unsigned* counter) {
+  __shared__ double sm[64];
+  double acc[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ri = f[i];
+    const double zi = ri * dinv[i];
+    r[i] = ri;
+    u[i] = 0.0;
+    z[i] = zi;
+    p[i] = 0.0;
+    acc[0] = fma(ri, ri, acc[0]);
+    acc[1] = fma(ri, zi, acc[1]);
+  }
+  double tot[2];
+  if (grid_sum_last<2>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+    const double norm_b = sqrt(fabs(tot[0]));
+    S->norm_b = norm_b;
+    S->rz = tot[1];
+    S->rr = tot[0];
+    S->rel = 1.0;
+    S->beta = 0.0;
+    S->alpha = 0.0;
+    S->iter = 0;
+    int flags = 0;
+    if (norm_b < 1e-300) {
+      flags = kFlagDone | kFlagZeroRhs | kFlagConverged;
+      S->rel = 0.0;
+    } else if (!(tot[1] > 0.0)) {
+      flags = kFlagDone | kFlagNonPosRz;
+    }
+    S->flags = flags;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_search64(int n, const double* __restrict__ z, double* __restrict__ p, const PcgScalars* S) {
+  if (S->flags & kFlagDone) return;
+  const double beta = S->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = fma(beta, p[i], z[i]);
+}
+
+template <typename T, typename Acc>
+__device__ __forceinline__ Acc row_dot(const int* __restrict__ rp, const int* __restrict__ ci,
+                                       const T* __restrict__ val, const T* __restrict__ x,
+                                       int row, int sub) {
+  Acc s = 0;
+  const int e = rp[row + 1];
+  for (int k = rp[row] + sub; k < e; k += kLpr) s = fma(static_cast<Acc>(val[k]), static_cast<Acc>(x[ci[k]]), s);
+  return s;
+}
+
+__global__ void __launch_bounds__(kSpmvThreads)
+k_spmv64(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+         const double* __restrict__ val, const double* __restrict__ p, double* __restrict__ Ap,
+         PcgScalars* S, double* partials, unsigned* counter) {
+  if (S->flags & kFlagDone) return;
+  __shared__ double sm[32];
+  const int sub = threadIdx.x & (kLpr - 1);
+  const int rows_per_block = kSpmvThreads / kLpr;
+  double acc[1] = {0.0};
+  for (int row = blockIdx.x * rows_per_block + threadIdx.x / kLpr; row < n;
+       row += gridDim.x * rows_per_block) {
+    double s = row_dot<double, double>(rp, ci, val, p, row, sub);
+#pragma unroll
+    for (int o = kLpr / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (sub == 0) {
+      Ap[row] = s;
+      acc[0] = fma(p[row], s, acc[0]);
+    }
+  }
+  double tot[1];
+  if (grid_sum_last<1>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+    const double pAp = tot[0];
+    S->pAp = pAp;
+    if (!(pAp > 0.0)) {
+      S->alpha = 0.0;
+      S->flags |= kFlagDone | kFlagBreakdown;
+    } else {
+      S->alpha = S->rz / pAp;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_update64(int n, double* __restrict__ u, double* __restrict__ r, double* __restrict__ z,
+           const double* __restrict__ p, const double* __restrict__ Ap,
+           const double* __restrict__ dinv, PcgScalars* S, double* partials, unsigned* counter) {
+  if (S->flags & kFlagDone) return;
+  __shared__ double sm[64];
+  const double alpha = S->alpha;
+  double acc[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    u[i] = fma(alpha, p[i], u[i]);
+    const double ri = fma(-alpha, Ap[i], r[i]);
+    const double zi = ri * dinv[i];
+    r[i] = ri;
+    z[i] = zi;
+    acc[0] = fma(ri, zi, acc[0]);
+    acc[1] = fma(ri, ri, acc[1]);
+  }
+  double tot[2];
+  if (grid_sum_last<2>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+    const double rz_new = tot[0], rr = tot[1];
+    const double rel = sqrt(fabs(rr)) / S->norm_b;
+    const int it = S->iter + 1;
+    S->iter = it;
+    S->rr = rr;
+    S->rel = rel;
+    int flags = S->flags;
+    if (rel < S->tol) {
+      flags |= kFlagDone | kFlagConverged;
+      S->beta = 0.0;
+    } else {
+      S->beta = rz_new / S->rz;
+      if (it >= S->max_iters) flags |= kFlagDone | kFlagMaxIters;
+    }
+    S->rz = rz_new;
+    S->flags = flags;
+  }
+}
+
+// ── FP32 inner kernels (mixed precision) ───────────────────────────────────
+
+// r32 = (float)(r64 * scale); u32 = 0; z = r*dinv; p_old = 0; dots.
+__global__ void __launch_bounds__(kThreads)
+k_init32(int n, const double* __restrict__ r64, double scale_unused, const float* __restrict__ dinv,
+         float* __restrict__ r, float* __restrict__ u, float* __restrict__ z,
+         float* __restrict__ p, PcgScalars* S, const PcgScalars* outer, double* partials,
+         unsigned* counter) {
+  __shared__ double sm[64];
+  const double scale = outer->scale;
+  float a0 = 0.f, a1 = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float ri = static_cast<float>(r64[i] * scale);
+    const float zi = ri * dinv[i];
+    r[i] = ri;
+    u[i] = 0.f;
+    z[i] = zi;
+    p[i] = 0.f;
+    a0 = fmaf(ri, ri, a0);
+    a1 = fmaf(ri, zi, a1);
+  }
+  double acc[2] = {a0, a1};
+  double tot[2];
+  if (grid_sum_last<2>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+    const double norm_b = sqrt(fabs(tot[0]));
+    S->norm_b = norm_b;
+    S->rz = tot[1];
+    S->rr = tot[0];
+    S->rel = 1.0;
+    S->beta = 0.0;
+    S->alpha = 0.0;
+    S->iter = 0;
+    int flags = 0;
+    if (norm_b < 1e-300) {
+      flags = kFlagDone | kFlagZeroRhs | kFlagConverged;
+      S->rel = 0.0;
+    } else if (!(tot[1] > 0.0)) {
+      flags = kFlagDone | kFlagNonPosRz;
+    }
+    S->flags = flags;
+  }
+  (void)scale_unused;
+}
+
+__global__ void __launch_bounds__(kSpmvThreads)
+k_spmv32_fused(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+               const float* __restrict__ val, const float* __restrict__ z,
+               const float* __restrict__ p_old, float* __restrict__ p_new,
+               float* __restrict__ Ap, PcgScalars* S, double* partials, unsigned* counter) {
+  if (S->flags & kFlagDone) return;
+  __shared__ double sm[32];
+  const float beta = static_cast<float>(S->beta);
+  const int sub = threadIdx.x & (kLpr - 1);
+  const int rows_per_block = kSpmvThreads / kLpr;
+  float accf = 0.f;
+  for (int row = blockIdx.x * rows_per_block + threadIdx.x / kLpr; row < n;
+       row += gridDim.x * rows_per_block) {
+    float s = 0.f;
+    const int e = rp[row + 1];
+    for (int k = rp[row] + sub; k < e; k += kLpr) {
+      const int c = ci[k];
+      s = fmaf(val[k], fmaf(beta, p_old[c], z[c]), s);
+    }
+#pragma unroll
+    for (int o = kLpr / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (sub == 0) {
+      const float pn = fmaf(beta, p_old[row], z[row]);
+      p_new[row] = pn;
+      Ap[row] = s;
+      accf = fmaf(pn, s, accf);
+    }
+  }
+  double acc[1] = {accf};
+  double tot[1];
+  if (grid_sum_last<1>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+    const double pAp = tot[0];
+    S->pAp = pAp;
+    if (!(pAp > 0.0)) {
+      S->alpha = 0.0;
+      S->flags |= kFlagDone | kFlagBreakdown;
+    } else {
+      S->alpha = S->rz / pAp;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_update32(int n, float* __restrict__ u, float* __restrict__ r, float* __restrict__ z,
+           const float* __restrict__ p, const float* __restrict__ Ap,
+           const float* __restrict__ dinv, PcgScalars* S, double* partials, unsigned* counter) {
+  if (S->flags & kFlagDone) return;
+  __shared__ double sm[64];
+  const float alpha = static_cast<float>(S->alpha);
+  float a0 = 0.f, a1 = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    u[i] = fmaf(alpha, p[i], u[i]);
+    const float ri = fmaf(-alpha, Ap[i], r[i]);
+    const float zi = ri * dinv[i];
+    r[i] = ri;
+    z[i] = zi;
+    a0 = fmaf(ri, zi, a0);
+    a1 = fmaf(ri, ri, a1);
+  }
+  double acc[2] = {a0, a1};
+  double tot[2];
+  if (grid_sum_last<2>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+    const double rz_new = tot[0], rr = tot[1];
+    const double rel = sqrt(fabs(rr)) / S->norm_b;
+    const int it = S->iter + 1;
+    S->iter = it;
+    S->rr = rr;
+    S->rel = rel;
+    int flags = S->flags;
+    if (rel < S->tol) {
+      flags |= kFlagDone | kFlagConverged;
+      S->beta = 0.0;
+    } else {
+      S->beta = rz_new / S->rz;
+      if (it >= S->max_iters) flags |= kFlagDone | kFlagMaxIters;
+    }
+    S->rz = rz_new;
+    S->flags = flags;
+  }
+}
+
+// ── FP64 refinement kernels ────────────────────────────────────────────────
+
+// r64 = f - K u64; ||r64||^2 -> outer scalars (rel vs ||f||, scale = 1/||r||).
+__global__ void __launch_bounds__(kSpmvThreads)
+k_residual64(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+             const double* __restrict__ val, const double* __restrict__ u,
+             const double* __restrict__ f, double* __restrict__ r, PcgScalars* O,
+             double* partials, unsigned* counter) {
+  __shared__ double sm[32];
+  const int sub = threadIdx.x & (kLpr - 1);
+  const int rows_per_block = kSpmvThreads / kLpr;
+  double acc[1] = {0.0};
+  for (int row = blockIdx.x * rows_per_block + threadIdx.x / kLpr; row < n;
+       row += gridDim.x * rows_per_block) {
+    double s = row_dot<double, double>(rp, ci, val, u, row, sub);
+#pragma unroll
+    for (int o = kLpr / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (sub == 0) {
+      const double ri = f[row] - s;
+      r[row] = ri;
+      acc[0] = fma(ri, ri, acc[0]);
+    }
+  }
+  double tot[1];
+  if (grid_sum_last<1>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+    const double rn = sqrt(fabs(tot[0]));
+    O->rr = tot[0];
+    O->rel = O->norm_b > 1e-300 ? rn / O->norm_b : rn;
+    O->scale = rn > 0.0 ? 1.0 / rn : 1.0;
+  }
+}
+
+// ||f||^2 and the first correction RHS (r64 = f, u64 = 0).
+__global__ void __launch_bounds__(kThreads)
+k_outer_init(int n, const double* __restrict__ f, double* __restrict__ r,
+             double* __restrict__ u, PcgScalars* O, double* partials, unsigned* counter) {
+  __shared__ double sm[32];
+  double acc[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double fi = f[i];
+    r[i] = fi;
+    u[i] = 0.0;
+    acc[0] = fma(fi, fi, acc[0]);
+  }
+  double tot[1];
+  if (grid_sum_last<1>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+    const double nb = sqrt(fabs(tot[0]));
+    O->norm_b = nb;
+    O->rr = tot[0];
+    O->rel = nb > 1e-300 ? 1.0 : 0.0;
+    O->scale = nb > 1e-300 ? 1.0 / nb : 1.0;
+    O->flags = nb < 1e-300 ? (kFlagDone | kFlagZeroRhs | kFlagConverged) : 0;
+    O->iter = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_accumulate(int n, double* __restrict__ u64, const float* __restrict__ d32,
+             const PcgScalars* O) {
+  const double inv = 1.0 / O->scale;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    u64[i] = fma(static_cast<double>(d32[i]), inv, u64[i]);
+}
+
+__global__ void k_cast_f32(long long n, const double* __restrict__ in, float* __restrict__ out) {
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    out[i] = static_cast<float>(in[i]);
+}
+
+}  // namespace
+
+// ── host orchestration ─────────────────────────────────────────────────────
+
+void PcgEngine::prepare(const AssembledCsr& op, bool need32, cudaStream_t s) {
+  op_ = &op;
+  n_ = op.n;
+  const size_t n = static_cast<size_t>(n_ > 0 ? n_ : 1);
+  const int vgrid = grid_for(n_, kThreads, num_sms_ * 4);
+  vec_grid_ = vgrid;
+  spmv_grid_ = grid_for(static_cast<long long>(n_) * kLpr, kSpmvThreads, num_sms_ * 8);
+  const int pmax = (vec_grid_ > spmv_grid_ ? vec_grid_ : spmv_grid_);
+  partials_.reserve(static_cast<size_t>(pmax) * 2);
+  counters_.reserve(8);
+  scal_.reserve(2);
+  VSGB_CUDA(cudaMemsetAsync(counters_.ptr, 0, sizeof(unsigned) * 8, s));
+  if (need32) {
+    val32_.reserve(static_cast<size_t>(op.nnz > 0 ? op.nnz : 1));
+    dinv32_.reserve(n);
+    k_cast_f32<<<num_sms_ * 8, kThreads, 0, s>>>(op.nnz, op.values.ptr, val32_.ptr);
+    VSGB_LAUNCH_CHECK();
+    k_cast_f32<<<num_sms_ * 4, kThreads, 0, s>>>(n_, op.dinv.ptr, dinv32_.ptr);
+    VSGB_LAUNCH_CHECK();
+    launches_ += 2;
+    has32_ = true;
+  } else {
+    has32_ = false;
+  }
+  ++generation_;
+}
+
+void PcgEngine::ensure_vectors(bool mixed) {
+  const size_t n = static_cast<size_t>(n_ > 0 ? n_ : 1);
+  r_.reserve(n);
+  z_.reserve(n);
+  p_.reserve(n);
+  Ap_.reserve(n);
+  u_.reserve(n);
+  if (mixed) {
+    r32_.reserve(n);
+    z32_.reserve(n);
+    p32a_.reserve(n);
+    p32b_.reserve(n);
+    Ap32_.reserve(n);
+    u32_.reserve(n);
+  }
+}
+
+void PcgEngine::read_scalars(cudaStream_t s, PcgScalars* host, int which) {
+  VSGB_CUDA(cudaMemcpyAsync(host, scal_.ptr + which, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+}
+
+void PcgEngine::set_limits(cudaStream_t s, int which, double tol, int max_iters) {
+  // tol / max_iters are written into the record by a tiny H2D copy before init.
+  PcgScalars h{};
+  h.tol = tol;
+  h.max_iters = max_iters;
+  VSGB_CUDA(cudaMemcpyAsync(&scal_.ptr[which].tol, &h.tol, sizeof(double), cudaMemcpyHostToDevice, s));
+  VSGB_CUDA(cudaMemcpyAsync(&scal_.ptr[which].max_iters, &h.max_iters, sizeof(int),
+                            cudaMemcpyHostToDevice, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+}
+
+void PcgEngine::launch_batch64(cudaStream_t s) {
+  const AssembledCsr& op = *op_;
+  for (int k = 0; k < check_every_; ++k) {
+    k_search64<<<vec_grid_, kThreads, 0, s>>>(n_, z_.ptr, p_.ptr, scal_.ptr);
+    k_spmv64<<<spmv_grid_, kSpmvThreads, 0, s>>>(n_, op.row_ptr.ptr, op.col_ind.ptr,
+                                                 op.values.ptr, p_.ptr, Ap_.ptr, scal_.ptr,
+                                                 partials_.ptr, counters_.ptr + 1);
+    k_update64<<<vec_grid_, kThreads, 0, s>>>(n_, u_.ptr, r_.ptr, z_.ptr, p_.ptr, Ap_.ptr,
+                                              op.dinv.ptr, scal_.ptr, partials_.ptr,
+                                              counters_.ptr + 2);
+  }
+  VSGB_LAUNCH_CHECK();
+}
+
+void PcgEngine::launch_batch32(cudaStream_t s) {
+  const AssembledCsr& op = *op_;
+  for (int k = 0; k < check_every_; ++k) {
+    float* pin = (k & 1) ? p32b_.ptr : p32a_.ptr;
+    float* pout = (k & 1) ? p32a_.ptr : p32b_.ptr;
+    k_spmv32_fused<<<spmv_grid_, kSpmvThreads, 0, s>>>(n_, op.row_ptr.ptr, op.col_ind.ptr,
+                                                       val32_.ptr, z32_.ptr, pin, pout,
+                                                       Ap32_.ptr, scal_.ptr, partials_.ptr,
+                                                       counters_.ptr + 1);
+    k_update32<<<vec_grid_, kThreads, 0, s>>>(n_, u32_.ptr, r32_.ptr, z32_.ptr, pout, Ap32_.ptr,
+                                              dinv32_.ptr, scal_.ptr, partials_.ptr,
+                                              counters_.ptr + 2);
+  }
+  VSGB_LAUNCH_CHECK();
+}
+
+// Runs batches until the device flags say done.  Uses a cached CUDA graph of
+// one batch when enabled.
+void PcgEngine::iterate(cudaStream_t s, bool fp32, PcgScalars* host) {
+  const int key = fp32 ? 1 : 0;
+  cudaGraphExec_t* exec = &graph_exec_[key];
+  if (use_graph_ && (graph_gen_[key] != generation_ || graph_batch_[key] != check_every_ ||
+                     *exec == nullptr)) {
+    if (*exec) {
+      cudaGraphExecDestroy(*exec);
+      *exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    VSGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      if (fp32)
+        launch_batch32(s);
+      else
+        launch_batch64(s);
+      VSGB_CUDA(cudaMemcpyAsync(host, scal_.ptr, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    VSGB_CUDA(cudaStreamEndCapture(s, &g));
+    VSGB_CUDA(cudaGraphInstantiate(exec, g, 0));
+    cudaGraphDestroy(g);
+    graph_gen_[key] = generation_;
+    graph_batch_[key] = check_every_;
+    graph_host_[key] = host;
+  }
+  const int per_iter = fp32 ? 2 : 3;
+  for (;;) {
+    if (use_graph_ && graph_host_[key] == host) {
+      VSGB_CUDA(cudaGraphLaunch(*exec, s));
+    } else {
+      if (fp32)
+        launch_batch32(s);
+      else
+        launch_batch64(s);
+      VSGB_CUDA(cudaMemcpyAsync(host, scal_.ptr, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    }
+    launches_ += static_cast<long long>(per_iter) * check_every_;
+    VSGB_CUDA(cudaStreamSynchronize(s));
+    if (host->flags & kFlagDone) break;
+  }
+}
+
+void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStream_t s,
+                           PcgScalars* host, SolveResult& res) {
+  ensure_vectors(false);
+  set_limits(s, 0, tol, max_iters);
+  k_init64<<<vec_grid_, kThreads, 0, s>>>(n_, d_f, op_->dinv.ptr, r_.ptr, u_.ptr, z_.ptr, p_.ptr,
+                                          scal_.ptr, partials_.ptr, counters_.ptr);
+  VSGB_LAUNCH_CHECK();
+  ++launches_;
+  read_scalars(s, host, 0);
+  res.iterations = 0;
+  res.converged = false;
+  res.rel = host->rel;
+  if (host->flags & kFlagZeroRhs) {
+    VSGB_CUDA(cudaMemsetAsync(u_.ptr, 0, sizeof(double) * n_, s));
+    res.converged = true;
+    res.rel = 0.0;
+    return;
+  }
+  if (host->flags & kFlagNonPosRz)
+    throw Error(VSGB_ERR_SINGULAR,
+                "GB300 PCG: non-positive initial r*z=" + std::to_string(host->rz) +
+                    " -- preconditioner is not SPD or matrix is singular");
+  iterate(s, false, host);
+  res.iterations = host->iter;
+  res.rel = host->rel;
+  res.converged = (host->flags & kFlagConverged) != 0;
+  res.breakdown = (host->flags & kFlagBreakdown) != 0;
+}
+
+void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int max_iters,
+                            int max_solves, cudaStream_t s, PcgScalars* host, SolveResult& res) {
+  ensure_vectors(true);
+  // Outer record (index 1) holds ||f||, the true residual and the RHS scale.
+  k_outer_init<<<vec_grid_, kThreads, 0, s>>>(n_, d_f, r_.ptr, u_.ptr, scal_.ptr + 1,
+                                              partials_.ptr, counters_.ptr + 3);
+  VSGB_LAUNCH_CHECK();
+  ++launches_;
+  PcgScalars outer{};
+  read_scalars(s, &outer, 1);
+  res.iterations = 0;
+  res.inner_solves = 0;
+  res.converged = false;
+  res.rel = outer.rel;
+  if (outer.flags & kFlagZeroRhs) {
+    res.converged = true;
+    res.rel = 0.0;
+    return;
+  }
+  set_limits(s, 0, inner_tol, max_iters);
+  double prev = 0.0;
+  bool have_prev = false;
+  for (int step = 0; step < max_solves; ++step) {
+    k_init32<<<vec_grid_, kThreads, 0, s>>>(n_, r_.ptr, 0.0, dinv32_.ptr, r32_.ptr, u32_.ptr,
+                                            z32_.ptr, p32a_.ptr, scal_.ptr, scal_.ptr + 1,
+                                            partials_.ptr, counters_.ptr);
+    VSGB_LAUNCH_CHECK();
+    ++launches_;
+    read_scalars(s, host, 0);
+    if (host->flags & kFlagNonPosRz)
+      throw Error(VSGB_ERR_SINGULAR,
+                  "GB300 PCG: non-positive initial r*z=" + std::to_string(host->rz) +
+                      " -- preconditioner is not SPD or matrix is singular");
+    if (!(host->flags & kFlagDone)) iterate(s, true, host);
+    ++res.inner_solves;
+    res.iterations += host->iter;
+    if (!(host->flags & kFlagConverged)) {
+      res.breakdown = (host->flags & kFlagBreakdown) != 0;
+      res.rel = host->rel;
+      res.inner_failed = true;
+      return;
+    }
+    k_accumulate<<<vec_grid_, kThreads, 0, s>>>(n_, u_.ptr, u32_.ptr, scal_.ptr + 1);
+    k_residual64<<<spmv_grid_, kSpmvThreads, 0, s>>>(n_, op_->row_ptr.ptr, op_->col_ind.ptr,
+                                                     op_->values.ptr, u_.ptr, d_f, r_.ptr,
+                                                     scal_.ptr + 1, partials_.ptr,
+                                                     counters_.ptr + 3);
+    VSGB_LAUNCH_CHECK();
+    launches_ += 2;
+    read_scalars(s, &outer, 1);
+    res.rel = outer.rel;
+    if (outer.rel <= tol) {
+      res.converged = true;
+      break;
+    }
+    if (have_prev && outer.rel >= prev * 0.9) {
+      res.stalled = true;
+      break;
+    }
+    prev = outer.rel;
+    have_prev = true;
+  }
+}
+
+void PcgEngine::time_spmv(int precision, int reps, cudaStream_t s, double* avg_ms) {
+  ensure_vectors(precision == VSGB_MIXED);
+  const AssembledCsr& op = *op_;
+  // Done flag cleared so the kernel does full work; scalars are scratch.
+  PcgScalars h{};
+  h.rz = 1.0;
+  h.beta = 0.5;
+  h.tol = 0.0;
+  h.max_iters = 1 << 30;
+  VSGB_CUDA(cudaMemcpyAsync(scal_.ptr, &h, sizeof(PcgScalars), cudaMemcpyHostToDevice, s));
+  VSGB_CUDA(cudaMemsetAsync(p_.ptr, 0, sizeof(double) * n_, s));
+  if (precision == VSGB_MIXED) {
+    VSGB_CUDA(cudaMemsetAsync(z32_.ptr, 0, sizeof(float) * n_, s));
+    VSGB_CUDA(cudaMemsetAsync(p32a_.ptr, 0, sizeof(float) * n_, s));
+  }
+  cudaEvent_t e0, e1;
+  VSGB_CUDA(cudaEventCreate(&e0));
+  VSGB_CUDA(cudaEventCreate(&e1));
+  auto one = [&]() {
+    if (precision == VSGB_MIXED)
+      k_spmv32_fused<<<spmv_grid_, kSpmvThreads, 0, s>>>(n_, op.row_ptr.ptr, op.col_ind.ptr,
+                                                         val32_.ptr, z32_.ptr, p32a_.ptr,
+                                                         p32b_.ptr, Ap32_.ptr, scal_.ptr,
+                                                         partials_.ptr, counters_.ptr + 1);
+    else
+      k_spmv64<<<spmv_grid_, kSpmvThreads, 0, s>>>(n_, op.row_ptr.ptr, op.col_ind.ptr,
+                                                   op.values.ptr, p_.ptr, Ap_.ptr, scal_.ptr,
+                                                   partials_.ptr, counters_.ptr + 1);
+  };
+  for (int w = 0; w < 3; ++w) one();
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  VSGB_CUDA(cudaEventRecord(e0, s));
+  for (int k = 0; k < reps; ++k) one();
+  VSGB_CUDA(cudaEventRecord(e1, s));
+  VSGB_LAUNCH_CHECK();
+  VSGB_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  VSGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  launches_ += reps + 3;
+  *avg_ms = static_cast<double>(ms) / reps;
+}
+
+double PcgEngine::spmv_bytes(int precision) const {
+  // Algorithmic bytes of one full-storage CSR SpMV: values + column indices +
+  // row pointers + x read once + y written once.
+  const double nnz = static_cast<double>(op_->nnz), n = static_cast<double>(n_);
+  if (precision == VSGB_MIXED) return 8.0 * nnz + 4.0 * (n + 1) + 8.0 * n;
+  return 12.0 * nnz + 4.0 * (n + 1) + 16.0 * n;
+}
+
+PcgEngine::~PcgEngine() {
+  for (auto& g : graph_exec_)
+    if (g) cudaGraphExecDestroy(g);
+}
+
+}  // namespace vsgb

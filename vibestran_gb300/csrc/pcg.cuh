@@ -1,0 +1,78 @@
+// vibestran_gb300/csrc/pcg.cuh — PCG engine over a resident full-storage CSR.
+#pragma once
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace vsgb {
+
+struct SolveResult {
+  int iterations = 0;
+  int inner_solves = 1;
+  bool converged = false;
+  bool breakdown = false;
+  bool stalled = false;
+  bool inner_failed = false;
+  double rel = 0.0;
+};
+
+class PcgEngine {
+ public:
+  explicit PcgEngine(int num_sms) : num_sms_(num_sms) {}
+  ~PcgEngine();
+  PcgEngine(const PcgEngine&) = delete;
+  PcgEngine& operator=(const PcgEngine&) = delete;
+
+  // Binds the operator; builds the FP32 copy when need32.
+  void prepare(const AssembledCsr& op, bool need32, cudaStream_t s);
+  bool has32() const { return has32_; }
+
+  // FP64 PCG on d_f; the solution is left in solution().
+  void solve_fp64(const double* d_f, double tol, int max_iters, cudaStream_t s,
+                  PcgScalars* host_pinned, SolveResult& res);
+  // FP32 inner PCG + FP64 refinement on the GPU; solution in solution().
+  void solve_mixed(const double* d_f, double tol, double inner_tol, int max_iters,
+                   int max_solves, cudaStream_t s, PcgScalars* host_pinned, SolveResult& res);
+
+  const double* solution() const { return u_.ptr; }
+  void time_spmv(int precision, int reps, cudaStream_t s, double* avg_ms);
+  double spmv_bytes(int precision) const;
+
+  void set_check_every(int k) { check_every_ = k < 2 ? 2 : (k + (k & 1)); }
+  void set_use_graph(bool g) { use_graph_ = g; }
+  long long launches() const { return launches_; }
+  void add_launches(long long k) { launches_ += k; }
+  int num_sms() const { return num_sms_; }
+
+ private:
+  void ensure_vectors(bool mixed);
+  void read_scalars(cudaStream_t s, PcgScalars* host, int which);
+  void set_limits(cudaStream_t s, int which, double tol, int max_iters);
+  void launch_batch64(cudaStream_t s);
+  void launch_batch32(cudaStream_t s);
+  void iterate(cudaStream_t s, bool fp32, PcgScalars* host);
+
+  int num_sms_;
+  const AssembledCsr* op_ = nullptr;
+  int n_ = 0;
+  int vec_grid_ = 1, spmv_grid_ = 1;
+  int check_every_ = 16;
+  bool use_graph_ = true;
+  bool has32_ = false;
+  long long launches_ = 0;
+  unsigned generation_ = 0;
+
+  DevBuf<float> val32_, dinv32_;
+  DevBuf<double> r_, z_, p_, Ap_, u_;
+  DevBuf<float> r32_, z32_, p32a_, p32b_, Ap32_, u32_;
+  DevBuf<PcgScalars> scal_;
+  DevBuf<double> partials_;
+  DevBuf<unsigned> counters_;
+
+  cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
+  unsigned graph_gen_[2] = {0, 0};
+  int graph_batch_[2] = {0, 0};
+  PcgScalars* graph_host_[2] = {nullptr, nullptr};
+};
+
+}  // namespace vsgb
