@@ -128,7 +128,7 @@ void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
   const int n = c->K.n;
   c->u.reserve(static_cast<size_t>(n) * nrhs);
   vsgb_stats st{};
-  st.format = 1;
+  st.format = c->eng->format_used();
   st.inner_solves = 0;
   st.converged = 1;
   float ms_total = 0.f;
@@ -261,6 +261,8 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
         break;
       case VSGB_OPT_FORMAT:
         c->format = static_cast<int>(value);
+        c->eng->set_format(c->format);
+        if (c->assembled) c->eng->prepare(c->K, c->precision == VSGB_MIXED, c->stream);
         break;
       default:
         throw Error(VSGB_ERR_INVALID, "unknown option " + std::to_string(option));
@@ -298,6 +300,9 @@ int vsgb_solve_csr(vsgb_ctx* c, int n, int nnz, const int* row_ptr, const int* c
       throw Error(VSGB_ERR_INVALID, "vsgb_solve_csr: invalid argument");
     if (row_ptr[0] != 0 || row_ptr[n] != nnz)
       throw Error(VSGB_ERR_INVALID, "vsgb_solve_csr: row_ptr does not span nnz");
+    for (int r = 0; r < n; ++r)
+      if (row_ptr[r + 1] < row_ptr[r])
+        throw Error(VSGB_ERR_INVALID, "vsgb_solve_csr: row_ptr decreases at row " + std::to_string(r));
     cudaStream_t s = c->stream;
     VSGB_CUDA(cudaEventRecord(c->ev[2], s));
     c->in_rp.reserve(static_cast<size_t>(n) + 1);
@@ -335,6 +340,15 @@ int vsgb_mesh_upload(vsgb_ctx* c, int n_nodes, const double* node_xyz, const int
         (n_elem > 0 && (!conn || !E || !nu)))
       throw Error(VSGB_ERR_INVALID, "vsgb_mesh_upload: invalid argument");
     if (n_elem > INT_MAX / 8) throw Error(VSGB_ERR_LIMIT, "too many elements");
+    // Every index a kernel will dereference is range-checked here, on the host.
+    for (long long k = 0; k < 8LL * n_elem; ++k)
+      if (conn[k] < 0 || conn[k] >= n_nodes)
+        throw Error(VSGB_ERR_INVALID, "element index " + std::to_string(k / 8) +
+                                          " references a node index out of range");
+    for (long long k = 0; k < 3LL * n_nodes; ++k)
+      if (node_eq3[k] < -1 || node_eq3[k] >= n_dof)
+        throw Error(VSGB_ERR_INVALID, "equation index out of range at node index " +
+                                          std::to_string(k / 3));
     cudaStream_t s = c->stream;
     c->n_nodes = n_nodes;
     c->n_elem = n_elem;

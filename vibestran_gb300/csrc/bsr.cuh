@@ -1,0 +1,36 @@
+// vibestran_gb300/csrc/bsr.cuh — 3x3 node-block sliced-ELL operator.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace vsgb {
+
+struct BsrSell {
+  int nb = 0;              // block rows (n / 3)
+  int nslices = 0;         // ceil(nb / 8)
+  long long steps = 0;     // 32-lane steps over all slices
+  long long nblocks = 0;   // stored (non-padding) blocks
+  bool valid = false, has64 = false, has32 = false;
+  DevBuf<int> slice_ptr;   // nslices + 1, in steps
+  DevBuf<int> rowlen;      // blocks per block row
+  DevBuf<int> cols;        // steps * 32
+  DevBuf<double> val64;    // steps * 32 * 9
+  DevBuf<float> val32;     // steps * 32 * 9
+  DevBuf<int> tmp;
+  DevBuf<long long> total;
+  std::vector<int> h_blen;
+};
+
+// Converts the full-storage CSR into the block layout; returns false (and
+// leaves B.valid false) when the equations are not node-aligned triples or the
+// blocks are less than 90% filled.
+bool build_bsr(const AssembledCsr& K, BsrSell& B, bool need64, bool need32, int num_sms,
+               cudaStream_t s);
+
+// Algorithmic bytes of one block SpMV (values + block indices + x + y).
+double bsr_bytes(const BsrSell& B, int precision);
+
+}  // namespace vsgb

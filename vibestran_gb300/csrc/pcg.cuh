@@ -1,6 +1,7 @@
 // vibestran_gb300/csrc/pcg.cuh — PCG engine over a resident full-storage CSR.
 #pragma once
 
+#include "bsr.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -40,6 +41,9 @@ class PcgEngine {
 
   void set_check_every(int k) { check_every_ = k < 2 ? 2 : (k + (k & 1)); }
   void set_use_graph(bool g) { use_graph_ = g; }
+  // 0 auto (3x3 blocks when node-aligned), 1 scalar CSR, 2 blocks required.
+  void set_format(int f) { format_ = f; }
+  int format_used() const { return use_bsr_ ? 2 : 1; }
   long long launches() const { return launches_; }
   void add_launches(long long k) { launches_ += k; }
   int num_sms() const { return num_sms_; }
@@ -48,6 +52,9 @@ class PcgEngine {
   void ensure_vectors(bool mixed);
   void read_scalars(cudaStream_t s, PcgScalars* host, int which);
   void set_limits(cudaStream_t s, int which, double tol, int max_iters);
+  void launch_spmv64(cudaStream_t s, const double* x, double* y);
+  void launch_spmv32(cudaStream_t s, const float* pin, float* pout);
+  void launch_residual64(cudaStream_t s, const double* d_f);
   void launch_batch64(cudaStream_t s);
   void launch_batch32(cudaStream_t s);
   void iterate(cudaStream_t s, bool fp32, PcgScalars* host);
@@ -62,6 +69,10 @@ class PcgEngine {
   long long launches_ = 0;
   unsigned generation_ = 0;
 
+  BsrSell bsr_;
+  bool use_bsr_ = false;
+  int format_ = 0;
+  int bsr_grid_ = 1;
   DevBuf<float> val32_, dinv32_;
   DevBuf<double> r_, z_, p_, Ap_, u_;
   DevBuf<float> r32_, z32_, p32a_, p32b_, Ap32_, u32_;
