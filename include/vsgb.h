@@ -173,6 +173,34 @@ int vsgb_time_spmv(vsgb_ctx* ctx, int precision, int reps, double* avg_ms, doubl
 /* Number of kernels this context launched since creation. */
 long long vsgb_kernel_launches(vsgb_ctx* ctx);
 
+/* ── allocation-free solve ──────────────────────────────────────────────── */
+
+/* Largest system (equations) vsgb_pcg_solve_noalloc accepts. */
+#define VSGB_NOALLOC_MAX_N 65536
+
+/* FP64 Jacobi PCG that allocates no GPU or pinned memory, for callers that
+ * cannot call cudaMalloc: code running inside another framework's memory pool,
+ * or a latency-critical loop where an allocation (which may synchronise the
+ * device or fail under memory pressure) is not allowed.  This entry point has
+ * no counterpart in the reference; it is the cuda-pcg FP64 Jacobi iteration
+ * (same recurrence, convergence test and error texts as vsgb_solve_csr) on
+ * caller-owned DEVICE buffers:
+ *   d_row_ptr[n+1], d_col_ind[nnz], d_values[nnz] — FULL-storage symmetric CSR
+ *   (both triangles), d_F[n] in, d_u[n] out; `stream` is a cudaStream_t (NULL =
+ *   legacy default stream) of the current device.
+ * Its scratch (inverse diagonal, r, z, p, Ap, reduction partials, scalars;
+ * about 2.7 MB) is one static __device__ array that every GPU loading the
+ * library holds until exit, so n is limited to VSGB_NOALLOC_MAX_N (larger n
+ * returns VSGB_ERR_LIMIT).  The first call on a device resolves the array's
+ * device address — make it before any stream capture on that device.  All
+ * calls share the array: calls that overlap on the GPU (other streams or
+ * host threads) race and must be serialised by the caller.  err receives the
+ * message of a failure (may be NULL). */
+int vsgb_pcg_solve_noalloc(int n, int nnz, const int* d_row_ptr, const int* d_col_ind,
+                           const double* d_values, const double* d_F, double* d_u, double tol,
+                           int max_iters, void* stream, int* iterations_out,
+                           double* rel_residual_out, char* err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

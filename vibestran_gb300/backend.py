@@ -60,8 +60,9 @@ EXPORTS = (
     "vsgb_assemble_chexa8", "vsgb_copy_csr_lower", "vsgb_solve_assembled", "vsgb_mesh_upload",
     "vsgb_assemble_resident", "vsgb_rhs_upload", "vsgb_solve_resident",
     "vsgb_solution_download", "vsgb_element_sensitivity", "vsgb_timer_start",
-    "vsgb_timer_stop", "vsgb_time_spmv", "vsgb_kernel_launches",
+    "vsgb_timer_stop", "vsgb_time_spmv", "vsgb_kernel_launches", "vsgb_pcg_solve_noalloc",
 )
+NOALLOC_MAX_N = 65536  # VSGB_NOALLOC_MAX_N
 
 
 class SolverError(RuntimeError):
@@ -130,6 +131,8 @@ def load_library(build_if_missing: bool = False):
     L.vsgb_time_spmv.argtypes = [vp, c_int, c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)]
     L.vsgb_kernel_launches.argtypes = [vp]
     L.vsgb_kernel_launches.restype = c_ll
+    L.vsgb_pcg_solve_noalloc.argtypes = [c_int, c_int, vp, vp, vp, vp, vp, c_dbl, c_int, vp,
+                                         ctypes.POINTER(c_int), ctypes.POINTER(c_dbl), cp, sz]
     _lib = L
     return L
 

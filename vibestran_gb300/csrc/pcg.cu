@@ -21,6 +21,8 @@
 // FP64 FMA rate for the FP64 path.
 
 #include <cmath>
+#include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -886,4 +888,212 @@ PcgEngine::~PcgEngine() {
     if (g) cudaGraphExecDestroy(g);
 }
 
+// ── Allocation-free FP64 PCG (vsgb_pcg_solve_noalloc) ─────────────────────
+//
+// For callers that must not allocate GPU memory: code that runs inside
+// another framework's memory pool, or a latency-critical loop where a
+// cudaMalloc (which can synchronise the device and can fail under memory
+// pressure) is not allowed.  The solver's scratch — Jacobi inverse diagonal,
+// r, z, p, Ap, the per-block reduction partials, the grid-reduction counters
+// and the PCG scalar record — lives in one file-scope __device__ array of
+// kNoAllocScratchBytes, held by every GPU that loads the library until the
+// process exits.  Systems are limited to VSGB_NOALLOC_MAX_N equations.
+
+namespace {
+
+constexpr int kNoAllocMaxGrid = 4096;  // blocks of any launch below
+constexpr size_t kNoAllocVecBytes = sizeof(double) * VSGB_NOALLOC_MAX_N;
+constexpr size_t kNoAllocPartialsBytes = sizeof(double) * 2 * kNoAllocMaxGrid;
+constexpr size_t kNoAllocCounterBytes = 256;
+constexpr size_t kNoAllocScalarsBytes = 256;
+constexpr size_t kNoAllocErrorBytes = 256;
+constexpr size_t kNoAllocScratchBytes = 5 * kNoAllocVecBytes + kNoAllocPartialsBytes +
+                                        kNoAllocCounterBytes + kNoAllocScalarsBytes +
+                                        kNoAllocErrorBytes;
+static_assert(sizeof(PcgScalars) <= kNoAllocScalarsBytes, "scalar record");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch per device (a host-side copy of the
+// symbol is only a stand-in, never a device address).
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+struct NoAllocError {
+  int code;  // 0 ok, 2 column out of range, 4 zero diagonal, 5 missing diagonal
+  int index;
+};
+
+// Column range check and Jacobi inverse diagonal of a full-storage CSR
+// (first entry with col == row, as build_jacobi_diagonal).
+__global__ void k_noalloc_diag(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                               const double* __restrict__ v, double* __restrict__ dinv,
+                               NoAllocError* err) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int b = rp[r], e = rp[r + 1];
+  bool found = false;
+  for (int k = b; k < e; ++k) {
+    const int c = ci[k];
+    if (c < 0 || c >= n) {
+      if (atomicCAS(&err->code, 0, 2) == 0) err->index = r;
+      dinv[r] = 0.0;
+      return;
+    }
+    if (!found && c == r) {
+      found = true;
+      if (v[k] == 0.0) {
+        if (atomicCAS(&err->code, 0, 4) == 0) err->index = r;
+        dinv[r] = 0.0;
+      } else {
+        dinv[r] = 1.0 / v[k];
+      }
+    }
+  }
+  if (!found) {
+    if (atomicCAS(&err->code, 0, 5) == 0) err->index = r;
+    dinv[r] = 0.0;
+  }
+}
+
+void noalloc_err(char* err, size_t len, const std::string& m) {
+  if (err && len > 0) std::snprintf(err, len, "%s", m.c_str());
+}
+
+}  // namespace
+
 }  // namespace vsgb
+
+extern "C" int vsgb_pcg_solve_noalloc(int n, int nnz, const int* d_row_ptr, const int* d_col_ind,
+                                      const double* d_values, const double* d_F, double* d_u,
+                                      double tol, int max_iters, void* stream,
+                                      int* iterations_out, double* rel_residual_out, char* err,
+                                      size_t errlen) {
+  using namespace vsgb;
+  if (iterations_out) *iterations_out = 0;
+  if (rel_residual_out) *rel_residual_out = 0.0;
+  if (n <= 0) {
+    noalloc_err(err, errlen, "CUDA PCG: stiffness matrix is empty -- no free DOFs");
+    return VSGB_ERR_INVALID;
+  }
+  if (n > VSGB_NOALLOC_MAX_N) {
+    noalloc_err(err, errlen, "vsgb_pcg_solve_noalloc: n = " + std::to_string(n) +
+                                 " exceeds the allocation-free limit of " +
+                                 std::to_string(VSGB_NOALLOC_MAX_N) + " equations");
+    return VSGB_ERR_LIMIT;
+  }
+  if (nnz < 0 || !d_row_ptr || (nnz > 0 && (!d_col_ind || !d_values)) || !d_F || !d_u) {
+    noalloc_err(err, errlen, "vsgb_pcg_solve_noalloc: invalid argument");
+    return VSGB_ERR_INVALID;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0;
+  int num_sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices ||
+      cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    noalloc_err(err, errlen, "vsgb_pcg_solve_noalloc: no usable current device");
+    return VSGB_ERR_NO_DEVICE;
+  }
+  unsigned char* base = nullptr;
+  {
+    // First call on a device resolves the scratch address (do it before any
+    // stream capture on that device).
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        noalloc_err(err, errlen, std::string("cudaGetSymbolAddress failed: ") +
+                                     cudaGetErrorString(e));
+        return VSGB_ERR_CUDA;
+      }
+      g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  double* dinv = reinterpret_cast<double*>(base);
+  double* r = reinterpret_cast<double*>(base + kNoAllocVecBytes);
+  double* z = reinterpret_cast<double*>(base + 2 * kNoAllocVecBytes);
+  double* p = reinterpret_cast<double*>(base + 3 * kNoAllocVecBytes);
+  double* Ap = reinterpret_cast<double*>(base + 4 * kNoAllocVecBytes);
+  unsigned char* tail = base + 5 * kNoAllocVecBytes;
+  double* partials = reinterpret_cast<double*>(tail);
+  unsigned* counters = reinterpret_cast<unsigned*>(tail + kNoAllocPartialsBytes);
+  PcgScalars* S = reinterpret_cast<PcgScalars*>(tail + kNoAllocPartialsBytes + kNoAllocCounterBytes);
+  NoAllocError* derr = reinterpret_cast<NoAllocError*>(tail + kNoAllocPartialsBytes +
+                                                        kNoAllocCounterBytes + kNoAllocScalarsBytes);
+  const int vec_grid = grid_for(n, kThreads, num_sms * 4);
+  const int spmv_grid = grid_for(static_cast<long long>(n) * kLpr, kSpmvThreads, num_sms * 8);
+  if (vec_grid > kNoAllocMaxGrid || spmv_grid > kNoAllocMaxGrid) {
+    noalloc_err(err, errlen, "vsgb_pcg_solve_noalloc: launch grid exceeds the scratch layout");
+    return VSGB_ERR_LIMIT;
+  }
+  auto cuda_fail = [&](cudaError_t e, const char* what) {
+    noalloc_err(err, errlen, std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+    return VSGB_ERR_CUDA;
+  };
+  cudaError_t e;
+  // The array keeps the previous call's contents: counters, error record and
+  // the scalar limits are reset here; vectors are fully rewritten by k_init64.
+  if ((e = cudaMemsetAsync(counters, 0, kNoAllocCounterBytes, s)) != cudaSuccess)
+    return cuda_fail(e, "reset counters");
+  if ((e = cudaMemsetAsync(derr, 0, sizeof(NoAllocError), s)) != cudaSuccess)
+    return cuda_fail(e, "reset error record");
+  PcgScalars h{};
+  h.tol = tol > 0.0 ? tol : 1e-8;
+  h.max_iters = max_iters > 0 ? max_iters : 10000;
+  if ((e = cudaMemcpyAsync(S, &h, sizeof(PcgScalars), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    return cuda_fail(e, "write limits");
+  k_noalloc_diag<<<grid_for(n, kThreads, 1 << 30), kThreads, 0, s>>>(n, d_row_ptr, d_col_ind,
+                                                                      d_values, dinv, derr);
+  NoAllocError herr{};
+  if ((e = cudaMemcpyAsync(&herr, derr, sizeof(herr), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return cuda_fail(e, "diagonal check");
+  if (herr.code == 2) {
+    noalloc_err(err, errlen, "column index out of range in row " + std::to_string(herr.index));
+    return VSGB_ERR_INVALID;
+  }
+  if (herr.code == 4 || herr.code == 5) {
+    noalloc_err(err, errlen, std::string("CUDA PCG: ") + (herr.code == 4 ? "zero" : "missing") +
+                                 " diagonal at row " + std::to_string(herr.index) +
+                                 " -- matrix is singular. Check boundary conditions.");
+    return VSGB_ERR_SINGULAR;
+  }
+  k_init64<<<vec_grid, kThreads, 0, s>>>(n, d_F, dinv, r, d_u, z, p, S, partials, counters);
+  if ((e = cudaMemcpyAsync(&h, S, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return cuda_fail(e, "PCG init");
+  if (h.flags & kFlagZeroRhs) return VSGB_OK;  // u = 0, 0 iterations
+  if (h.flags & kFlagNonPosRz) {
+    noalloc_err(err, errlen, "CUDA PCG: non-positive initial r*z=" + std::to_string(h.rz) +
+                                 " -- preconditioner is not SPD or matrix is singular");
+    return VSGB_ERR_SINGULAR;
+  }
+  const int check_every = 16;
+  const long long max_batches = (h.max_iters + check_every - 1) / check_every + 4;
+  for (long long batch = 0; batch <= max_batches; ++batch) {
+    for (int k = 0; k < check_every; ++k) {
+      k_search64<<<vec_grid, kThreads, 0, s>>>(n, z, p, S);
+      k_spmv64<<<spmv_grid, kSpmvThreads, 0, s>>>(n, d_row_ptr, d_col_ind, d_values, p, Ap, S,
+                                                  partials, counters + 1);
+      k_update64<<<vec_grid, kThreads, 0, s>>>(n, d_u, r, z, p, Ap, dinv, S, partials,
+                                               counters + 2);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "PCG launch");
+    if ((e = cudaMemcpyAsync(&h, S, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+      return cuda_fail(e, "PCG iteration");
+    if (h.flags & kFlagDone) break;
+  }
+  if (iterations_out) *iterations_out = h.iter;
+  if (rel_residual_out) *rel_residual_out = h.rel;
+  if (!(h.flags & kFlagConverged) || h.iter >= h.max_iters) {
+    noalloc_err(err, errlen, "CUDA PCG: did not converge after " + std::to_string(h.max_iters) +
+                                 " iterations (relative residual " + std::to_string(h.rel) +
+                                 " > tolerance " + std::to_string(h.tol) + ")");
+    return VSGB_ERR_NOT_CONVERGED;
+  }
+  return VSGB_OK;
+}
