@@ -55,6 +55,7 @@ extern "C" {
 #define VSGB_OPT_CHECK_EVERY 6    /* iterations launched between host convergence checks */
 #define VSGB_OPT_USE_GRAPH 7      /* 1: replay iteration batches as CUDA graphs (default 1) */
 #define VSGB_OPT_FORMAT 8         /* 0 auto, 1 scalar CSR, 2 3x3 node blocks */
+#define VSGB_OPT_RESIDENT 9       /* 1: one persistent launch per PCG solve (default 1) */
 
 typedef struct vsgb_ctx vsgb_ctx;
 

@@ -52,6 +52,7 @@ OPT_MAX_SOLVES = 5
 OPT_CHECK_EVERY = 6
 OPT_USE_GRAPH = 7
 OPT_FORMAT = 8
+OPT_RESIDENT = 9
 
 # The symbols include/vsgb.h declares (checked by tests against the .so).
 EXPORTS = (

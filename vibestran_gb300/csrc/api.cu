@@ -264,6 +264,10 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
         c->eng->set_format(c->format);
         if (c->assembled) c->eng->prepare(c->K, c->precision == VSGB_MIXED, c->stream);
         break;
+      case VSGB_OPT_RESIDENT:
+        c->eng->set_resident(value != 0.0);
+        if (c->assembled) c->eng->prepare(c->K, c->precision == VSGB_MIXED, c->stream);
+        break;
       default:
         throw Error(VSGB_ERR_INVALID, "unknown option " + std::to_string(option));
     }

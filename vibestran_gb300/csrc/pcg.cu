@@ -391,29 +391,42 @@ struct BsrView {
 template <typename T, typename Gather>
 __device__ __forceinline__ void bsr_row_block(const BsrView& B, const T* __restrict__ vals,
                                               int sl, int lane, Gather gx, T& y0, T& y1, T& y2) {
-  const int r = lane >> 2, q = lane & 3;
-  const int R = sl * 8 + r;
-  const int len = R < B.nb ? B.rowlen[R] : 0;
   const int base = B.slice_ptr[sl], steps = B.slice_ptr[sl + 1] - base;
   y0 = y1 = y2 = T(0);
-#pragma unroll 2
-  for (int t = 0; t < steps; ++t) {
-    if (4 * t + q < len) {
-      const size_t st = static_cast<size_t>(base + t);
-      const int c = __ldg(&B.cols[st * 32 + lane]);
-      const T* v = vals + st * 288 + lane;
-      T x0, x1, x2;
-      gx(c, x0, x1, x2);
-      y0 = fmat(__ldg(v + 0), x0, y0);
-      y0 = fmat(__ldg(v + 32), x1, y0);
-      y0 = fmat(__ldg(v + 64), x2, y0);
-      y1 = fmat(__ldg(v + 96), x0, y1);
-      y1 = fmat(__ldg(v + 128), x1, y1);
-      y1 = fmat(__ldg(v + 160), x2, y1);
-      y2 = fmat(__ldg(v + 192), x0, y2);
-      y2 = fmat(__ldg(v + 224), x1, y2);
-      y2 = fmat(__ldg(v + 256), x2, y2);
+  // Branch-free over the slice's steps: padding slots hold block column 0 and
+  // zero values (allocated and zero-filled), so they add nothing, and the
+  // loads of several steps can be in flight at once.
+  const int* cp = B.cols + static_cast<size_t>(base) * 32 + lane;
+  const T* vp = vals + static_cast<size_t>(base) * 288 + lane;
+  int t = 0;
+  for (; t + 2 <= steps; t += 2) {
+    const int c0 = __ldcg(cp + 32 * t), c1 = __ldcg(cp + 32 * (t + 1));
+    T a[2][9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      a[0][k] = __ldcg(vp + 288 * t + 32 * k);
+      a[1][k] = __ldcg(vp + 288 * (t + 1) + 32 * k);
     }
+    T x0, x1, x2, w0, w1, w2;
+    gx(c0, x0, x1, x2);
+    gx(c1, w0, w1, w2);
+    y0 = fmat(a[0][0], x0, fmat(a[0][1], x1, fmat(a[0][2], x2, y0)));
+    y1 = fmat(a[0][3], x0, fmat(a[0][4], x1, fmat(a[0][5], x2, y1)));
+    y2 = fmat(a[0][6], x0, fmat(a[0][7], x1, fmat(a[0][8], x2, y2)));
+    y0 = fmat(a[1][0], w0, fmat(a[1][1], w1, fmat(a[1][2], w2, y0)));
+    y1 = fmat(a[1][3], w0, fmat(a[1][4], w1, fmat(a[1][5], w2, y1)));
+    y2 = fmat(a[1][6], w0, fmat(a[1][7], w1, fmat(a[1][8], w2, y2)));
+  }
+  if (t < steps) {
+    const int c0 = __ldcg(cp + 32 * t);
+    T a[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a[k] = __ldcg(vp + 288 * t + 32 * k);
+    T x0, x1, x2;
+    gx(c0, x0, x1, x2);
+    y0 = fmat(a[0], x0, fmat(a[1], x1, fmat(a[2], x2, y0)));
+    y1 = fmat(a[3], x0, fmat(a[4], x1, fmat(a[5], x2, y1)));
+    y2 = fmat(a[6], x0, fmat(a[7], x1, fmat(a[8], x2, y2)));
   }
 #pragma unroll
   for (int o = 1; o <= 2; o <<= 1) {
@@ -558,6 +571,13 @@ void PcgEngine::prepare(const AssembledCsr& op, bool need32, cudaStream_t s) {
   bsr_grid_ = use_bsr_ ? grid_for(static_cast<long long>(bsr_.nslices) * 32, kSpmvThreads,
                                   1 << 30)
                        : 1;
+  res_.ok32 = res_.ok64 = false;
+  if (use_bsr_ && resident_) {
+    int dev = 0;
+    VSGB_CUDA(cudaGetDevice(&dev));
+    resident_prepare(bsr_, op.dinv.ptr, need32, dev, num_sms_, res_, s);
+    launches_ += 2;
+  }
   int pmax = (vec_grid_ > spmv_grid_ ? vec_grid_ : spmv_grid_);
   if (bsr_grid_ > pmax) pmax = bsr_grid_;
   partials_.reserve(static_cast<size_t>(pmax) * 2);
@@ -744,6 +764,22 @@ void PcgEngine::iterate(cudaStream_t s, bool fp32, PcgScalars* host) {
 void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStream_t s,
                            PcgScalars* host, SolveResult& res) {
   ensure_vectors(false);
+  if (resident_used(false)) {
+    resident_solve64(bsr_, res_, d_f, u_.ptr, scal_.ptr, tol, max_iters, s, op_->dinv.ptr);
+    ++launches_;
+    read_scalars(s, host, 0);
+    if (host->flags & kFlagResidentAbort)
+      throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
+    if (host->flags & kFlagNonPosRz)
+      throw Error(VSGB_ERR_SINGULAR,
+                  "GB300 PCG: non-positive initial r*z=" + std::to_string(host->rz) +
+                      " -- preconditioner is not SPD or matrix is singular");
+    res.iterations = host->iter;
+    res.rel = host->rel;
+    res.converged = (host->flags & kFlagConverged) != 0;
+    res.breakdown = (host->flags & kFlagBreakdown) != 0;
+    return;
+  }
   set_limits(s, 0, tol, max_iters);
   k_init64<<<vec_grid_, kThreads, 0, s>>>(n_, d_f, op_->dinv.ptr, r_.ptr, u_.ptr, z_.ptr, p_.ptr,
                                           scal_.ptr, partials_.ptr, counters_.ptr);
@@ -793,6 +829,44 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
   double prev = 0.0;
   bool have_prev = false;
   for (int step = 0; step < max_solves; ++step) {
+    if (resident_used(true)) {
+      // One launch: FP32 inner solve of the scaled correction and the FP64
+      // accumulation u += delta / scale.
+      resident_solve32(bsr_, res_, r_.ptr, u_.ptr, scal_.ptr, scal_.ptr + 1, inner_tol,
+                       max_iters, s, op_->dinv.ptr);
+      ++launches_;
+      read_scalars(s, host, 0);
+      if (host->flags & kFlagResidentAbort)
+        throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
+      if (host->flags & kFlagNonPosRz)
+        throw Error(VSGB_ERR_SINGULAR,
+                    "GB300 PCG: non-positive initial r*z=" + std::to_string(host->rz) +
+                        " -- preconditioner is not SPD or matrix is singular");
+      ++res.inner_solves;
+      res.iterations += host->iter;
+      if (!(host->flags & kFlagConverged)) {
+        res.breakdown = (host->flags & kFlagBreakdown) != 0;
+        res.rel = host->rel;
+        res.inner_failed = true;
+        return;
+      }
+      launch_residual64(s, d_f);
+      VSGB_LAUNCH_CHECK();
+      ++launches_;
+      read_scalars(s, &outer, 1);
+      res.rel = outer.rel;
+      if (outer.rel <= tol) {
+        res.converged = true;
+        break;
+      }
+      if (have_prev && outer.rel >= prev * 0.9) {
+        res.stalled = true;
+        break;
+      }
+      prev = outer.rel;
+      have_prev = true;
+      continue;
+    }
     k_init32<<<vec_grid_, kThreads, 0, s>>>(n_, r_.ptr, 0.0, dinv32_.ptr, r32_.ptr, u32_.ptr,
                                             z32_.ptr, p32a_.ptr, scal_.ptr, scal_.ptr + 1,
                                             partials_.ptr, counters_.ptr);

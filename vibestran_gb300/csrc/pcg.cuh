@@ -4,6 +4,7 @@
 #include "bsr.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
+#include "resident.cuh"
 
 namespace vsgb {
 
@@ -44,6 +45,11 @@ class PcgEngine {
   // 0 auto (3x3 blocks when node-aligned), 1 scalar CSR, 2 blocks required.
   void set_format(int f) { format_ = f; }
   int format_used() const { return use_bsr_ ? 2 : 1; }
+  // Persistent one-launch-per-solve kernels on the block operator (default on).
+  void set_resident(bool r) { resident_ = r; }
+  bool resident_used(bool mixed) const {
+    return resident_ && use_bsr_ && (mixed ? res_.ok32 : res_.ok64);
+  }
   long long launches() const { return launches_; }
   void add_launches(long long k) { launches_ += k; }
   int num_sms() const { return num_sms_; }
@@ -70,6 +76,8 @@ class PcgEngine {
   unsigned generation_ = 0;
 
   BsrSell bsr_;
+  ResidentPlan res_;
+  bool resident_ = true;
   bool use_bsr_ = false;
   int format_ = 0;
   int bsr_grid_ = 1;

@@ -1,0 +1,663 @@
+// vibestran_gb300/csrc/resident.cu — persistent Jacobi PCG (one launch per solve).
+//
+// Why: per PCG iteration the launch-per-kernel form pays two or three kernel
+// boundaries (~2 us each on GB300) plus per-kernel reduction tails, while the
+// FP32 block operator of the 84k-element cantilever (94 MB) fits in the 126 MB
+// L2, where it streams at ~18-22 TB/s (vs ~7 TB/s from HBM).  Here one
+// cooperative launch keeps one CTA per SM for the whole solve:
+//   * each CTA owns a step-balanced, contiguous range of block-row slices, so
+//     its rows are the contiguous equations [24*s0, 24*s1);
+//   * the CTA's own vectors (r, z, u, p, Ap, diag^-1) live in shared memory;
+//   * each iteration first stages x = z + beta*p over the CTA's column window
+//     into shared memory (one L2 read per needed node instead of one per
+//     block), then streams its slices of the operator from L2;
+//   * the two dot-product reductions per iteration are grid-wide: per-CTA
+//     partials, a bounded-spin grid barrier, and a fixed-order sum that every
+//     CTA computes identically (so all CTAs take the same branch).
+// The recurrence, convergence test and breakdown / zero-RHS handling are those
+// of run_pcg_prepared (src/solver/cuda_pcg_backend_impl.hpp:1688-1999).
+
+#include <algorithm>
+#include <climits>
+
+#include "kernels.cuh"
+#include "resident.cuh"
+
+namespace vsgb {
+
+namespace {
+
+constexpr int kResThreads = 512;
+constexpr int kResWarps = kResThreads / 32;
+constexpr long long kSpinLimit = 1LL << 22;  // ~1 s of polling, then abort
+constexpr int kFlagAbort = 64;
+
+template <typename T>
+struct ResArgs {
+  int nb, n;
+  const int* __restrict__ slice_ptr;
+  const int* __restrict__ cols;
+  const T* __restrict__ vals;
+  const int* __restrict__ cta_slice;
+  const int* __restrict__ cta_win;
+  const double* __restrict__ dinv;
+  const double* __restrict__ rhs;
+  double* __restrict__ u_out;
+  T* z4;
+  T* p4a;
+  T* p4b;
+  double* partials;
+  unsigned* count;
+  int* abort_flag;
+  PcgScalars* S;
+  const PcgScalars* O;
+  double tol;
+  int max_iters;
+  int rows_max;  // own-row stride of the shared-memory vectors
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid barrier over a monotonic counter; false when it gave up (the abort flag
+// is then set for every CTA).
+__device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, int* s_ok) {
+  target += gridDim.x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(count, 1u);
+    int ok = 1;
+    long long spins = 0;
+    while (ld_acquire_u32(count) < target) {
+      if (*reinterpret_cast<volatile int*>(abort_flag)) {
+        ok = 0;
+        break;
+      }
+      if (++spins > kSpinLimit) {
+        atomicExch(abort_flag, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+// Grid-wide sum of NV doubles: CTA sums -> partial slot -> barrier -> fixed
+// order sum by warp 0 of every CTA (bitwise identical in all CTAs).
+// Per-thread partials are summed over the warp in their own precision A (FP32
+// in the FP32 solve: GB300 runs FP64 at 1/58 of the FP32 rate), then the
+// kResWarps warp sums and the CTA partials are added in FP64, in fixed order.
+template <typename A, int NV>
+__device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned* count,
+                               unsigned& target, int* abort_flag, double* sm, int* s_ok,
+                               double (&tot)[NV]) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sm[wid * NV + k] = static_cast<double>(v[k]);
+  __syncthreads();
+  double* part = partials + static_cast<size_t>(slot) * gridDim.x * NV;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < kResWarps; ++w) s += sm[w * NV + k];
+      part[blockIdx.x * NV + k] = s;
+    }
+  }
+  const bool ok = grid_sync(count, target, abort_flag, s_ok);
+  if (threadIdx.x < 32) {
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    for (unsigned c = threadIdx.x; c < gridDim.x; c += 32)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] += __ldcg(&part[c * NV + k]);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = warp_sum(acc[k]);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) sm[32 * NV + k] = acc[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = sm[32 * NV + k];
+  __syncthreads();
+  return ok;
+}
+
+__device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return fma(a, b, c); }
+
+// Three components of a node-padded vector (4 per node, 16/32-byte aligned),
+// read through L2 (other CTAs wrote them before the last grid barrier).
+__device__ __forceinline__ void ld3(const float* p, float& a, float& b, float& c) {
+  const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+  a = v.x;
+  b = v.y;
+  c = v.z;
+}
+__device__ __forceinline__ void ld3(const double* p, double& a, double& b, double& c) {
+  const double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  a = v.x;
+  b = v.y;
+  c = __ldcg(p + 2);
+}
+// Three components of a node of the shared-memory window (one 16-byte load
+// for FP32).
+__device__ __forceinline__ void lds3(const float* p, float& a, float& b, float& c) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  a = v.x;
+  b = v.y;
+  c = v.z;
+}
+__device__ __forceinline__ void lds3(const double* p, double& a, double& b, double& c) {
+  const double2 v = *reinterpret_cast<const double2*>(p);
+  a = v.x;
+  b = v.y;
+  c = p[2];
+}
+__device__ __forceinline__ void st3(float* p, float a, float b, float c) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, 0.f);
+}
+__device__ __forceinline__ void st3(double* p, double a, double b, double c) {
+  *reinterpret_cast<double2*>(p) = make_double2(a, b);
+  p[2] = c;
+}
+
+template <typename T, bool kWindow, bool kMixed>
+__global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[96];
+  __shared__ int s_ok;
+  __shared__ int s_next;  // next slice handed to a warp in phase 1
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int c = blockIdx.x;
+  const int s0 = a.cta_slice[c], s1 = a.cta_slice[c + 1], ns = s1 - s0;
+  const int g0 = 24 * s0;
+  const int nrows = max(0, min(24 * s1, a.n) - g0);
+  T* RR = reinterpret_cast<T*>(smem);
+  T* Z = RR + a.rows_max;
+  T* U = Z + a.rows_max;
+  T* P = U + a.rows_max;
+  T* AP = P + a.rows_max;
+  T* D = AP + a.rows_max;
+  T* win = D + a.rows_max;  // 4 per node when kWindow
+  const int wb = a.cta_win[2 * c], we = a.cta_win[2 * c + 1];
+  unsigned target = 0;
+  int slot = 0;
+  bool ok = true;
+  const double scale = kMixed ? a.O->scale : 1.0;
+
+  // ── init: r = rhs, u = 0, z = r / diag, p = 0 ──
+  T acc2[2] = {T(0), T(0)};
+  for (int lr = tid; lr < nrows; lr += kResThreads) {
+    const int g = g0 + lr;
+    const int R = g / 3, q = g - 3 * R;
+    const double d = a.dinv[g];
+    const T rv = kMixed ? static_cast<T>(a.rhs[g] * scale) : static_cast<T>(a.rhs[g]);
+    const T dv = static_cast<T>(d);
+    const T zv = rv * dv;
+    RR[lr] = rv;
+    U[lr] = T(0);
+    Z[lr] = zv;
+    P[lr] = T(0);
+    AP[lr] = T(0);
+    D[lr] = dv;
+    a.z4[4 * R + q] = zv;
+    a.p4a[4 * R + q] = T(0);
+    a.p4b[4 * R + q] = T(0);
+    acc2[0] = rfma(rv, rv, acc2[0]);
+    acc2[1] = rfma(rv, zv, acc2[1]);
+  }
+  double tot2[2];
+  ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok, tot2);
+  slot ^= 1;
+  // The scalar recurrence runs on thread 0 only (FP64 sqrt / division are long
+  // instruction sequences on GB300's FP64 pipe) and is broadcast through
+  // shared memory: s_sc = {alpha, beta}.
+  __shared__ double s_sc[2];
+  __shared__ int s_flags;
+  double norm_b = 0.0, rz = 0.0, rel = 1.0, pAp = 0.0, rr = 0.0, beta = 0.0, alpha = 0.0;
+  int flags = 0, it = 0;
+  T* p_old = a.p4a;
+  T* p_new = a.p4b;
+  if (tid == 0) {
+    norm_b = sqrt(fabs(tot2[0]));
+    rz = tot2[1];
+    rr = tot2[0];
+    if (!ok) {
+      flags = kFlagDone | kFlagAbort;
+    } else if (norm_b < 1e-300) {
+      flags = kFlagDone | kFlagZeroRhs | kFlagConverged;
+      rel = 0.0;
+    } else if (!(rz > 0.0)) {
+      flags = kFlagDone | kFlagNonPosRz;
+    }
+    s_flags = flags;
+    s_sc[1] = 0.0;
+  }
+  __syncthreads();
+  flags = s_flags;
+
+  while (!(flags & kFlagDone)) {
+    // ── phase 1: x = z + beta p over the window, Ap = K x, own p update ──
+    const T tb = static_cast<T>(beta);
+    if (tid == 0) s_next = kResWarps;
+    if (!kWindow) __syncthreads();
+    if (kWindow) {
+      // kFill nodes per thread per round: all their loads are in flight
+      // together (one L2 round trip per round instead of one per node).
+      constexpr int kFill = 4;
+      for (int j0 = wb + tid; j0 <= we; j0 += kFill * kResThreads) {
+        T z[kFill][3], q[kFill][3];
+#pragma unroll
+        for (int u = 0; u < kFill; ++u) {
+          const int j = j0 + u * kResThreads;
+          if (j <= we) {
+            ld3(a.z4 + 4 * static_cast<size_t>(j), z[u][0], z[u][1], z[u][2]);
+            ld3(p_old + 4 * static_cast<size_t>(j), q[u][0], q[u][1], q[u][2]);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kFill; ++u) {
+          const int j = j0 + u * kResThreads;
+          if (j <= we)
+            st3(win + 4 * (j - wb), rfma(tb, q[u][0], z[u][0]), rfma(tb, q[u][1], z[u][1]),
+                rfma(tb, q[u][2], z[u][2]));
+        }
+      }
+      __syncthreads();
+    }
+    T accp[1] = {T(0)};
+    // Slices are handed out dynamically (first one per warp statically), so
+    // warps that drew short slices take more and the phase ends together.
+    for (int ls = warp; ls < ns;) {
+      const int sl = s0 + ls;
+      const int base = a.slice_ptr[sl], steps = a.slice_ptr[sl + 1] - base;
+      const int* cp = a.cols + static_cast<size_t>(base) * 32 + lane;
+      const T* vp = a.vals + static_cast<size_t>(base) * 288 + lane;
+      T y0 = T(0), y1 = T(0), y2 = T(0);
+      // Up to kAhead steps of operator loads are issued before any of them is
+      // consumed, so each warp keeps ~kAhead*40 B (FP32) per lane in flight.
+      constexpr int kAhead = sizeof(T) == 4 ? 4 : 2;
+      for (int t0 = 0; t0 < steps; t0 += kAhead) {
+        int col[kAhead];
+        T v[kAhead][9];
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+          if (t0 + u < steps) {
+            col[u] = __ldcg(cp + 32 * (t0 + u));
+#pragma unroll
+            for (int k = 0; k < 9; ++k) v[u][k] = __ldcg(vp + 288 * (t0 + u) + 32 * k);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+          if (t0 + u < steps) {
+            T x0, x1, x2;
+            if (kWindow) {
+              lds3(win + 4 * (col[u] - wb), x0, x1, x2);
+            } else {
+              T z0, z1, z2, q0, q1, q2;
+              ld3(a.z4 + 4 * static_cast<size_t>(col[u]), z0, z1, z2);
+              ld3(p_old + 4 * static_cast<size_t>(col[u]), q0, q1, q2);
+              x0 = rfma(tb, q0, z0);
+              x1 = rfma(tb, q1, z1);
+              x2 = rfma(tb, q2, z2);
+            }
+            y0 = rfma(v[u][0], x0, rfma(v[u][1], x1, rfma(v[u][2], x2, y0)));
+            y1 = rfma(v[u][3], x0, rfma(v[u][4], x1, rfma(v[u][5], x2, y1)));
+            y2 = rfma(v[u][6], x0, rfma(v[u][7], x1, rfma(v[u][8], x2, y2)));
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 1; o <= 2; o <<= 1) {
+        y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+        y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+        y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+      }
+      const int r = lane >> 2, q = lane & 3;
+      const int R = 8 * sl + r;
+      if (q < 3 && R < a.nb) {
+        const int lr = 24 * ls + 3 * r + q;
+        const T yq = q == 0 ? y0 : (q == 1 ? y1 : y2);
+        const T pn = rfma(tb, P[lr], Z[lr]);
+        P[lr] = pn;
+        AP[lr] = yq;
+        p_new[4 * R + q] = pn;
+        accp[0] = rfma(pn, yq, accp[0]);
+      }
+      int nxt = 0;
+      if (lane == 0) nxt = atomicAdd(&s_next, 1);
+      ls = __shfl_sync(0xffffffffu, nxt, 0);
+    }
+    double totp[1];
+    ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok, totp);
+    slot ^= 1;
+    if (tid == 0) {
+      pAp = totp[0];
+      if (!ok) {
+        flags |= kFlagDone | kFlagAbort;
+      } else if (!(pAp > 0.0)) {
+        flags |= kFlagDone | kFlagBreakdown;
+      } else {
+        alpha = rz / pAp;
+      }
+      s_flags = flags;
+      s_sc[0] = alpha;
+    }
+    __syncthreads();
+    flags = s_flags;
+    if (flags & kFlagDone) break;
+    const T ta = static_cast<T>(s_sc[0]);
+    // ── phase 2: u, r, z updates on the own rows ──
+    acc2[0] = acc2[1] = T(0);
+    for (int lr = tid; lr < nrows; lr += kResThreads) {
+      const int g = g0 + lr;
+      const int R = g / 3, q = g - 3 * R;
+      U[lr] = rfma(ta, P[lr], U[lr]);
+      const T rv = rfma(-ta, AP[lr], RR[lr]);
+      const T zv = rv * D[lr];
+      RR[lr] = rv;
+      Z[lr] = zv;
+      a.z4[4 * R + q] = zv;
+      acc2[0] = rfma(rv, zv, acc2[0]);
+      acc2[1] = rfma(rv, rv, acc2[1]);
+    }
+    ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok, tot2);
+    slot ^= 1;
+    ++it;
+    if (tid == 0) {
+      if (!ok) {
+        flags |= kFlagDone | kFlagAbort;
+      } else {
+        rr = tot2[1];
+        rel = sqrt(fabs(rr)) / norm_b;
+        if (rel < a.tol) {
+          flags |= kFlagDone | kFlagConverged;
+          beta = 0.0;
+        } else {
+          beta = tot2[0] / rz;
+          if (it >= a.max_iters) flags |= kFlagDone | kFlagMaxIters;
+        }
+        rz = tot2[0];
+      }
+      s_flags = flags;
+      s_sc[1] = beta;
+    }
+    __syncthreads();
+    flags = s_flags;
+    if (flags & kFlagAbort) break;
+    beta = s_sc[1];
+    T* t = p_old;
+    p_old = p_new;
+    p_new = t;
+  }
+
+  // ── results ──
+  if (!(flags & kFlagAbort)) {
+    const double inv_scale = kMixed ? 1.0 / scale : 1.0;
+    for (int lr = tid; lr < nrows; lr += kResThreads) {
+      const int g = g0 + lr;
+      if (kMixed)
+        a.u_out[g] = fma(static_cast<double>(U[lr]), inv_scale, a.u_out[g]);
+      else
+        a.u_out[g] = static_cast<double>(U[lr]);
+    }
+  }
+  if (c == 0 && tid == 0) {
+    a.S->iter = it;
+    a.S->rel = rel;
+    a.S->rr = rr;
+    a.S->rz = rz;
+    a.S->pAp = pAp;
+    a.S->norm_b = norm_b;
+    a.S->beta = beta;
+    a.S->flags = flags;
+  }
+}
+
+// Padding slots point at a column inside the slice's own range (values are
+// zero), so every column read stays inside the CTA window.
+__global__ void k_fix_padding(int nb, int nslices, const int* __restrict__ slice_ptr,
+                              const int* __restrict__ rowlen, int* __restrict__ cols) {
+  const int sl = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (sl >= nslices) return;
+  const int lane = threadIdx.x & 31, r = lane >> 2, q = lane & 3;
+  const int R = 8 * sl + r;
+  const int len = R < nb ? rowlen[R] : 0;
+  for (int t = 0; t < slice_ptr[sl + 1] - slice_ptr[sl]; ++t)
+    if (4 * t + q >= len) cols[(static_cast<size_t>(slice_ptr[sl]) + t) * 32 + lane] = 8 * sl;
+}
+
+__global__ void k_slice_minmax(int nslices, const int* __restrict__ slice_ptr,
+                               const int* __restrict__ cols, int* __restrict__ mm) {
+  const int sl = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (sl >= nslices) return;
+  const int lane = threadIdx.x & 31;
+  int lo = INT_MAX, hi = -1;
+  for (int t = 0; t < slice_ptr[sl + 1] - slice_ptr[sl]; ++t) {
+    const int c = cols[(static_cast<size_t>(slice_ptr[sl]) + t) * 32 + lane];
+    lo = min(lo, c);
+    hi = max(hi, c);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (lane == 0) {
+    mm[2 * sl] = lo;
+    mm[2 * sl + 1] = hi;
+  }
+}
+
+template <typename T, bool kWindow, bool kMixed>
+void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const double* rhs,
+                     double* u, PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
+                     T* z4, T* p4a, T* p4b, const double* dinv, size_t smem, cudaStream_t s) {
+  ResArgs<T> a;
+  a.nb = B.nb;
+  a.n = 3 * B.nb;
+  a.slice_ptr = B.slice_ptr.ptr;
+  a.cols = B.cols.ptr;
+  a.vals = vals;
+  a.cta_slice = P.cta_slice.ptr;
+  a.cta_win = P.cta_win.ptr;
+  a.dinv = dinv;
+  a.rhs = rhs;
+  a.u_out = u;
+  a.z4 = z4;
+  a.p4a = p4a;
+  a.p4b = p4b;
+  a.partials = P.partials.ptr;
+  a.count = P.barrier.ptr;
+  a.abort_flag = P.abort_flag.ptr;
+  a.S = S;
+  a.O = O;
+  a.tol = tol;
+  a.max_iters = max_iters;
+  a.rows_max = 24 * P.max_slices;
+  VSGB_CUDA(cudaMemsetAsync(P.barrier.ptr, 0, sizeof(unsigned), s));
+  VSGB_CUDA(cudaMemsetAsync(P.abort_flag.ptr, 0, sizeof(int), s));
+  void* args[] = {&a};
+  VSGB_CUDA(cudaLaunchCooperativeKernel(
+      reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed>), dim3(P.ctas),
+      dim3(kResThreads), args, smem, s));
+}
+
+template <typename T, bool kWindow, bool kMixed>
+bool configure(size_t smem, int* blocks) {
+  const void* fn = reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed>);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(smem)) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, kResThreads, smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return *blocks >= 1;
+}
+
+}  // namespace
+
+void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int device, int num_sms,
+                      ResidentPlan& P, cudaStream_t s) {
+  (void)dinv;
+  P.ok32 = P.ok64 = false;
+  if (!B.valid || B.nslices < num_sms) return;
+  int coop = 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess ||
+      !coop) {
+    cudaGetLastError();
+    return;
+  }
+  int smem_optin = 0;
+  VSGB_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  const int ns = B.nslices, nb = B.nb;
+  // Steps per slice (host copy of the block-row lengths from build_bsr).
+  std::vector<long long> pre(static_cast<size_t>(ns) + 1, 0);
+  for (int sl = 0; sl < ns; ++sl) {
+    int mx = 0;
+    for (int r = 0; r < 8; ++r) {
+      const int R = 8 * sl + r;
+      if (R < nb) mx = std::max(mx, B.h_blen[R]);
+    }
+    pre[sl + 1] = pre[sl] + (mx + 3) / 4 + 1;  // +1: per-slice epilogue cost
+  }
+  const int G = num_sms;
+  std::vector<int> cs(static_cast<size_t>(G) + 1, 0);
+  for (int g = 1; g < G; ++g) {
+    const long long goal = pre[ns] * g / G;
+    cs[g] = static_cast<int>(std::lower_bound(pre.begin(), pre.end(), goal) - pre.begin());
+    cs[g] = std::max(cs[g], cs[g - 1]);
+  }
+  cs[G] = ns;
+  int max_slices = 0;
+  for (int g = 0; g < G; ++g) max_slices = std::max(max_slices, cs[g + 1] - cs[g]);
+  // Padding slots -> in-range columns; per-slice column ranges -> CTA windows.
+  const int wgrid = (ns + 7) / 8;
+  k_fix_padding<<<wgrid, 256, 0, s>>>(nb, ns, B.slice_ptr.ptr, B.rowlen.ptr, B.cols.ptr);
+  VSGB_LAUNCH_CHECK();
+  DevBuf<int> mm;
+  mm.reserve(2 * static_cast<size_t>(ns));
+  k_slice_minmax<<<wgrid, 256, 0, s>>>(ns, B.slice_ptr.ptr, B.cols.ptr, mm.ptr);
+  VSGB_LAUNCH_CHECK();
+  std::vector<int> hmm(2 * static_cast<size_t>(ns));
+  VSGB_CUDA(cudaMemcpyAsync(hmm.data(), mm.ptr, sizeof(int) * 2 * ns, cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> win(2 * static_cast<size_t>(G));
+  int max_win = 0;
+  for (int g = 0; g < G; ++g) {
+    int lo = INT_MAX, hi = -1;
+    for (int sl = cs[g]; sl < cs[g + 1]; ++sl) {
+      lo = std::min(lo, hmm[2 * sl]);
+      hi = std::max(hi, hmm[2 * sl + 1]);
+    }
+    if (hi < lo) lo = hi = 0;
+    win[2 * g] = lo;
+    win[2 * g + 1] = hi;
+    max_win = std::max(max_win, hi - lo + 1);
+  }
+  P.ctas = G;
+  P.threads = kResThreads;
+  P.max_slices = max_slices;
+  P.cta_slice.reserve(static_cast<size_t>(G) + 1);
+  P.cta_win.reserve(2 * static_cast<size_t>(G));
+  VSGB_CUDA(cudaMemcpyAsync(P.cta_slice.ptr, cs.data(), sizeof(int) * (G + 1),
+                            cudaMemcpyHostToDevice, s));
+  VSGB_CUDA(cudaMemcpyAsync(P.cta_win.ptr, win.data(), sizeof(int) * 2 * G,
+                            cudaMemcpyHostToDevice, s));
+  P.partials.reserve(2 * static_cast<size_t>(G) * 2);
+  P.barrier.reserve(1);
+  P.abort_flag.reserve(1);
+  const size_t rows = 24 * static_cast<size_t>(max_slices);
+  const size_t nodes4 = 4 * static_cast<size_t>(nb);
+  auto fit = [&](size_t bytes) { return bytes <= static_cast<size_t>(smem_optin); };
+  // FP64
+  {
+    const size_t own = 6 * rows * sizeof(double);
+    const size_t w = 4 * static_cast<size_t>(max_win) * sizeof(double);
+    int blocks = 0;
+    if (fit(own + w) && configure<double, true, false>(own + w, &blocks)) {
+      P.win64 = true;
+      P.smem64 = own + w;
+      P.ok64 = true;
+    } else if (fit(own) && configure<double, false, false>(own, &blocks)) {
+      P.win64 = false;
+      P.smem64 = own;
+      P.ok64 = true;
+    }
+    if (P.ok64) {
+      P.z4d.reserve(nodes4);
+      P.p4da.reserve(nodes4);
+      P.p4db.reserve(nodes4);
+      VSGB_CUDA(cudaMemsetAsync(P.z4d.ptr, 0, sizeof(double) * nodes4, s));
+      VSGB_CUDA(cudaMemsetAsync(P.p4da.ptr, 0, sizeof(double) * nodes4, s));
+      VSGB_CUDA(cudaMemsetAsync(P.p4db.ptr, 0, sizeof(double) * nodes4, s));
+    }
+  }
+  if (need32 && B.has32) {
+    const size_t own = 6 * rows * sizeof(float);
+    const size_t w = 4 * static_cast<size_t>(max_win) * sizeof(float);
+    int blocks = 0;
+    if (fit(own + w) && configure<float, true, true>(own + w, &blocks)) {
+      P.win32 = true;
+      P.smem32 = own + w;
+      P.ok32 = true;
+    } else if (fit(own) && configure<float, false, true>(own, &blocks)) {
+      P.win32 = false;
+      P.smem32 = own;
+      P.ok32 = true;
+    }
+    if (P.ok32) {
+      P.z4f.reserve(nodes4);
+      P.p4fa.reserve(nodes4);
+      P.p4fb.reserve(nodes4);
+      VSGB_CUDA(cudaMemsetAsync(P.z4f.ptr, 0, sizeof(float) * nodes4, s));
+      VSGB_CUDA(cudaMemsetAsync(P.p4fa.ptr, 0, sizeof(float) * nodes4, s));
+      VSGB_CUDA(cudaMemsetAsync(P.p4fb.ptr, 0, sizeof(float) * nodes4, s));
+    }
+  }
+  VSGB_CUDA(cudaStreamSynchronize(s));
+}
+
+void resident_solve32(const BsrSell& B, ResidentPlan& P, const double* r64, double* u64,
+                      PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
+                      cudaStream_t s, const double* dinv) {
+  if (P.win32)
+    launch_resident<float, true, true>(B, P, B.val32.ptr, r64, u64, S, O, tol, max_iters,
+                                       P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, P.smem32, s);
+  else
+    launch_resident<float, false, true>(B, P, B.val32.ptr, r64, u64, S, O, tol, max_iters,
+                                        P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, P.smem32, s);
+}
+
+void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double* u,
+                      PcgScalars* S, double tol, int max_iters, cudaStream_t s,
+                      const double* dinv) {
+  if (P.win64)
+    launch_resident<double, true, false>(B, P, B.val64.ptr, f, u, S, nullptr, tol, max_iters,
+                                         P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, P.smem64, s);
+  else
+    launch_resident<double, false, false>(B, P, B.val64.ptr, f, u, S, nullptr, tol, max_iters,
+                                          P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, P.smem64, s);
+}
+
+}  // namespace vsgb

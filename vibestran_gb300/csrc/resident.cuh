@@ -1,0 +1,46 @@
+// vibestran_gb300/csrc/resident.cuh — persistent (SM-resident) Jacobi PCG on the
+// 3x3 block operator: one cooperative launch runs every iteration of a solve.
+#pragma once
+
+#include <vector>
+
+#include "bsr.cuh"
+#include "common.cuh"
+
+namespace vsgb {
+
+struct ResidentPlan {
+  bool ok32 = false, ok64 = false;  // usable for FP32 inner / FP64 solves
+  bool win32 = false, win64 = false;  // x window staged in shared memory
+  int ctas = 0, threads = 0;
+  size_t smem32 = 0, smem64 = 0;
+  int max_slices = 0;               // slices of the largest CTA range
+  DevBuf<int> cta_slice;            // ctas + 1: slice range of each CTA
+  DevBuf<int> cta_win;              // 2 * ctas: [first, last] block column per CTA
+  DevBuf<double> partials;          // 2 barriers x ctas x 2 values
+  DevBuf<unsigned> barrier;         // monotonic arrival counter
+  DevBuf<int> abort_flag;           // set by a barrier that gave up waiting
+  DevBuf<float> z4f, p4fa, p4fb, dinv4f;    // node-padded FP32 vectors (4 per node)
+  DevBuf<double> z4d, p4da, p4db, dinv4d;   // node-padded FP64 vectors
+};
+
+// Plans CTA ranges / windows and allocates the padded vectors; leaves both
+// ok flags false when the device or the operator does not allow it.
+void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int device,
+                      int num_sms, ResidentPlan& P, cudaStream_t s);
+
+// One FP32 inner solve: rhs = (float)(r64 * O->scale); on convergence
+// u64 += delta / O->scale.  Final counts/flags land in *S.
+void resident_solve32(const BsrSell& B, ResidentPlan& P, const double* r64, double* u64,
+                      PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
+                      cudaStream_t s, const double* dinv);
+
+// One FP64 solve of K u = f; u written (zeros on a zero RHS).
+void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double* u,
+                      PcgScalars* S, double tol, int max_iters, cudaStream_t s,
+                      const double* dinv);
+
+// Flag set in PcgScalars::flags when a grid barrier gave up waiting.
+constexpr int kFlagResidentAbort = 64;
+
+}  // namespace vsgb
