@@ -47,6 +47,18 @@ struct WarpSmem {
 // Ke staging aliases g/wg (dead after the moment accumulation): 594 >= 576.
 static_assert(sizeof(double) * 2 * 9 * kVN * 3 >= sizeof(double) * 576, "Ke alias");
 
+// 1/sqrt(d) in FP64 from an FP32 seed and two Newton-Raphson steps
+// y <- y * (1.5 - 0.5 d y^2): quadratic convergence takes the ~2^-22 seed error
+// below FP64 rounding.  Outside the FP32 range the library square root is used.
+__device__ __forceinline__ double rsqrt_nr(double d) {
+  if (!(d > 1e-30 && d < 1e30)) return 1.0 / sqrt(d);
+  double y = static_cast<double>(rsqrtf(static_cast<float>(d)));
+  const double h = 0.5 * d;
+  y = y * fma(-h * y, y, 1.5);
+  y = y * fma(-h * y, y, 1.5);
+  return y;
+}
+
 __device__ __forceinline__ int pair_index(int A, int B) {  // A <= B < 11
   return A * kVN - (A * (A - 1)) / 2 + (B - A);
 }
@@ -232,27 +244,43 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
         const int r = t / 9, k = t - 9 * r;
         s.Kua[r][k] = kval(s, lam, mu, r / 3, r % 3, 8 + k / 3, k % 3);
       }
-      if (lane == 0) {
-        int fail = 0;
-        for (int jc = 0; jc < 9; ++jc) {
-          double d = kval(s, lam, mu, 8 + jc / 3, jc % 3, 8 + jc / 3, jc % 3);
-          for (int k = 0; k < jc; ++k) d -= s.L[jc][k] * s.L[jc][k];
+      // Right-looking Cholesky of Kaa spread over the warp: per column one lane
+      // forms the pivot, the lanes below scale the column and the trailing
+      // triangle (<= 36 entries) is updated by all lanes.  Every FP64 warp
+      // instruction occupies GB300's FP64 pipe regardless of active lanes, so
+      // the serial (one-lane) form costs ~5x more.
+      for (int t = lane; t < 45; t += 32) {
+        const int i = static_cast<int>((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f + 1e-4f);
+        const int k = t - i * (i + 1) / 2;
+        s.L[i][k] = kval(s, lam, mu, 8 + i / 3, i % 3, 8 + k / 3, k % 3);
+      }
+      __syncwarp();
+      int fail = 0;
+      for (int jc = 0; jc < 9; ++jc) {
+        if (lane == 0) {
+          double d = s.L[jc][jc];
           if (!(d > 0.0)) {
             fail = 1;
             d = 1.0;
           }
-          const double ljj = sqrt(d);
-          s.L[jc][jc] = ljj;
-          const double inv = 1.0 / ljj;
+          const double inv = rsqrt_nr(d);
+          s.L[jc][jc] = d * inv;
           s.Linv[jc] = inv;
-          for (int i = jc + 1; i < 9; ++i) {
-            double v = kval(s, lam, mu, 8 + i / 3, i % 3, 8 + jc / 3, jc % 3);
-            for (int k = 0; k < jc; ++k) v -= s.L[i][k] * s.L[jc][k];
-            s.L[i][jc] = v * inv;
-          }
         }
-        if (fail) record_element_error(err, e, 2);
+        __syncwarp();
+        const double inv = s.Linv[jc];
+        if (lane > jc && lane < 9) s.L[lane][jc] *= inv;
+        __syncwarp();
+        const int m = 8 - jc;  // trailing size
+        for (int t = lane; t < m * (m + 1) / 2; t += 32) {
+          const int ii = static_cast<int>((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f + 1e-4f);
+          const int kk = t - ii * (ii + 1) / 2;
+          const int i = jc + 1 + ii, k = jc + 1 + kk;
+          s.L[i][k] -= s.L[i][jc] * s.L[k][jc];
+        }
+        __syncwarp();
       }
+      if (lane == 0 && fail) record_element_error(err, e, 2);
       __syncwarp();
       // X[:, c] = Kaa^-1 Kau[:, c] for the 24 columns (one lane each).
       if (lane < 24) {
