@@ -56,6 +56,9 @@ extern "C" {
 #define VSGB_OPT_USE_GRAPH 7      /* 1: replay iteration batches as CUDA graphs (default 1) */
 #define VSGB_OPT_FORMAT 8         /* 0 auto, 1 scalar CSR, 2 3x3 node blocks */
 #define VSGB_OPT_RESIDENT 9       /* 1: one persistent launch per PCG solve (default 1) */
+#define VSGB_OPT_BATCHED 10       /* 1: nrhs > 1 solves all load cases in one batched PCG
+                                     on the 3x3 block operator (default 1); 0: one solve
+                                     per load case, as the reference's subcase loop */
 
 typedef struct vsgb_ctx vsgb_ctx;
 
@@ -135,8 +138,10 @@ int vsgb_assemble_chexa8(vsgb_ctx* ctx, int n_nodes, const double* node_xyz,
 int vsgb_copy_csr_lower(vsgb_ctx* ctx, int* row_ptr, int* col_ind, double* values);
 
 /* Solve with the resident K: F[n*nrhs] host -> u_out[n*nrhs] host.
- * nrhs > 1 runs the load cases as one batched PCG (one matrix sweep per
- * iteration for all right-hand sides). */
+ * nrhs > 1 on the 3x3 block operator runs the load cases as one batched PCG
+ * (16 right-hand sides per matrix sweep, each with its own recurrence and
+ * stopping test); the scalar-CSR operator, or VSGB_OPT_BATCHED = 0, solves
+ * them one after another. */
 int vsgb_solve_assembled(vsgb_ctx* ctx, const double* F, int nrhs, double* u_out,
                          vsgb_stats* stats);
 
@@ -173,6 +178,14 @@ int vsgb_timer_stop(vsgb_ctx* ctx, double* ms);
 int vsgb_time_spmv(vsgb_ctx* ctx, int precision, int reps, double* avg_ms, double* bytes);
 /* Number of kernels this context launched since creation. */
 long long vsgb_kernel_launches(vsgb_ctx* ctx);
+
+/* Per-load-case outcome of the last solve (k < nrhs): PCG iterations
+ * (mixed: summed over inner solves), relative residual, converged flag and
+ * whether the load cases ran as one batched PCG.  The reference reports one
+ * subcase per solve() call (SolverBackend::last_iteration_count /
+ * last_estimated_error, include/solver/solver_backend.hpp:39-43). */
+int vsgb_rhs_stats(vsgb_ctx* ctx, int k, int* iterations, double* rel_residual, int* converged,
+                   int* batched);
 
 /* ── allocation-free solve ──────────────────────────────────────────────── */
 

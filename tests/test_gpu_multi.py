@@ -1,0 +1,117 @@
+"""Batched PCG: several load cases share each sweep of the 3x3 block operator.
+
+Every load case must give what its own solve gives (the reference's subcase
+loop, linear_static.cpp:212-275): FP64 to 1e-8 of the sparse-direct answer,
+mixed to 1e-6, iteration counts within a couple of the one-at-a-time solve,
+zero load cases returning u = 0 after 0 iterations, and the batched solve
+bitwise reproducible.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N_CASES = 20  # one batch of 16 and one of 4
+
+
+@pytest.fixture(scope="module")
+def multi_model(vsgb, oracle):
+    from vibestran_gb300 import cantilever as C
+    m = C.small_block(16, 6, 6, 0.05, seed=31, jitter=0.1, hetero=True)
+    m.loads = C.face_random_loads(m, N_CASES, np.random.default_rng(7))
+    eq6, n = vsgb.build_dof_map(m)
+    F = np.stack([vsgb.apply_forces(m, eq6, n, k) for k in range(N_CASES)], axis=1)
+    eq_o, n_o = oracle.dof_map(m)
+    K = oracle.assemble_chexa8(m, eq_o, n_o)
+    U = oracle.sparse_direct_solve(K, F)
+    return m, eq6, n, F, U
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def _assembled(vsgb, m, eq6, n, mixed, tol, batched, inner=0.0):
+    cls = vsgb.Gb300MixedPcgSolverBackend if mixed else vsgb.Gb300PcgSolverBackend
+    be = cls.try_create(tol, 20000)
+    be.set_option(vsgb.OPT_BATCHED, 1 if batched else 0)
+    if inner:
+        be.set_option(vsgb.OPT_INNER_TOL, inner)
+        be.set_option(vsgb.OPT_MAX_SOLVES, 6)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    return be, asm
+
+
+def test_batched_fp64_matches_sequential_and_direct(vsgb, multi_model):
+    m, eq6, n, F, U = multi_model
+    be, asm = _assembled(vsgb, m, eq6, n, False, 1e-10, True)
+    Ub = asm.solve(F)
+    assert be.last_stats.format == 2
+    stats_b = [be.rhs_stats(k) for k in range(N_CASES)]
+    assert all(s["batched"] and s["converged"] for s in stats_b)
+    be.set_option(vsgb.OPT_BATCHED, 0)
+    Us = asm.solve(F)
+    stats_s = [be.rhs_stats(k) for k in range(N_CASES)]
+    assert not any(s["batched"] for s in stats_s)
+    for k in range(N_CASES):
+        assert _rel(Ub[:, k], U[:, k]) <= 1e-8, k
+        assert _rel(Us[:, k], U[:, k]) <= 1e-8, k
+        assert abs(stats_b[k]["iterations"] - stats_s[k]["iterations"]) <= 2, k
+        assert stats_b[k]["rel_residual"] < 1e-10
+    # batched solve is bitwise reproducible
+    be.set_option(vsgb.OPT_BATCHED, 1)
+    assert np.array_equal(asm.solve(F), Ub)
+    be.close()
+
+
+def test_batched_mixed(vsgb, multi_model):
+    m, eq6, n, F, U = multi_model
+    be, asm = _assembled(vsgb, m, eq6, n, True, 1e-8, True, inner=1e-3)
+    Ub = asm.solve(F)
+    for k in range(N_CASES):
+        s = be.rhs_stats(k)
+        assert s["batched"] and s["converged"] and s["rel_residual"] <= 1e-8, (k, s)
+        assert _rel(Ub[:, k], U[:, k]) <= 1e-6, k
+    assert be.last_stats.inner_solves >= 2 * N_CASES
+    be.close()
+
+
+def test_batched_zero_and_ragged_cases(vsgb, multi_model):
+    m, eq6, n, F, U = multi_model
+    G = F[:, :3].copy()
+    G[:, 1] = 0.0
+    for mixed in (False, True):
+        be, asm = _assembled(vsgb, m, eq6, n, mixed, 1e-10 if not mixed else 1e-8, True,
+                             inner=1e-3 if mixed else 0.0)
+        Ub = asm.solve(G)
+        s1 = be.rhs_stats(1)
+        assert s1["batched"] and s1["iterations"] == 0 and s1["converged"]
+        assert np.abs(Ub[:, 1]).max() == 0.0
+        tol = 1e-6 if mixed else 1e-8
+        assert _rel(Ub[:, 0], U[:, 0]) <= tol and _rel(Ub[:, 2], U[:, 2]) <= tol
+        be.close()
+
+
+def test_batched_csr_entry_point(vsgb, oracle, multi_model):
+    """SolverBackend::solve with a host CSR and several load cases."""
+    m, eq6, n, F, U = multi_model
+    eq_o, n_o = oracle.dof_map(m)
+    Ko = oracle.assemble_chexa8(m, eq_o, n_o)
+    K = vsgb.CsrData(Ko.row_ptr, Ko.col_ind, Ko.values, Ko.n, Ko.nnz, Ko.lower)
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-10, 20000)
+    Ub = be.solve(K, F[:, :16])
+    assert be.rhs_stats(0)["batched"]
+    for k in range(16):
+        assert _rel(Ub[:, k], U[:, k]) <= 1e-8, k
+    be.close()
+
+
+def test_batched_not_converged_raises(vsgb, multi_model):
+    m, eq6, n, F, U = multi_model
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-12, 5)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    with pytest.raises(vsgb.SolverError, match="did not converge after 5 iterations"):
+        asm.solve(F[:, :4])
+    be.close()

@@ -53,9 +53,11 @@ OPT_CHECK_EVERY = 6
 OPT_USE_GRAPH = 7
 OPT_FORMAT = 8
 OPT_RESIDENT = 9
+OPT_BATCHED = 10
 
 # The symbols include/vsgb.h declares (checked by tests against the .so).
 EXPORTS = (
+    "vsgb_rhs_stats",
     "vsgb_create", "vsgb_destroy", "vsgb_set_option", "vsgb_last_error", "vsgb_device_name",
     "vsgb_backend_name", "vsgb_solve_csr", "vsgb_build_dof_map", "vsgb_apply_forces",
     "vsgb_assemble_chexa8", "vsgb_copy_csr_lower", "vsgb_solve_assembled", "vsgb_mesh_upload",
@@ -132,6 +134,8 @@ def load_library(build_if_missing: bool = False):
     L.vsgb_time_spmv.argtypes = [vp, c_int, c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)]
     L.vsgb_kernel_launches.argtypes = [vp]
     L.vsgb_kernel_launches.restype = c_ll
+    L.vsgb_rhs_stats.argtypes = [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_dbl),
+                                 ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.vsgb_pcg_solve_noalloc.argtypes = [c_int, c_int, vp, vp, vp, vp, vp, c_dbl, c_int, vp,
                                          ctypes.POINTER(c_int), ctypes.POINTER(c_dbl), cp, sz]
     _lib = L
@@ -256,6 +260,17 @@ class Gb300PcgSolverBackend:
 
     def kernel_launches(self) -> int:
         return int(load_library().vsgb_kernel_launches(self._ctx.ptr))
+
+    def rhs_stats(self, k: int) -> dict:
+        """Outcome of load case k in the last solve (iterations, relative
+        residual, converged, whether the cases ran as one batched PCG)."""
+        it, conv, bat = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        rel = ctypes.c_double(0.0)
+        self._ctx.check(load_library().vsgb_rhs_stats(
+            self._ctx.ptr, k, ctypes.byref(it), ctypes.byref(rel), ctypes.byref(conv),
+            ctypes.byref(bat)))
+        return {"iterations": it.value, "rel_residual": rel.value,
+                "converged": bool(conv.value), "batched": bool(bat.value)}
 
     @property
     def context(self) -> _Context:

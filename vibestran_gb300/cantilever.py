@@ -158,9 +158,10 @@ def cantilever_84k_jitter(seed: int = 20260301) -> SolidModel:
     return m
 
 
-def block_160k_16rhs(seed: int = 20260304, nrhs: int = 16) -> SolidModel:
-    rng = np.random.default_rng(seed)
-    m = block(100, 40, 40, 0.01, name="block_160k_16rhs")
+def face_random_loads(m: SolidModel, nrhs: int, rng: np.random.Generator,
+                      sigma: float = 100.0) -> list:
+    """nrhs load cases of i.i.d. N(0, sigma) x/y/z FORCEs on the free z-max
+    face nodes (the clamped i = 0 column excluded)."""
     nx, ny, nz = m.shape
     ids0 = m.node_ids - 1
     k = ids0 % (nz + 1)
@@ -168,9 +169,15 @@ def block_160k_16rhs(seed: int = 20260304, nrhs: int = 16) -> SolidModel:
     face = m.node_ids[(k == nz) & (i > 0)].astype(np.int32)
     loads = []
     for _ in range(nrhs):
-        f = rng.normal(0.0, 100.0, size=(face.shape[0], 3))
+        f = rng.normal(0.0, sigma, size=(face.shape[0], 3))
         loads.append((face, np.ones(face.shape[0]), f))
-    m.loads = loads
+    return loads
+
+
+def block_160k_16rhs(seed: int = 20260304, nrhs: int = 16) -> SolidModel:
+    rng = np.random.default_rng(seed)
+    m = block(100, 40, 40, 0.01, name="block_160k_16rhs")
+    m.loads = face_random_loads(m, nrhs, rng)
     m.seed = seed
     return m
 

@@ -53,6 +53,9 @@ struct vsgb_ctx {
   long long launches = 0;
   int last_iters = 0;
   double last_rel = 0.0;
+  bool batched = true;                 // several load cases share each matrix sweep
+  bool last_batched = false;
+  std::vector<vsgb::SolveResult> rhs;  // per-load-case results of the last solve
 };
 
 namespace {
@@ -124,7 +127,57 @@ void reset_assembly_error(vsgb_ctx* c) {
   c->scr.flag.reserve(1);
 }
 
+std::string not_converged_text(const vsgb_ctx* c, double rel) {
+  // cuda_pcg_backend_impl.hpp:1964-1970
+  return "CUDA PCG: did not converge after " + std::to_string(c->max_iters) +
+         " iterations (relative residual " + std::to_string(rel) + " > tolerance " +
+         std::to_string(c->tol) + "). Consider increasing max iterations or using a direct solver.";
+}
+
+// nrhs > 1 on the block operator: one batched PCG for all load cases.
+void run_batched(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
+  const int n = c->K.n;
+  c->u.reserve(static_cast<size_t>(n) * nrhs);
+  const bool mixed = c->precision == VSGB_MIXED;
+  VSGB_CUDA(cudaEventRecord(c->ev[0], c->stream));
+  c->eng->solve_multi(c->f.ptr, nrhs, c->u.ptr, mixed, c->tol, inner_tolerance(c), c->max_iters,
+                      c->max_solves, c->stream, c->rhs);
+  VSGB_CUDA(cudaEventRecord(c->ev[1], c->stream));
+  VSGB_CUDA(cudaEventSynchronize(c->ev[1]));
+  float ms = 0.f;
+  VSGB_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+  c->last_batched = true;
+  vsgb_stats st{};
+  st.format = c->eng->format_used();
+  st.converged = 1;
+  for (const vsgb::SolveResult& r : c->rhs) {
+    st.iterations = r.iterations > st.iterations ? r.iterations : st.iterations;
+    st.inner_solves += r.inner_solves;
+    st.rel_residual = r.rel > st.rel_residual ? r.rel : st.rel_residual;
+    if (!r.converged) st.converged = 0;
+  }
+  c->last_iters = st.iterations;
+  c->last_rel = st.rel_residual;
+  for (const vsgb::SolveResult& r : c->rhs) {
+    // Same outcomes as one solve per load case: FP64 throws on a case that
+    // did not converge, mixed throws only when an inner solve failed.
+    if (mixed ? r.inner_failed : !r.converged)
+      throw Error(VSGB_ERR_NOT_CONVERGED, not_converged_text(c, r.rel));
+  }
+  if (stats) {
+    st.solve_ms = ms;
+    st.spmv_bytes = c->eng->spmv_bytes(c->precision);
+    *stats = st;
+  }
+}
+
 void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
+  if (nrhs > 1 && c->batched && c->eng->multi_supported()) {
+    run_batched(c, nrhs, stats);
+    return;
+  }
+  c->last_batched = false;
+  c->rhs.assign(static_cast<size_t>(nrhs), vsgb::SolveResult{});
   const int n = c->K.n;
   c->u.reserve(static_cast<size_t>(n) * nrhs);
   vsgb_stats st{};
@@ -154,6 +207,7 @@ void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
     st.rel_residual = res.rel > st.rel_residual ? res.rel : st.rel_residual;
     c->last_iters = res.iterations;
     c->last_rel = res.rel;
+    c->rhs[static_cast<size_t>(k)] = res;
     const std::string tail = " (relative residual " + std::to_string(res.rel) + " > tolerance " +
                              std::to_string(c->tol) +
                              "). Consider increasing max iterations or using a direct solver.";
@@ -267,6 +321,9 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
       case VSGB_OPT_RESIDENT:
         c->eng->set_resident(value != 0.0);
         if (c->assembled) c->eng->prepare(c->K, c->precision == VSGB_MIXED, c->stream);
+        break;
+      case VSGB_OPT_BATCHED:
+        c->batched = value != 0.0;
         break;
       default:
         throw Error(VSGB_ERR_INVALID, "unknown option " + std::to_string(option));
@@ -523,5 +580,19 @@ int vsgb_time_spmv(vsgb_ctx* c, int precision, int reps, double* avg_ms, double*
 }
 
 long long vsgb_kernel_launches(vsgb_ctx* c) { return c ? c->eng->launches() : -1; }
+
+int vsgb_rhs_stats(vsgb_ctx* c, int k, int* iterations, double* rel_residual, int* converged,
+                   int* batched) {
+  return guarded(c, [&] {
+    if (k < 0 || static_cast<size_t>(k) >= c->rhs.size())
+      throw Error(VSGB_ERR_INVALID, "vsgb_rhs_stats: load case " + std::to_string(k) +
+                                        " not in the last solve");
+    const vsgb::SolveResult& r = c->rhs[static_cast<size_t>(k)];
+    if (iterations) *iterations = r.iterations;
+    if (rel_residual) *rel_residual = r.rel;
+    if (converged) *converged = r.converged ? 1 : 0;
+    if (batched) *batched = c->last_batched ? 1 : 0;
+  });
+}
 
 }  // extern "C"

@@ -1,0 +1,890 @@
+// vibestran_gb300/csrc/multi.cu — batched Jacobi-PCG over up to 16 load cases.
+//
+// The reference solves subcases one after another, each with its own
+// cuda-pcg call (linear_static.cpp:212-275; cuda_pcg_backend_impl.hpp:1688-1999).
+// Here the right-hand sides of one model share each sweep of the matrix:
+// vectors are stored as panels [n][16] (the 16 load cases of a DOF are
+// contiguous), so one 3x3 block of K meets 3 x 16 values of the panel and the
+// SpMM does 144 FMAs per 9 matrix values — the matrix stream, which bounds a
+// single-RHS iteration, is amortised 16 ways.  Each column keeps its own PCG
+// scalars (alpha, beta, rz, stopping test on the unpreconditioned residual
+// sqrt(r.r)/||b|| < tol), so every column follows the reference recurrence;
+// a finished column gets alpha = 0 and no longer moves.  Mixed precision runs
+// FP32 inner solves of the scaled residual and refines each column in FP64
+// on the GPU (cuda_pcg_backend_impl.hpp:2134-2262 refines on the host).
+//
+// Rooflines (config of 504 300 equations, 4.36 M stored 3x3 blocks):
+//   FP32 SpMM  — matrix 4.36M x (36 + 4) B streamed once, the panel gathered
+//                through L1/L2: HBM-bound, ~1.26 GFLOP at ~2.7 flop/B.
+//   FP64 SpMM  — 628 M DFMA per sweep: FP64-pipe bound on GB300.
+//   vector kernels — HBM streams of 16-wide panels.
+// All reductions are fixed-order (per-lane -> warp -> block -> block-ordered
+// grid sum), so a batched solve is bitwise reproducible.
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pcg.cuh"
+
+namespace vsgb {
+
+namespace {
+
+constexpr int kP = 16;     // panel width (load cases per batch)
+constexpr int kMT = 256;   // threads per block of the SpMM / transpose kernels
+constexpr int kVT = 1024;  // threads per block of the panel vector kernels (one block per SM)
+constexpr int kFlagStalled = 128;   // refinement stopped improving (outer record)
+constexpr int kFlagInactive = 256;  // column not part of this solve
+
+struct MultiState {
+  int done;       // every column finished
+  int iter;       // iterations run in this solve
+  int max_iters;
+  int ncols;
+  double tol;
+  double rz[kP], pAp[kP], alpha[kP], beta[kP], rr[kP], rel[kP], norm_b[kP];
+  int flags[kP];
+  int iters[kP];  // iteration count at which the column finished
+};
+
+struct MultiOuter {
+  double norm_f[kP], rel[kP], prev[kP], scale[kP];
+  int flags[kP];
+  int active[kP];  // column takes part in the current inner solve
+  int done;
+  int pad;
+};
+
+struct MView {
+  int nb, nslices;
+  const int* __restrict__ slice_ptr;
+  const int* __restrict__ cols;
+};
+
+// Fixed-order grid reduction of per-column sums.  acc[Q][R] holds this
+// thread's sums of quantity q for columns cb..cb+R-1, where cb is the same
+// for every lane with the same (lane & 3) in a warp.  Returns true in the
+// block that finished last, with the Q x 16 totals in s_tot[q * 16 + k].
+// BT is the block size; s_red holds BT doubles.
+template <int Q, int R, int BT>
+__device__ __forceinline__ bool mcol_sum_last(double (&acc)[Q][R], int cb, double* partials,
+                                              unsigned* counter, double* s_red /* BT */,
+                                              double* s_tot /* Q * kP */) {
+  constexpr int QM = Q * kP;
+  constexpr int NW = BT / 32;
+  static_assert(QM <= BT && NW * QM <= BT, "reduction shape");
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < Q; ++q)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      double v = acc[q][r];
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 8);
+      v += __shfl_xor_sync(0xffffffffu, v, 16);
+      acc[q][r] = v;
+    }
+  for (int t = threadIdx.x; t < NW * QM; t += BT) s_red[t] = 0.0;
+  __syncthreads();
+  if (lane < 4)
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+      for (int r = 0; r < R; ++r) s_red[(wid * Q + q) * kP + cb + r] = acc[q][r];
+  __syncthreads();
+  const int nblk = gridDim.x * gridDim.y;
+  const int b = blockIdx.y * gridDim.x + blockIdx.x;
+  // partials are column-major (column t at partials + t * nblk) so that the
+  // last block reads each column with coalesced loads
+  if (threadIdx.x < QM) {
+    double s = 0.0;
+    for (int w = 0; w < NW; ++w) s += s_red[w * QM + threadIdx.x];
+    partials[static_cast<size_t>(threadIdx.x) * nblk + b] = s;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == static_cast<unsigned>(nblk - 1));
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  // one warp per column: lane l takes blocks l, l+32, ...; each round issues
+  // 8 independent loads before adding them in block order, then a butterfly
+  for (int col = wid; col < QM; col += NW) {
+    const double* pc = partials + static_cast<size_t>(col) * nblk;
+    double s = 0.0;
+    for (int b0 = lane; b0 < nblk; b0 += 256) {
+      double v[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) v[m] = (b0 + 32 * m < nblk) ? __ldcg(pc + b0 + 32 * m) : 0.0;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) s += v[m];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) s_tot[col] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+__device__ __forceinline__ void all_done(MultiState* S) {
+  int all = 1;
+  for (int k = 0; k < kP; ++k) all &= (S->flags[k] & kFlagDone) ? 1 : 0;
+  S->done = all;
+}
+
+// ── panel <-> column-major transposes (32 DOFs per block) ─────────────────
+
+__global__ void __launch_bounds__(kMT)
+k_pack(int n, int ncols, const double* __restrict__ F, double* __restrict__ panel) {
+  __shared__ double tile[kP][33];
+  const int i0 = blockIdx.x * 32;
+  for (int t = threadIdx.x; t < kP * 32; t += kMT) {
+    const int k = t >> 5, i = t & 31;
+    tile[k][i] = (k < ncols && i0 + i < n) ? F[static_cast<size_t>(k) * n + i0 + i] : 0.0;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kP * 32; t += kMT) {
+    const int i = t >> 4, k = t & 15;
+    if (i0 + i < n) panel[static_cast<size_t>(i0 + i) * kP + k] = tile[k][i];
+  }
+}
+
+__global__ void __launch_bounds__(kMT)
+k_unpack(int n, int ncols, const double* __restrict__ panel, double* __restrict__ U) {
+  __shared__ double tile[kP][33];
+  const int i0 = blockIdx.x * 32;
+  for (int t = threadIdx.x; t < kP * 32; t += kMT) {
+    const int i = t >> 4, k = t & 15;
+    tile[k][i] = (i0 + i < n) ? panel[static_cast<size_t>(i0 + i) * kP + k] : 0.0;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kP * 32; t += kMT) {
+    const int k = t >> 5, i = t & 31;
+    if (k < ncols && i0 + i < n) U[static_cast<size_t>(k) * n + i0 + i] = tile[k][i];
+  }
+}
+
+// ── 4-wide panel chunk access ─────────────────────────────────────────────
+
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0];
+  const double2 b = reinterpret_cast<const double2*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double (&v)[4]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+
+// RN consecutive panel values (RN = 2 or 4, 8/16-byte aligned).
+template <int RN, typename T>
+__device__ __forceinline__ void ldn(const T* p, T (&v)[RN]) {
+  if constexpr (RN == 4) {
+    ld4(p, v);
+  } else if constexpr (sizeof(T) == 8) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    v[0] = a.x; v[1] = a.y;
+  } else {
+    const float2 a = *reinterpret_cast<const float2*>(p);
+    v[0] = a.x; v[1] = a.y;
+  }
+}
+template <int RN, typename T>
+__device__ __forceinline__ void stn(T* p, const T (&v)[RN]) {
+  if constexpr (RN == 4) {
+    st4(p, v);
+  } else if constexpr (sizeof(T) == 8) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+  } else {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  }
+}
+
+// ── SpMM on the 3x3 sliced-ELL operator ───────────────────────────────────
+// One warp per slice of 8 block rows; the 4 lanes of block row r = lane/4
+// share every block of that row, and lane q = lane%4 owns columns
+// g0 + q*G/4 .. +G/4-1 of the 3 output rows.  Per step the warp loads the
+// step's 32 blocks coalesced (lane = slot, L1-bypassing), then in 4 sub-steps
+// broadcasts block u of each row over its quad and every lane gathers its
+// G/4 panel columns of the block column: the quad reads one contiguous
+// 64-byte run per block row of x, so a gather touches 8 cache lines for 8
+// blocks instead of one line per 16 bytes.  Sums run in slot order, so the
+// result is reproducible.  The next step's blocks are loaded before the
+// current step is consumed.
+template <typename T, int G>
+__device__ __forceinline__ void mspmm_slice(const MView& B, const T* __restrict__ vals,
+                                            const T* __restrict__ x, int sl, int lane, int g0,
+                                            T (&out)[3][G / 4]) {
+  constexpr int RN = G / 4;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int r = 0; r < RN; ++r) out[i][r] = T(0);
+  const int base = B.slice_ptr[sl], steps = B.slice_ptr[sl + 1] - base;
+  const int* cp = B.cols + static_cast<size_t>(base) * 32 + lane;
+  const T* vp = vals + static_cast<size_t>(base) * 288 + lane;
+  const T* xq = x + g0 + RN * (lane & 3);
+  const int quad = lane & ~3;
+  int cn = 0;
+  T an[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) an[k] = T(0);
+  if (steps > 0) {
+    cn = __ldcg(cp);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) an[k] = __ldcg(vp + 32 * k);
+  }
+  for (int t = 0; t < steps; ++t) {
+    const int cown = cn;
+    T aown[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) aown[k] = an[k];
+    if (t + 1 < steps) {
+      cn = __ldcg(cp + 32 * (t + 1));
+#pragma unroll
+      for (int k = 0; k < 9; ++k) an[k] = __ldcg(vp + 288 * (t + 1) + 32 * k);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int src = quad | u;
+      const int c = __shfl_sync(0xffffffffu, cown, src);
+      T a[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a[k] = __shfl_sync(0xffffffffu, aown[k], src);
+      const T* xc = xq + static_cast<size_t>(c) * (3 * kP);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        T xv[RN];
+        ldn<RN>(xc + j * kP, xv);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int r = 0; r < RN; ++r) out[i][r] = fmaT(a[3 * i + j], xv[r], out[i][r]);
+      }
+    }
+  }
+}
+
+// Ap = K p for the columns of block row group blockIdx.y; p.Ap per column,
+// then alpha = rz / p.Ap (breakdown when p.Ap <= 0, as cuda_pcg_backend_impl.hpp:688-694).
+template <typename T, int G>
+__global__ void __launch_bounds__(kMT)
+k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restrict__ Ap,
+        MultiState* S, double* partials, unsigned* counter) {
+  if (S->done) return;
+  __shared__ double s_red[kMT];
+  __shared__ double s_tot[kP];
+  constexpr int RN = G / 4;
+  const int lane = threadIdx.x & 31;
+  const int g0 = blockIdx.y * G, cb = g0 + (lane & 3) * RN;
+  constexpr int wpb = kMT / 32;
+  T pap[RN];
+#pragma unroll
+  for (int r = 0; r < RN; ++r) pap[r] = T(0);
+  for (int sl = blockIdx.x * wpb + (threadIdx.x >> 5); sl < B.nslices; sl += gridDim.x * wpb) {
+    T out[3][RN];
+    mspmm_slice<T, G>(B, vals, p, sl, lane, g0, out);
+    const int R = sl * 8 + (lane >> 2);
+    if (R < B.nb) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const size_t o = static_cast<size_t>(3 * R + i) * kP + cb;
+        T pv[RN];
+        ldn<RN>(p + o, pv);
+        stn<RN>(Ap + o, out[i]);
+#pragma unroll
+        for (int r = 0; r < RN; ++r) pap[r] = fmaT(pv[r], out[i][r], pap[r]);
+      }
+    }
+  }
+  double a[1][RN];
+#pragma unroll
+  for (int r = 0; r < RN; ++r) a[0][r] = static_cast<double>(pap[r]);
+  if (mcol_sum_last<1, RN, kMT>(a, cb, partials, counter, s_red, s_tot)) {
+    if (threadIdx.x < kP) {
+      const int k = threadIdx.x;
+      int f = S->flags[k];
+      if (!(f & kFlagDone)) {
+        const double pAp = s_tot[k];
+        S->pAp[k] = pAp;
+        if (!(pAp > 0.0)) {
+          S->alpha[k] = 0.0;
+          f |= kFlagDone | kFlagBreakdown;
+          S->iters[k] = S->iter;
+        } else {
+          S->alpha[k] = S->rz[k] / pAp;
+        }
+        S->flags[k] = f;
+      } else {
+        S->alpha[k] = 0.0;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) all_done(S);
+  }
+}
+
+// r = f - K u (FP64) and ||r|| per column; updates the refinement record:
+// convergence (rel <= tol), stagnation (rel >= 0.9 * previous) and the scale
+// 1/||r|| of the next inner right-hand side.
+template <int G>
+__global__ void __launch_bounds__(kMT)
+k_mresidual(MView B, const double* __restrict__ vals, const double* __restrict__ u,
+            const double* __restrict__ f, double* __restrict__ r, MultiOuter* O, double tol,
+            double* partials, unsigned* counter) {
+  __shared__ double s_red[kMT];
+  __shared__ double s_tot[kP];
+  constexpr int RN = G / 4;
+  const int lane = threadIdx.x & 31;
+  const int g0 = blockIdx.y * G, cb = g0 + (lane & 3) * RN;
+  constexpr int wpb = kMT / 32;
+  double a[1][RN];
+#pragma unroll
+  for (int q = 0; q < RN; ++q) a[0][q] = 0.0;
+  for (int sl = blockIdx.x * wpb + (threadIdx.x >> 5); sl < B.nslices; sl += gridDim.x * wpb) {
+    double out[3][RN];
+    mspmm_slice<double, G>(B, vals, u, sl, lane, g0, out);
+    const int R = sl * 8 + (lane >> 2);
+    if (R < B.nb) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const size_t o = static_cast<size_t>(3 * R + i) * kP + cb;
+        double fv[RN], rv[RN];
+        ldn<RN>(f + o, fv);
+#pragma unroll
+        for (int q = 0; q < RN; ++q) {
+          rv[q] = fv[q] - out[i][q];
+          a[0][q] = fma(rv[q], rv[q], a[0][q]);
+        }
+        stn<RN>(r + o, rv);
+      }
+    }
+  }
+  if (mcol_sum_last<1, RN, kMT>(a, cb, partials, counter, s_red, s_tot)) {
+    if (threadIdx.x < kP) {
+      const int k = threadIdx.x;
+      if (O->active[k]) {
+        const double rn = sqrt(fabs(s_tot[k]));
+        const double rel = O->norm_f[k] > 1e-300 ? rn / O->norm_f[k] : rn;
+        int fl = O->flags[k];
+        O->rel[k] = rel;
+        O->scale[k] = rn > 0.0 ? 1.0 / rn : 1.0;
+        if (rel <= tol)
+          fl |= kFlagDone | kFlagConverged;
+        else if (O->prev[k] > 0.0 && rel >= O->prev[k] * 0.9)
+          fl |= kFlagDone | kFlagStalled;
+        O->prev[k] = rel;
+        O->flags[k] = fl;
+        O->active[k] = (fl & kFlagDone) ? 0 : 1;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int all = 1;
+      for (int k = 0; k < kP; ++k) all &= (O->flags[k] & kFlagDone) ? 1 : 0;
+      O->done = all;
+    }
+  }
+}
+
+// ── panel vector kernels: thread = one DOF x 4 columns (cb = 4*(lane&3)) ─
+
+// r = f, u = 0 (FP64 panels) and ||f|| per column for the refinement record.
+__global__ void __launch_bounds__(kVT, 1)
+k_mouter_init(int n, int ncols, const double* __restrict__ f, double* __restrict__ r,
+              double* __restrict__ u, MultiOuter* O, double* partials, unsigned* counter) {
+  __shared__ double s_red[kVT];
+  __shared__ double s_tot[kP];
+  const int cb = 4 * (threadIdx.x & 3);
+  double a[1][4] = {{0.0, 0.0, 0.0, 0.0}};
+  const double zero[4] = {0.0, 0.0, 0.0, 0.0};
+  const long long nc = static_cast<long long>(n) * 4;
+  for (long long c = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x; c < nc;
+       c += static_cast<long long>(gridDim.x) * kVT) {
+    const size_t o = static_cast<size_t>(c >> 2) * kP + cb;
+    double fv[4];
+    ld4(f + o, fv);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) a[0][j] = fma(fv[j], fv[j], a[0][j]);
+    st4(r + o, fv);
+    st4(u + o, zero);
+  }
+  if (mcol_sum_last<1, 4, kVT>(a, cb, partials, counter, s_red, s_tot)) {
+    if (threadIdx.x < kP) {
+      const int k = threadIdx.x;
+      const double nb = sqrt(fabs(s_tot[k]));
+      int fl = 0;
+      if (k >= ncols)
+        fl = kFlagDone | kFlagInactive;
+      else if (nb < 1e-300)  // zero load case: u = 0 (cuda_pcg_backend_impl.hpp:1820-1830)
+        fl = kFlagDone | kFlagZeroRhs | kFlagConverged;
+      O->norm_f[k] = nb;
+      O->rel[k] = (fl & kFlagDone) ? 0.0 : 1.0;
+      O->prev[k] = 0.0;
+      O->scale[k] = nb > 1e-300 ? 1.0 / nb : 1.0;
+      O->flags[k] = fl;
+      O->active[k] = (fl & kFlagDone) ? 0 : 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int all = 1;
+      for (int k = 0; k < kP; ++k) all &= (O->flags[k] & kFlagDone) ? 1 : 0;
+      O->done = all;
+    }
+  }
+}
+
+// PCG start: r = src * scale (src = f, or the FP64 residual of the
+// refinement), u = 0, z = D^-1 r, p = z; r.z and r.r per column.
+template <typename T>
+__global__ void __launch_bounds__(kVT, 1)
+k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
+        const T* __restrict__ dinv, T* __restrict__ r, T* __restrict__ u, T* __restrict__ p,
+        MultiState* S, double tol, int max_iters, double* partials, unsigned* counter) {
+  __shared__ double s_red[kVT];
+  __shared__ double s_tot[2 * kP];
+  const int cb = 4 * (threadIdx.x & 3);
+  double sc[4];
+  bool act[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    act[j] = O ? (O->active[cb + j] != 0) : (cb + j < ncols);
+    sc[j] = O ? O->scale[cb + j] : 1.0;
+  }
+  T rz[4] = {T(0), T(0), T(0), T(0)}, rr[4] = {T(0), T(0), T(0), T(0)};
+  const T zero[4] = {T(0), T(0), T(0), T(0)};
+  const long long nc = static_cast<long long>(n) * 4;
+  for (long long c = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x; c < nc;
+       c += static_cast<long long>(gridDim.x) * kVT) {
+    const long long i = c >> 2;
+    const size_t o = static_cast<size_t>(i) * kP + cb;
+    double sv[4];
+    ld4(src + o, sv);
+    const T d = dinv[i];
+    T rv[4], zv[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      rv[j] = act[j] ? static_cast<T>(sv[j] * sc[j]) : T(0);
+      zv[j] = rv[j] * d;
+      rz[j] = fmaT(rv[j], zv[j], rz[j]);
+      rr[j] = fmaT(rv[j], rv[j], rr[j]);
+    }
+    st4(r + o, rv);
+    st4(u + o, zero);
+    st4(p + o, zv);
+  }
+  double a[2][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    a[0][j] = static_cast<double>(rz[j]);
+    a[1][j] = static_cast<double>(rr[j]);
+  }
+  if (mcol_sum_last<2, 4, kVT>(a, cb, partials, counter, s_red, s_tot)) {
+    if (threadIdx.x < kP) {
+      const int k = threadIdx.x;
+      const double rzk = s_tot[k], rrk = s_tot[kP + k], nb = sqrt(fabs(rrk));
+      const bool active = O ? (O->active[k] != 0) : (k < ncols);
+      int fl = 0;
+      if (!active)
+        fl = kFlagDone | kFlagInactive;
+      else if (nb < 1e-300)
+        fl = kFlagDone | kFlagZeroRhs | kFlagConverged;
+      else if (!(rzk > 0.0))  // cuda_pcg_backend_impl.hpp:1859-1862
+        fl = kFlagDone | kFlagNonPosRz;
+      S->rz[k] = rzk;
+      S->rr[k] = rrk;
+      S->norm_b[k] = nb;
+      S->rel[k] = (fl & kFlagDone) ? 0.0 : 1.0;
+      S->alpha[k] = S->beta[k] = S->pAp[k] = 0.0;
+      S->flags[k] = fl;
+      S->iters[k] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      S->iter = 0;
+      S->tol = tol;
+      S->max_iters = max_iters;
+      S->ncols = ncols;
+      all_done(S);
+    }
+  }
+}
+
+// u += alpha p, r -= alpha Ap, z = D^-1 r (not stored); r.z, r.r per column,
+// then the per-column stopping test rel = sqrt(r.r)/||b|| < tol
+// (cuda_pcg_backend_impl.hpp:723-729) and beta = rz_new / rz.
+template <typename T>
+__global__ void __launch_bounds__(kVT, 1)
+k_mupdate(int n, T* __restrict__ u, T* __restrict__ r, const T* __restrict__ p,
+          const T* __restrict__ Ap, const T* __restrict__ dinv, MultiState* S, double* partials,
+          unsigned* counter) {
+  if (S->done) return;
+  __shared__ double s_red[kVT];
+  __shared__ double s_tot[2 * kP];
+  const int cb = 4 * (threadIdx.x & 3);
+  T al[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) al[j] = static_cast<T>(S->alpha[cb + j]);
+  T rz[4] = {T(0), T(0), T(0), T(0)}, rr[4] = {T(0), T(0), T(0), T(0)};
+  const long long nc = static_cast<long long>(n) * 4;
+  for (long long c = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x; c < nc;
+       c += static_cast<long long>(gridDim.x) * kVT) {
+    const long long i = c >> 2;
+    const size_t o = static_cast<size_t>(i) * kP + cb;
+    T uv[4], rv[4], pv[4], av[4];
+    ld4(u + o, uv);
+    ld4(r + o, rv);
+    ld4(p + o, pv);
+    ld4(Ap + o, av);
+    const T d = dinv[i];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      uv[j] = fmaT(al[j], pv[j], uv[j]);
+      rv[j] = fmaT(-al[j], av[j], rv[j]);
+      const T z = rv[j] * d;
+      rz[j] = fmaT(rv[j], z, rz[j]);
+      rr[j] = fmaT(rv[j], rv[j], rr[j]);
+    }
+    st4(u + o, uv);
+    st4(r + o, rv);
+  }
+  double a[2][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    a[0][j] = static_cast<double>(rz[j]);
+    a[1][j] = static_cast<double>(rr[j]);
+  }
+  if (mcol_sum_last<2, 4, kVT>(a, cb, partials, counter, s_red, s_tot)) {
+    if (threadIdx.x < kP) {
+      const int k = threadIdx.x;
+      int fl = S->flags[k];
+      if (!(fl & kFlagDone)) {
+        const double rzn = s_tot[k], rrk = s_tot[kP + k];
+        const double rel = sqrt(fabs(rrk)) / S->norm_b[k];
+        const int it = S->iter + 1;
+        S->rr[k] = rrk;
+        S->rel[k] = rel;
+        if (rel < S->tol) {
+          fl |= kFlagDone | kFlagConverged;
+          S->beta[k] = 0.0;
+          S->iters[k] = it;
+        } else {
+          S->beta[k] = rzn / S->rz[k];
+          if (it >= S->max_iters) {
+            fl |= kFlagDone | kFlagMaxIters;
+            S->iters[k] = it;
+          }
+        }
+        S->rz[k] = rzn;
+        S->flags[k] = fl;
+      } else {
+        S->beta[k] = 0.0;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      S->iter += 1;
+      all_done(S);
+    }
+  }
+}
+
+// p = D^-1 r + beta p.
+template <typename T>
+__global__ void __launch_bounds__(kVT, 1)
+k_mdirection(int n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ p,
+             const MultiState* S) {
+  if (S->done) return;
+  const int cb = 4 * (threadIdx.x & 3);
+  T be[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) be[j] = static_cast<T>(S->beta[cb + j]);
+  const long long nc = static_cast<long long>(n) * 4;
+  for (long long c = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x; c < nc;
+       c += static_cast<long long>(gridDim.x) * kVT) {
+    const long long i = c >> 2;
+    const size_t o = static_cast<size_t>(i) * kP + cb;
+    T rv[4], pv[4];
+    ld4(r + o, rv);
+    ld4(p + o, pv);
+    const T d = dinv[i];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) pv[j] = fmaT(be[j], pv[j], rv[j] * d);
+    st4(p + o, pv);
+  }
+}
+
+// u64 += d32 / scale for the columns refined in this step.
+__global__ void __launch_bounds__(kVT, 1)
+k_maccumulate(int n, double* __restrict__ u64, const float* __restrict__ d32,
+              const MultiOuter* O) {
+  const int k = threadIdx.x & 15;
+  const bool act = O->active[k] != 0;
+  const double inv = 1.0 / O->scale[k];
+  if (!act) return;
+  const long long tot = static_cast<long long>(n) * kP;
+  for (long long i = static_cast<long long>(blockIdx.x) * kVT + threadIdx.x; i < tot;
+       i += static_cast<long long>(gridDim.x) * kVT)
+    u64[i] = fma(static_cast<double>(d32[i]), inv, u64[i]);
+}
+
+}  // namespace
+
+}  // namespace vsgb
+
+namespace vsgb {
+
+struct MultiWork {
+  DevBuf<double> f, r64, u64, p64, Ap64;  // FP64 panels
+  DevBuf<float> r32, u32, p32, Ap32;      // FP32 panels (mixed inner solves)
+  DevBuf<MultiState> S;
+  DevBuf<MultiOuter> O;
+  DevBuf<double> partials;
+  DevBuf<unsigned> counters;
+  MultiState* hS = nullptr;  // pinned
+  MultiOuter* hO = nullptr;  // pinned
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  unsigned exec_epoch[2] = {0, 0};
+  int exec_batch[2] = {0, 0};
+  unsigned epoch = 1;     // bumped whenever a buffer moves or the operator changes
+  unsigned op_gen = 0;    // operator generation the buffers were sized for
+
+  ~MultiWork() {
+    for (auto& g : exec)
+      if (g) cudaGraphExecDestroy(g);
+    if (hS) cudaFreeHost(hS);
+    if (hO) cudaFreeHost(hO);
+  }
+};
+
+void destroy_multi(MultiWork* w) { delete w; }
+
+namespace {
+
+int occupancy_grid(const void* fn, int num_sms) {
+  int per_sm = 0;
+  VSGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMT, 0));
+  return num_sms * (per_sm > 0 ? per_sm : 1);
+}
+
+// One iteration for T: SpMM (+alpha), update (+beta, stopping test), direction.
+template <typename T, int G>
+void launch_multi_iter(const MView& B, const T* vals, const T* dinv, T* r, T* u, T* p, T* Ap,
+                       MultiWork& W, int n, dim3 sgrid, int vgrid, cudaStream_t s) {
+  k_mspmm<T, G><<<sgrid, kMT, 0, s>>>(B, vals, p, Ap, W.S.ptr, W.partials.ptr, W.counters.ptr + 1);
+  k_mupdate<T><<<vgrid, kVT, 0, s>>>(n, u, r, p, Ap, dinv, W.S.ptr, W.partials.ptr,
+                                     W.counters.ptr + 2);
+  k_mdirection<T><<<vgrid, kVT, 0, s>>>(n, r, dinv, p, W.S.ptr);
+}
+
+}  // namespace
+
+void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed, double tol,
+                            double inner_tol, int max_iters, int max_solves, cudaStream_t s,
+                            std::vector<SolveResult>& res) {
+  if (!use_bsr_) throw Error(VSGB_ERR_STATE, "batched PCG needs the 3x3 block operator");
+  if (mixed && !(bsr_.has32 && has32_))
+    throw Error(VSGB_ERR_STATE, "batched mixed PCG needs the FP32 operator copy");
+  if (!multi_) multi_ = new MultiWork();
+  MultiWork& W = *multi_;
+  if (W.op_gen != generation_) {
+    W.op_gen = generation_;
+    ++W.epoch;
+  }
+  const size_t n = static_cast<size_t>(n_);
+  const size_t np = n * kP;
+  auto grow = [&W](auto& buf, size_t cnt) {
+    if (cnt > buf.cap) {
+      buf.reserve(cnt);
+      ++W.epoch;
+    }
+  };
+  grow(W.f, np);
+  grow(W.u64, np);
+  grow(W.r64, np);
+  if (mixed) {
+    grow(W.r32, np);
+    grow(W.u32, np);
+    grow(W.p32, np);
+    grow(W.Ap32, np);
+  } else {
+    grow(W.p64, np);
+    grow(W.Ap64, np);
+  }
+  grow(W.S, 1);
+  grow(W.O, 1);
+  grow(W.counters, 8);
+  if (!W.hS) VSGB_CUDA(cudaMallocHost(&W.hS, sizeof(MultiState)));
+  if (!W.hO) VSGB_CUDA(cudaMallocHost(&W.hO, sizeof(MultiOuter)));
+
+  const MView B{bsr_.nb, bsr_.nslices, bsr_.slice_ptr.ptr, bsr_.cols.ptr};
+  const int vgrid = grid_for(static_cast<long long>(n) * 4, kVT, num_sms_);
+  const int slice_blocks = (bsr_.nslices + kMT / 32 - 1) / (kMT / 32);
+  auto cap = [slice_blocks](int g) { return g < slice_blocks ? g : (slice_blocks > 0 ? slice_blocks : 1); };
+  const dim3 g32(cap(occupancy_grid(reinterpret_cast<const void*>(&k_mspmm<float, 16>), num_sms_)), 1);
+  const dim3 g64(cap(occupancy_grid(reinterpret_cast<const void*>(&k_mspmm<double, 8>), num_sms_)), 2);
+  const dim3 gres(cap(occupancy_grid(reinterpret_cast<const void*>(&k_mresidual<8>), num_sms_)), 2);
+  size_t pmax = static_cast<size_t>(vgrid);
+  for (const dim3& g : {g32, g64, gres})
+    if (static_cast<size_t>(g.x) * g.y > pmax) pmax = static_cast<size_t>(g.x) * g.y;
+  grow(W.partials, pmax * 2 * kP);
+  VSGB_CUDA(cudaMemsetAsync(W.counters.ptr, 0, sizeof(unsigned) * 8, s));
+
+  auto read_state = [&]() {
+    VSGB_CUDA(cudaMemcpyAsync(W.hS, W.S.ptr, sizeof(MultiState), cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  };
+  auto read_outer = [&]() {
+    VSGB_CUDA(cudaMemcpyAsync(W.hO, W.O.ptr, sizeof(MultiOuter), cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  };
+  auto batch = [&](bool fp32) {
+    for (int k = 0; k < check_every_; ++k) {
+      if (fp32)
+        launch_multi_iter<float, 16>(B, bsr_.val32.ptr, dinv32_.ptr, W.r32.ptr, W.u32.ptr,
+                                     W.p32.ptr, W.Ap32.ptr, W, n_, g32, vgrid, s);
+      else
+        launch_multi_iter<double, 8>(B, bsr_.val64.ptr, op_->dinv.ptr, W.r64.ptr, W.u64.ptr,
+                                     W.p64.ptr, W.Ap64.ptr, W, n_, g64, vgrid, s);
+    }
+    VSGB_LAUNCH_CHECK();
+    VSGB_CUDA(cudaMemcpyAsync(W.hS, W.S.ptr, sizeof(MultiState), cudaMemcpyDeviceToHost, s));
+  };
+  // Batches of check_every iterations (a cached CUDA graph) until every
+  // column reports done; the device stops itself at max_iters.
+  auto iterate_all = [&](bool fp32) {
+    const int key = fp32 ? 1 : 0;
+    if (use_graph_ && (W.exec[key] == nullptr || W.exec_epoch[key] != W.epoch ||
+                       W.exec_batch[key] != check_every_)) {
+      if (W.exec[key]) {
+        cudaGraphExecDestroy(W.exec[key]);
+        W.exec[key] = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      VSGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        batch(fp32);
+      } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      VSGB_CUDA(cudaStreamEndCapture(s, &g));
+      VSGB_CUDA(cudaGraphInstantiate(&W.exec[key], g, 0));
+      cudaGraphDestroy(g);
+      W.exec_epoch[key] = W.epoch;
+      W.exec_batch[key] = check_every_;
+    }
+    const long long max_batches = (static_cast<long long>(max_iters) + check_every_ - 1) /
+                                      check_every_ + 4;
+    for (long long b = 0;; ++b) {
+      if (b > max_batches)
+        throw Error(VSGB_ERR_CUDA, "batched PCG device state did not report completion");
+      if (use_graph_)
+        VSGB_CUDA(cudaGraphLaunch(W.exec[key], s));
+      else
+        batch(fp32);
+      launches_ += 3LL * check_every_;
+      VSGB_CUDA(cudaStreamSynchronize(s));
+      if (W.hS->done) break;
+    }
+  };
+  auto check_start = [&]() {
+    for (int k = 0; k < kP; ++k)
+      if (W.hS->flags[k] & kFlagNonPosRz)
+        throw Error(VSGB_ERR_SINGULAR,
+                    "GB300 PCG: non-positive initial r*z=" + std::to_string(W.hS->rz[k]) +
+                        " -- preconditioner is not SPD or matrix is singular");
+  };
+
+  res.assign(static_cast<size_t>(nrhs), SolveResult{});
+  const int pack_grid = static_cast<int>((n + 31) / 32);
+  for (int k0 = 0; k0 < nrhs; k0 += kP) {
+    const int nc = nrhs - k0 < kP ? nrhs - k0 : kP;
+    k_pack<<<pack_grid, kMT, 0, s>>>(n_, nc, d_F + static_cast<size_t>(k0) * n, W.f.ptr);
+    VSGB_LAUNCH_CHECK();
+    ++launches_;
+    if (!mixed) {
+      k_minit<double><<<vgrid, kVT, 0, s>>>(n_, nc, W.f.ptr, nullptr, op_->dinv.ptr, W.r64.ptr,
+                                            W.u64.ptr, W.p64.ptr, W.S.ptr, tol, max_iters,
+                                            W.partials.ptr, W.counters.ptr);
+      VSGB_LAUNCH_CHECK();
+      ++launches_;
+      read_state();
+      check_start();
+      if (!W.hS->done) iterate_all(false);
+      read_state();
+      for (int k = 0; k < nc; ++k) {
+        SolveResult& R = res[static_cast<size_t>(k0 + k)];
+        const int fl = W.hS->flags[k];
+        R.iterations = W.hS->iters[k];
+        R.rel = W.hS->rel[k];
+        R.converged = (fl & kFlagConverged) != 0;
+        R.breakdown = (fl & kFlagBreakdown) != 0;
+      }
+    } else {
+      k_mouter_init<<<vgrid, kVT, 0, s>>>(n_, nc, W.f.ptr, W.r64.ptr, W.u64.ptr, W.O.ptr,
+                                          W.partials.ptr, W.counters.ptr + 3);
+      VSGB_LAUNCH_CHECK();
+      ++launches_;
+      read_outer();
+      for (int k = 0; k < nc; ++k) res[static_cast<size_t>(k0 + k)].inner_solves = 0;
+      for (int step = 0; step < max_solves && !W.hO->done; ++step) {
+        k_minit<float><<<vgrid, kVT, 0, s>>>(n_, nc, W.r64.ptr, W.O.ptr, dinv32_.ptr, W.r32.ptr,
+                                             W.u32.ptr, W.p32.ptr, W.S.ptr, inner_tol, max_iters,
+                                             W.partials.ptr, W.counters.ptr);
+        VSGB_LAUNCH_CHECK();
+        ++launches_;
+        read_state();
+        check_start();
+        if (!W.hS->done) iterate_all(true);
+        read_state();
+        bool failed = false;
+        for (int k = 0; k < nc; ++k) {
+          if (!W.hO->active[k]) continue;
+          SolveResult& R = res[static_cast<size_t>(k0 + k)];
+          ++R.inner_solves;
+          R.iterations += W.hS->iters[k];
+          if (!(W.hS->flags[k] & kFlagConverged)) {
+            R.inner_failed = true;
+            R.breakdown = (W.hS->flags[k] & kFlagBreakdown) != 0;
+            R.rel = W.hS->rel[k];
+            failed = true;
+          }
+        }
+        if (failed) return;
+        k_maccumulate<<<num_sms_, kVT, 0, s>>>(n_, W.u64.ptr, W.u32.ptr, W.O.ptr);
+        k_mresidual<8><<<gres, kMT, 0, s>>>(B, bsr_.val64.ptr, W.u64.ptr, W.f.ptr, W.r64.ptr,
+                                            W.O.ptr, tol, W.partials.ptr, W.counters.ptr + 4);
+        VSGB_LAUNCH_CHECK();
+        launches_ += 2;
+        read_outer();
+      }
+      for (int k = 0; k < nc; ++k) {
+        SolveResult& R = res[static_cast<size_t>(k0 + k)];
+        const int fl = W.hO->flags[k];
+        R.rel = W.hO->rel[k];
+        R.converged = (fl & kFlagConverged) != 0;
+        R.stalled = (fl & kFlagStalled) != 0;
+      }
+    }
+    k_unpack<<<pack_grid, kMT, 0, s>>>(n_, nc, W.u64.ptr, d_U + static_cast<size_t>(k0) * n);
+    VSGB_LAUNCH_CHECK();
+    ++launches_;
+  }
+}
+
+}  // namespace vsgb

@@ -960,6 +960,7 @@ double PcgEngine::spmv_bytes(int precision) const {
 PcgEngine::~PcgEngine() {
   for (auto& g : graph_exec_)
     if (g) cudaGraphExecDestroy(g);
+  destroy_multi(multi_);
 }
 
 // ── Allocation-free FP64 PCG (vsgb_pcg_solve_noalloc) ─────────────────────

@@ -8,6 +8,9 @@
 
 namespace vsgb {
 
+struct MultiWork;
+void destroy_multi(MultiWork* w);
+
 struct SolveResult {
   int iterations = 0;
   int inner_solves = 1;
@@ -54,6 +57,16 @@ class PcgEngine {
   void add_launches(long long k) { launches_ += k; }
   int num_sms() const { return num_sms_; }
 
+  // Batched PCG over several load cases (3x3 block operator only): every
+  // iteration sweeps the matrix once for up to 16 right-hand sides, each
+  // with its own alpha/beta and convergence test.  d_F and d_U are
+  // column-major n x nrhs device arrays (load case k at F + k*n).  Mixed
+  // precision runs FP32 inner solves with per-case FP64 refinement.
+  bool multi_supported() const { return use_bsr_; }
+  void solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed, double tol,
+                   double inner_tol, int max_iters, int max_solves, cudaStream_t s,
+                   std::vector<SolveResult>& res);
+
  private:
   void ensure_vectors(bool mixed);
   void read_scalars(cudaStream_t s, PcgScalars* host, int which);
@@ -92,6 +105,8 @@ class PcgEngine {
   unsigned graph_gen_[2] = {0, 0};
   int graph_batch_[2] = {0, 0};
   PcgScalars* graph_host_[2] = {nullptr, nullptr};
+
+  MultiWork* multi_ = nullptr;  // batched-solve buffers (multi.cu)
 };
 
 }  // namespace vsgb
