@@ -56,9 +56,11 @@ extern "C" {
 #define VSGB_OPT_USE_GRAPH 7      /* 1: replay iteration batches as CUDA graphs (default 1) */
 #define VSGB_OPT_FORMAT 8         /* 0 auto, 1 scalar CSR, 2 3x3 node blocks */
 #define VSGB_OPT_RESIDENT 9       /* 1: one persistent launch per PCG solve (default 1) */
-#define VSGB_OPT_BATCHED 10       /* 1: nrhs > 1 solves all load cases in one batched PCG
-                                     on the 3x3 block operator (default 1); 0: one solve
-                                     per load case, as the reference's subcase loop */
+#define VSGB_OPT_BATCHED 10       /* load cases (nrhs > 1) on the 3x3 block operator:
+                                     0 one solve per case, as the reference's subcase
+                                     loop; 1 (default) one batched PCG from 4 cases
+                                     (mixed) or 10 cases (FP64) up, where it is faster;
+                                     2 always batched */
 
 typedef struct vsgb_ctx vsgb_ctx;
 
@@ -138,10 +140,10 @@ int vsgb_assemble_chexa8(vsgb_ctx* ctx, int n_nodes, const double* node_xyz,
 int vsgb_copy_csr_lower(vsgb_ctx* ctx, int* row_ptr, int* col_ind, double* values);
 
 /* Solve with the resident K: F[n*nrhs] host -> u_out[n*nrhs] host.
- * nrhs > 1 on the 3x3 block operator runs the load cases as one batched PCG
- * (16 right-hand sides per matrix sweep, each with its own recurrence and
- * stopping test); the scalar-CSR operator, or VSGB_OPT_BATCHED = 0, solves
- * them one after another. */
+ * Several load cases on the 3x3 block operator run as one batched PCG (16
+ * right-hand sides per matrix sweep, each with its own recurrence and
+ * stopping test) as VSGB_OPT_BATCHED selects; otherwise, and on the
+ * scalar-CSR operator, they are solved one after another. */
 int vsgb_solve_assembled(vsgb_ctx* ctx, const double* F, int nrhs, double* u_out,
                          vsgb_stats* stats);
 
@@ -167,6 +169,19 @@ int vsgb_solution_download(vsgb_ctx* ctx, double* u_out);
  * for compliance F^T u, lambda = u). */
 int vsgb_element_sensitivity(vsgb_ctx* ctx, const double* u, const double* lambda,
                              double* dJdE_out);
+
+/* Adjoint gradients of the resident model with respect to every element's
+ * Young's modulus.  No counterpart in the reference (it has no sensitivity
+ * analysis); the functionals are compliance C = F^T u and a linear response
+ * J = dJdu^T u.  Solves K [u, lambda] = [F, dJdu] (one load case when dJdu
+ * is NULL) with the context's precision and tolerance, then in one pass over
+ * the stored element matrices
+ *   dC/dE_e = -u_e^T K_e^0 u_e,   dJ/dE_e = -lambda_e^T K_e^0 u_e,
+ * K_e^0 = K_e / E_e.  u_out[n], lambda_out[n], dCdE_out[n_elem] and
+ * dJdE_out[n_elem] may each be NULL; lambda_out and dJdE_out need dJdu. */
+int vsgb_adjoint_gradients(vsgb_ctx* ctx, const double* F, const double* dJdu, double* u_out,
+                           double* lambda_out, double* dCdE_out, double* dJdE_out,
+                           vsgb_stats* stats);
 
 /* ── measurement helpers ────────────────────────────────────────────────── */
 

@@ -309,3 +309,68 @@ def solve_model(model, tol=None, load_index=0, direct=True):
     else:
         u, _, _ = pcg_jacobi(K, F, tol or 1e-10, 100000)
     return eq6, n, K, F, u
+
+
+# ── gradients with respect to element moduli ──────────────────────────────
+# The reference has no sensitivity analysis; these restate the adjoint of the
+# linear-static equations K(E) u = F for the GPU gradients to be checked
+# against: for J = c^T u, dJ/dE_e = -lam_e^T (dK_e/dE_e) u_e with K lam = c,
+# and dK_e/dE_e = K_e / E_e because the CHEXA8 stiffness is linear in E for a
+# fixed Poisson ratio (isotropic_D, src/elements/solid_elements.cpp:17-27).
+
+def element_dofs(model, eq6) -> np.ndarray:
+    """(M, 24) equation numbers of each element's T1-T3 DOFs, -1 when
+    constrained (solid_global_dof_indices, src/elements/solid_elements.cpp:29-42)."""
+    return np.asarray(eq6)[model.conn][:, :, :3].reshape(model.n_elem, 24)
+
+
+def element_gradient(model, eq6, u, lam, kes=None, elems=None) -> np.ndarray:
+    """FP64 dJ/dE_e = -lam_e^T (K_e / E_e) u_e for every element, or for the
+    listed elements only (their K_e formed one by one)."""
+    idx = element_dofs(model, eq6)
+    E = np.asarray(model.E)
+    if elems is not None:
+        elems = np.asarray(elems)
+        idx, E = idx[elems], E[elems]
+        kes = np.stack([chexa8_ke(model.xyz[model.conn[e]], model.E[e], model.nu[e],
+                                  model.form[e]) for e in elems])
+    elif kes is None:
+        kes = chexa8_ke_batch(model)
+
+    def take(v):
+        return np.where(idx >= 0, np.asarray(v, np.float64)[np.maximum(idx, 0)], 0.0)
+
+    return -np.einsum("ei,eij,ej->e", take(lam), kes, take(u)) / E
+
+
+def fd_gradient(model, eq6, K: Csr, u, C, elems, h=1e-4, kes=None) -> np.ndarray:
+    """Central differences of J_k = C[:, k]^T u for E_e -> E_e (1 +- h).
+
+    Difference form: with dK = +-h K_e (the element's stiffness scales with
+    E_e), (K + dK) du = -dK u gives J(E_e (1 +- h)) - J = C^T du exactly, so
+    nothing is lost to subtracting two nearly equal solutions.  Sparse direct
+    solves in FP64.  Returns (len(elems), C.shape[1])."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    kes = chexa8_ke_batch(model) if kes is None else kes
+    C = np.asarray(C, np.float64).reshape(K.n, -1)
+    full = K.expanded_symmetric() if K.lower else K
+    A = sp.csr_matrix((full.values, full.col_ind, full.row_ptr), shape=(K.n, K.n))
+    idx = element_dofs(model, eq6)
+    out = np.zeros((len(elems), C.shape[1]))
+    for t, e in enumerate(elems):
+        sel = idx[e] >= 0
+        g = idx[e][sel]
+        Ke = kes[e][np.ix_(sel, sel)]
+        rows = np.repeat(g, g.shape[0])
+        cols = np.tile(g, g.shape[0])
+        dJ = []
+        for s in (1.0, -1.0):
+            dK = s * h * Ke
+            Ap = (A + sp.csr_matrix((dK.reshape(-1), (rows, cols)), shape=A.shape)).tocsc()
+            rhs = np.zeros(K.n)
+            rhs[g] = -(dK @ np.asarray(u)[g])
+            du = spla.spsolve(Ap, rhs, permc_spec="MMD_AT_PLUS_A")
+            dJ.append(C.T @ du)
+        out[t] = (dJ[0] - dJ[1]) / (2.0 * h * model.E[e])
+    return out

@@ -34,7 +34,7 @@ def _rel(a, b):
 def _assembled(vsgb, m, eq6, n, mixed, tol, batched, inner=0.0):
     cls = vsgb.Gb300MixedPcgSolverBackend if mixed else vsgb.Gb300PcgSolverBackend
     be = cls.try_create(tol, 20000)
-    be.set_option(vsgb.OPT_BATCHED, 1 if batched else 0)
+    be.set_option(vsgb.OPT_BATCHED, 2 if batched else 0)
     if inner:
         be.set_option(vsgb.OPT_INNER_TOL, inner)
         be.set_option(vsgb.OPT_MAX_SOLVES, 6)
@@ -60,7 +60,7 @@ def test_batched_fp64_matches_sequential_and_direct(vsgb, multi_model):
         assert abs(stats_b[k]["iterations"] - stats_s[k]["iterations"]) <= 2, k
         assert stats_b[k]["rel_residual"] < 1e-10
     # batched solve is bitwise reproducible
-    be.set_option(vsgb.OPT_BATCHED, 1)
+    be.set_option(vsgb.OPT_BATCHED, 2)
     assert np.array_equal(asm.solve(F), Ub)
     be.close()
 
@@ -101,7 +101,7 @@ def test_batched_csr_entry_point(vsgb, oracle, multi_model):
     K = vsgb.CsrData(Ko.row_ptr, Ko.col_ind, Ko.values, Ko.n, Ko.nnz, Ko.lower)
     be = vsgb.Gb300PcgSolverBackend.try_create(1e-10, 20000)
     Ub = be.solve(K, F[:, :16])
-    assert be.rhs_stats(0)["batched"]
+    assert be.rhs_stats(0)["batched"]  # auto mode batches 16 FP64 cases
     for k in range(16):
         assert _rel(Ub[:, k], U[:, k]) <= 1e-8, k
     be.close()
@@ -110,6 +110,7 @@ def test_batched_csr_entry_point(vsgb, oracle, multi_model):
 def test_batched_not_converged_raises(vsgb, multi_model):
     m, eq6, n, F, U = multi_model
     be = vsgb.Gb300PcgSolverBackend.try_create(1e-12, 5)
+    be.set_option(vsgb.OPT_BATCHED, 2)
     asm = vsgb.ChexaAssembler(be)
     asm.assemble(m, eq6, n)
     with pytest.raises(vsgb.SolverError, match="did not converge after 5 iterations"):

@@ -57,7 +57,7 @@ OPT_BATCHED = 10
 
 # The symbols include/vsgb.h declares (checked by tests against the .so).
 EXPORTS = (
-    "vsgb_rhs_stats",
+    "vsgb_rhs_stats", "vsgb_adjoint_gradients",
     "vsgb_create", "vsgb_destroy", "vsgb_set_option", "vsgb_last_error", "vsgb_device_name",
     "vsgb_backend_name", "vsgb_solve_csr", "vsgb_build_dof_map", "vsgb_apply_forces",
     "vsgb_assemble_chexa8", "vsgb_copy_csr_lower", "vsgb_solve_assembled", "vsgb_mesh_upload",
@@ -134,6 +134,7 @@ def load_library(build_if_missing: bool = False):
     L.vsgb_time_spmv.argtypes = [vp, c_int, c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)]
     L.vsgb_kernel_launches.argtypes = [vp]
     L.vsgb_kernel_launches.restype = c_ll
+    L.vsgb_adjoint_gradients.argtypes = [vp, _f64p, vp, vp, vp, vp, vp, ctypes.POINTER(VsgbStats)]
     L.vsgb_rhs_stats.argtypes = [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_dbl),
                                  ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.vsgb_pcg_solve_noalloc.argtypes = [c_int, c_int, vp, vp, vp, vp, vp, c_dbl, c_int, vp,
@@ -396,6 +397,28 @@ class ChexaAssembler:
         self.backend.context.check(
             load_library().vsgb_solution_download(self.backend.context.ptr, u))
         return u if nrhs == 1 else u.reshape(nrhs, self.n).T.copy()
+
+    def adjoint_gradients(self, F, dJdu=None, with_adjoint=False):
+        """Compliance and linear-response gradients w.r.t. every element's E
+        from one solve of K [u, lam] = [F, dJdu]: returns (u, dC/dE, dJ/dE or
+        None), plus lam when with_adjoint."""
+        F = np.ascontiguousarray(F, np.float64)
+        u = np.zeros(self.n)
+        dC = np.zeros(self.n_elem)
+        has_j = dJdu is not None
+        dJ = np.zeros(self.n_elem) if has_j else None
+        lam = np.zeros(self.n) if (has_j and with_adjoint) else None
+        dj_in = np.ascontiguousarray(dJdu, np.float64) if has_j else None
+
+        def ptr(a):
+            return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+        st = VsgbStats()
+        self.backend.context.check(load_library().vsgb_adjoint_gradients(
+            self.backend.context.ptr, F, ptr(dj_in), ptr(u), ptr(lam), ptr(dC), ptr(dJ),
+            ctypes.byref(st)))
+        self.backend._record(st)
+        return (u, dC, dJ, lam) if with_adjoint else (u, dC, dJ)
 
     def sensitivity(self, u, lam) -> np.ndarray:
         out = np.zeros(self.n_elem)

@@ -174,6 +174,17 @@ def face_random_loads(m: SolidModel, nrhs: int, rng: np.random.Generator,
     return loads
 
 
+def tip_mean_uz_functional(m: SolidModel, eq6: np.ndarray, n: int) -> np.ndarray:
+    """dJ/du of J = mean of -u_z over the free x = L (i = nx) face nodes."""
+    nx, ny, nz = m.shape
+    i = (m.node_ids - 1) // ((ny + 1) * (nz + 1))
+    eqz = np.asarray(eq6)[np.nonzero(i == nx)[0], 2]
+    eqz = eqz[eqz >= 0]
+    c = np.zeros(n)
+    c[eqz] = -1.0 / eqz.shape[0]
+    return c
+
+
 def block_160k_16rhs(seed: int = 20260304, nrhs: int = 16) -> SolidModel:
     rng = np.random.default_rng(seed)
     m = block(100, 40, 40, 0.01, name="block_160k_16rhs")

@@ -53,7 +53,8 @@ struct vsgb_ctx {
   long long launches = 0;
   int last_iters = 0;
   double last_rel = 0.0;
-  bool batched = true;                 // several load cases share each matrix sweep
+  DevBuf<double> grad;                 // adjoint gradients (2 x n_elem)
+  int batched = 1;                     // 0 never, 1 auto, 2 always batch load cases
   bool last_batched = false;
   std::vector<vsgb::SolveResult> rhs;  // per-load-case results of the last solve
 };
@@ -171,8 +172,18 @@ void run_batched(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
   }
 }
 
+// Auto mode batches from the load-case count where one 16-wide sweep beats
+// that many single-case iterations of the persistent solver: about 3 (mixed,
+// the FP32 sweep is bound by gathering the 16-wide panel) and about 9 (FP64,
+// both forms are bound by the FP64 pipe).
+bool use_batched(const vsgb_ctx* c, int nrhs) {
+  if (nrhs < 2 || c->batched == 0 || !c->eng->multi_supported()) return false;
+  if (c->batched == 2) return true;
+  return nrhs >= (c->precision == VSGB_MIXED ? 4 : 10);
+}
+
 void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
-  if (nrhs > 1 && c->batched && c->eng->multi_supported()) {
+  if (use_batched(c, nrhs)) {
     run_batched(c, nrhs, stats);
     return;
   }
@@ -322,9 +333,12 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
         c->eng->set_resident(value != 0.0);
         if (c->assembled) c->eng->prepare(c->K, c->precision == VSGB_MIXED, c->stream);
         break;
-      case VSGB_OPT_BATCHED:
-        c->batched = value != 0.0;
+      case VSGB_OPT_BATCHED: {
+        const int b = static_cast<int>(value);
+        if (b < 0 || b > 2) throw Error(VSGB_ERR_INVALID, "batched mode must be 0, 1 or 2");
+        c->batched = b;
         break;
+      }
       default:
         throw Error(VSGB_ERR_INVALID, "unknown option " + std::to_string(option));
     }
@@ -544,10 +558,45 @@ int vsgb_element_sensitivity(vsgb_ctx* c, const double* u, const double* lambda,
     upload(du.ptr, u, sizeof(double) * c->n_dof, s);
     upload(dl.ptr, lambda, sizeof(double) * c->n_dof, s);
     vsgb::launch_element_sensitivity(c->n_elem, c->conn.ptr, c->eq3.ptr, c->E.ptr, c->kbuf.ptr,
-                                     du.ptr, dl.ptr, out.ptr, c->num_sms, s);
+                                     du.ptr, dl.ptr, out.ptr, nullptr, nullptr, c->num_sms, s);
     c->eng->add_launches(1);
     VSGB_CUDA(cudaMemcpyAsync(dJdE_out, out.ptr, sizeof(double) * c->n_elem,
                               cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int vsgb_adjoint_gradients(vsgb_ctx* c, const double* F, const double* dJdu, double* u_out,
+                           double* lambda_out, double* dCdE_out, double* dJdE_out,
+                           vsgb_stats* stats) {
+  return guarded(c, [&] {
+    if (!c->assembled) throw Error(VSGB_ERR_STATE, "nothing assembled");
+    if (!F) throw Error(VSGB_ERR_INVALID, "vsgb_adjoint_gradients: F is null");
+    if ((dJdE_out || lambda_out) && !dJdu)
+      throw Error(VSGB_ERR_INVALID, "vsgb_adjoint_gradients: dJ/du is needed for lambda / dJdE");
+    cudaStream_t s = c->stream;
+    const size_t n = static_cast<size_t>(c->K.n);
+    const int nrhs = dJdu ? 2 : 1;
+    c->f.reserve(n * nrhs);
+    upload(c->f.ptr, F, sizeof(double) * n, s);
+    if (dJdu) upload(c->f.ptr + n, dJdu, sizeof(double) * n, s);
+    c->nrhs = nrhs;
+    run_solves(c, nrhs, stats);  // u and lambda from one batched solve
+    c->grad.reserve(2 * static_cast<size_t>(c->n_elem) + 2);
+    double* dC = c->grad.ptr;
+    double* dJ = c->grad.ptr + c->n_elem + 1;
+    // compliance: lambda = u; J: lambda solves K lambda = dJ/du
+    vsgb::launch_element_sensitivity(c->n_elem, c->conn.ptr, c->eq3.ptr, c->E.ptr, c->kbuf.ptr,
+                                     c->u.ptr, c->u.ptr, dC, dJdu ? c->u.ptr + n : nullptr,
+                                     dJdu ? dJ : nullptr, c->num_sms, s);
+    c->eng->add_launches(1);
+    if (u_out) VSGB_CUDA(cudaMemcpyAsync(u_out, c->u.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    if (lambda_out)
+      VSGB_CUDA(cudaMemcpyAsync(lambda_out, c->u.ptr + n, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    if (dCdE_out)
+      VSGB_CUDA(cudaMemcpyAsync(dCdE_out, dC, sizeof(double) * c->n_elem, cudaMemcpyDeviceToHost, s));
+    if (dJdE_out)
+      VSGB_CUDA(cudaMemcpyAsync(dJdE_out, dJ, sizeof(double) * c->n_elem, cudaMemcpyDeviceToHost, s));
     VSGB_CUDA(cudaStreamSynchronize(s));
   });
 }

@@ -344,23 +344,29 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
 }
 
 // Adjoint sensitivity: dJ/dE_e = -lam_e^T (Ke / E_e) u_e (Ke is linear in E
-// for fixed nu).  One warp per element; Ke rows read from the stiffness buffer.
+// for fixed nu, so dK_e/dE_e = Ke / E_e).  One warp per element; lane r < 24
+// forms row r of Ke u_e from the stored element matrix (the 24 row reads of
+// one element share their sectors through L1), then the lam and lam2 dot
+// products are warp sums.  FP64-pipe bound: 24 warp FMAs per element.
 __global__ void k_element_sensitivity(int n_elem, const int* __restrict__ conn,
                                       const int* __restrict__ eq3, const double* __restrict__ E,
                                       const double* __restrict__ kbuf,
                                       const double* __restrict__ u,
                                       const double* __restrict__ lam,
-                                      double* __restrict__ out) {
+                                      double* __restrict__ out,
+                                      const double* __restrict__ lam2,
+                                      double* __restrict__ out2) {
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (blockDim.x >> 5);
   for (int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < n_elem;
        e += warps_total) {
-    double ue = 0.0, le = 0.0;
+    double ue = 0.0, le = 0.0, le2 = 0.0;
     if (lane < 24) {
       const int eq = eq3[3 * conn[8 * e + lane / 3] + lane % 3];
       if (eq >= 0) {
         ue = u[eq];
         le = lam[eq];
+        if (lam2) le2 = lam2[eq];
       }
     }
     // (Ke u_e)_r for r = lane
@@ -368,11 +374,15 @@ __global__ void k_element_sensitivity(int n_elem, const int* __restrict__ conn,
     double acc = 0.0;
     for (int c = 0; c < 24; ++c) {
       const double uc = __shfl_sync(0xffffffffu, ue, c);
-      if (lane < 24) acc = fma(ke[lane * 24 + c], uc, acc);
+      if (lane < 24) acc = fma(__ldg(&ke[lane * 24 + c]), uc, acc);
     }
-    double v = (lane < 24) ? le * acc : 0.0;
-    v = warp_sum(v);
-    if (lane == 0) out[e] = -v / E[e];
+    const double inv_e = 1.0 / E[e];
+    const double v = warp_sum((lane < 24) ? le * acc : 0.0);
+    if (lane == 0) out[e] = -v * inv_e;
+    if (out2) {
+      const double v2 = warp_sum((lane < 24) ? le2 * acc : 0.0);
+      if (lane == 0) out2[e] = -v2 * inv_e;
+    }
   }
 }
 
@@ -396,10 +406,12 @@ void launch_chexa8_stiffness(int n_elem, const double* xyz, const int* conn, con
 
 void launch_element_sensitivity(int n_elem, const int* conn, const int* eq3, const double* E,
                                 const double* kbuf, const double* u, const double* lam,
-                                double* out, int num_sms, cudaStream_t s) {
+                                double* out, const double* lam2, double* out2, int num_sms,
+                                cudaStream_t s) {
   if (n_elem <= 0) return;
   const int grid = grid_for(static_cast<long long>(n_elem) * 32, kThreads, num_sms * 16);
-  k_element_sensitivity<<<grid, kThreads, 0, s>>>(n_elem, conn, eq3, E, kbuf, u, lam, out);
+  k_element_sensitivity<<<grid, kThreads, 0, s>>>(n_elem, conn, eq3, E, kbuf, u, lam, out, lam2,
+                                                  out2);
   VSGB_LAUNCH_CHECK();
 }
 
