@@ -135,6 +135,138 @@ def _barrier(dist):
         dist.barrier()
 
 
+def _mixed_backend(B, device, tol=None, max_solves=None):
+    be = B.Gb300MixedPcgSolverBackend.try_create(tol or MIXED_TOL, 50000, device)
+    be.set_option(B.OPT_INNER_TOL, MIXED_INNER_TOL)
+    be.set_option(B.OPT_MAX_SOLVES, max_solves or MIXED_MAX_SOLVES)
+    return be
+
+
+def extra_multi_rhs(B, C, device):
+    """16 load cases on the 100x40x40 block (n = 504 300): one batched mixed
+    PCG (16 right-hand sides per matrix sweep, CUDA-graph replayed) against 16
+    sequential persistent mixed solves, same tolerances."""
+    m = C.block_160k_16rhs()
+    eq6, n = B.build_dof_map(m)
+    F = np.stack([B.apply_forces(m, eq6, n, k) for k in range(16)], axis=1)
+    be = _mixed_backend(B, device)
+    asm = B.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    asm.upload_rhs(F)
+    out = {"workload": "block_160k_16rhs", "elements": m.n_elem, "dofs": n, "rhs": 16,
+           "seed": m.seed}
+    U = {}
+    for mode, flag in (("batched", 2), ("sequential", 0)):
+        be.set_option(B.OPT_BATCHED, flag)
+        asm.solve_resident()  # warm-up (graphs, buffers)
+        B.timer_start(be)
+        st = asm.solve_resident()
+        ms = B.timer_stop(be)
+        its = [be.rhs_stats(k)["iterations"] for k in range(16)]
+        U[mode] = asm.download()
+        out[mode] = {"solve_s": ms / 1e3, "iterations_max": max(its),
+                     "iterations_sum": int(sum(its)), "rel_residual_max": st.rel_residual}
+    out["speedup_batched_vs_sequential"] = out["sequential"]["solve_s"] / out["batched"]["solve_s"]
+    out["max_rel_diff_batched_vs_sequential"] = float(max(
+        np.linalg.norm(U["batched"][:, k] - U["sequential"][:, k]) /
+        np.linalg.norm(U["sequential"][:, k]) for k in range(16)))
+    be.close()
+    return out
+
+
+def extra_adjoint(B, C, device, n_fd=4):
+    """Gradients of compliance and of the mean -z tip displacement w.r.t. all
+    250 000 element moduli (100x50x50, n = 780 300, log-uniform E): one call
+    (solves of K [u, lam] = [F, c] + one element pass), checked against the
+    FP64 CPU gradient on 1024 seeded elements and central differences
+    (relative step 1e-4, difference form, GPU re-assembly) on n_fd elements."""
+    import copy
+    from oracle import oracle as O
+    m = C.block_250k_adjoint()
+    eq6, n = B.build_dof_map(m)
+    F = B.apply_forces(m, eq6, n)
+    c = C.tip_mean_uz_functional(m, eq6, n)
+    be = _mixed_backend(B, device, tol=1e-10, max_solves=8)
+    asm = B.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    asm.adjoint_gradients(F, c)  # warm-up
+    t0 = time.perf_counter()
+    u, dC, dJ, lam = asm.adjoint_gradients(F, c, with_adjoint=True)
+    wall = time.perf_counter() - t0
+    st = be.last_stats
+    sub = np.sort(np.random.default_rng(5).choice(m.n_elem, 1024, replace=False))
+    gC = O.element_gradient(m, eq6, u, u, elems=sub)
+    gJ = O.element_gradient(m, eq6, u, lam, elems=sub)
+    h, fd_err = 1e-4, 0.0
+    be.set_option(B.OPT_TOLERANCE, 1e-11)
+    idx = O.element_dofs(m, eq6)
+    for e in np.sort(np.random.default_rng(2026).choice(m.n_elem, n_fd, replace=False)):
+        Ke = O.chexa8_ke(m.xyz[m.conn[e]], m.E[e], m.nu[e], m.form[e])
+        sel = idx[e] >= 0
+        g = idx[e][sel]
+        d = []
+        for s in (1.0, -1.0):
+            m2 = copy.copy(m)
+            m2.E = m.E.copy()
+            m2.E[e] *= 1.0 + s * h
+            asm.assemble(m2, eq6, n)
+            rhs = np.zeros(n)
+            rhs[g] = -(s * h * Ke[np.ix_(sel, sel)]) @ u[g]
+            du = asm.solve(rhs)
+            d.append((F @ du, c @ du))
+        for k, ref in ((0, dC[e]), (1, dJ[e])):
+            fd = (d[0][k] - d[1][k]) / (2.0 * h * m.E[e])
+            fd_err = max(fd_err, abs(fd - ref) / abs(ref))
+    be.close()
+    return {"workload": "block_250k_adjoint", "elements": m.n_elem, "dofs": n, "seed": m.seed,
+            "functionals": ["compliance F.u", "mean -u_z over the tip face"],
+            "gradient_s": wall, "solve_s": st.solve_ms / 1e3, "iterations": st.iterations,
+            "inner_solves": st.inner_solves, "tolerance": 1e-10,
+            "cpu_fp64_gradient_max_rel_err": float(max(
+                np.abs(gC - dC[sub]).max() / np.abs(dC).max(),
+                np.abs(gJ - dJ[sub]).max() / np.abs(dJ).max())),
+            "central_fd_max_rel_err": fd_err, "fd_elements": n_fd}
+
+
+def extra_jitter(B, C, device, uniform):
+    """Jittered (U(+-0.2 h) interior nodes) heterogeneous (log-uniform E)
+    84 000-element cantilever: FP64 and mixed iteration counts at the headline
+    tolerances against the uniform mesh's, and the error against the FP64
+    sparse-direct fingerprint."""
+    m = C.cantilever_84k_jitter()
+    eq6, n = B.build_dof_map(m)
+    F = B.apply_forces(m, eq6, n)
+    be = _mixed_backend(B, device)
+    asm = B.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    asm.upload_rhs(F)
+    asm.solve_resident()
+    st_m = asm.solve_resident()
+    u_m = asm.download()
+    be.set_option(B.OPT_PRECISION, B.FP64)
+    be.set_option(B.OPT_TOLERANCE, FP64_TOL)
+    asm.solve_resident()
+    st_d = asm.solve_resident()
+    u_d = asm.download()
+    be.close()
+    out = {"workload": "cantilever_84k_jitter", "dofs": n, "seed": m.seed,
+           "fp64": {"iterations": st_d.iterations, "solve_s": st_d.solve_ms / 1e3},
+           "mixed": {"iterations_fp32": st_m.iterations, "inner_solves": st_m.inner_solves,
+                     "solve_s": st_m.solve_ms / 1e3},
+           "iteration_growth_vs_uniform": {
+               "fp64": st_d.iterations / uniform["fp64"],
+               "fp32_inner": st_m.iterations / uniform["mixed"]}}
+    path = os.path.join(ROOT, "tests", "golden", "cantilever_84k_jitter_direct.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            g = json.load(fh)
+        eqs = np.concatenate([g["tip_eq"], g["sample_eq"]])
+        ref = np.concatenate([g["tip_uz"], g["sample_u"]])
+        for key, u in (("fp64", u_d), ("mixed", u_m)):
+            out[key]["rel_err_vs_direct"] = float(np.linalg.norm(u[eqs] - ref) / np.linalg.norm(ref))
+    return out
+
+
 def cpu_reference(model, eq6, n, F, steps, warmup, threads):
     """CPU restatement of the reference path on the host cores (oracle port)."""
     from oracle import oracle as O
@@ -157,6 +289,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the 16-load-case, adjoint and jittered-mesh measurements")
     a = ap.parse_args()
 
     from vibestran_gb300 import cantilever as C
@@ -227,6 +361,12 @@ def main():
     u_mixed = asm.download()
     err_mixed = float(np.linalg.norm(u_mixed - u_ref) / np.linalg.norm(u_ref))
     t_step = _allmax(dist, ms / 1e3 / a.steps)
+    # Dominant kernel of the timed region: the persistent FP32 inner solve
+    # (one launch per inner solve), timed by events around each launch.
+    res_ms = sum(s.kernel_ms for s in stats)
+    res_it = sum(s.kernel_iterations for s in stats)
+    res_launches = sum(s.inner_solves for s in stats)
+    res_bytes_it = stats[-1].spmv_bytes
 
     # Phase split: assembly alone and solve alone (device events inside the library).
     B.timer_start(be)
@@ -242,11 +382,11 @@ def main():
     u_fp64 = asm.download()
     err_fp64 = float(np.linalg.norm(u_fp64 - u_ref) / np.linalg.norm(u_ref))
 
-    # Dominant kernel roofline: the FP32 block SpMV of the inner solve.
+    # Launch-path block SpMVs (not in the step) for comparison.
     spmv_ms, spmv_bytes = B.time_spmv(be, B.MIXED, 200)
     spmv64_ms, spmv64_bytes = B.time_spmv(be, B.FP64, 200)
     peak, peak_kind = _peaks()
-    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    achieved = res_it * res_bytes_it / (res_ms * 1e-3) / 1e9 if res_ms > 0 else None
     be.set_option(B.OPT_PRECISION, B.MIXED)
     be.set_option(B.OPT_TOLERANCE, MIXED_TOL)
 
@@ -273,6 +413,13 @@ def main():
     cpu_t, cpu_used, cpu_iters = cpu_reference(model, eq6, n, F, a.cpu_steps, 1,
                                                os.cpu_count() or 1)
     it_mixed = st_mixed.iterations
+    extras = None
+    if not a.no_extras:
+        be_e2e.close()
+        extras = {"multi_rhs_16": extra_multi_rhs(B, C, device),
+                  "adjoint_250k": extra_adjoint(B, C, device),
+                  "jitter_84k": extra_jitter(B, C, device,
+                                             {"fp64": st_fp64.iterations, "mixed": it_mixed})}
     line = {
         "metric": METRIC,
         "value": t_step / 1.0,  # seconds per SOL 101 step (whole job: max over ranks)
@@ -301,15 +448,21 @@ def main():
         "fp64": {"solve_s": statistics.median(fp64_solve) / 1e3, "iterations": st_fp64.iterations,
                  "pcg_iter_per_s": st_fp64.iterations / (statistics.median(fp64_solve) / 1e3)},
         "speedup_mixed_vs_fp64_solve": statistics.median(fp64_solve) / statistics.median(mixed_solve),
-        "roofline": {"kernel": "k_bsr_spmv32_fused", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind,
-                     "traffic": _traffic("k_bsr_spmv32_fused"),
-                     "algorithmic_bytes": spmv_bytes, "avg_launch_us": spmv_ms * 1e3,
-                     "fp64_spmv": {"avg_launch_us": spmv64_ms * 1e3, "bytes": spmv64_bytes,
-                                   "achieved_gbs": spmv64_bytes / (spmv64_ms * 1e-3) / 1e9,
-                                   "fp64_fma_floor_us":
-                                       2.0 * (2 * asm.nnz_lower - n) / FP64_TFLOPS / 1e6}},
+        "roofline": {"kernel": "k_resident_pcg<float> (persistent FP32 inner solve)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
+                     "traffic": _traffic("k_resident_pcg_f32"),
+                     "algorithmic_bytes": res_it * res_bytes_it / max(res_launches, 1),
+                     "avg_launch_us": 1e3 * res_ms / max(res_launches, 1),
+                     "iterations_per_launch": res_it / max(res_launches, 1),
+                     "bytes_per_iteration": res_bytes_it,
+                     "us_per_iteration": 1e3 * res_ms / res_it if res_it else None,
+                     "launch_path_spmv32": {"avg_launch_us": spmv_ms * 1e3, "bytes": spmv_bytes,
+                                            "achieved_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9},
+                     "launch_path_spmv64": {"avg_launch_us": spmv64_ms * 1e3, "bytes": spmv64_bytes,
+                                            "achieved_gbs": spmv64_bytes / (spmv64_ms * 1e-3) / 1e9,
+                                            "fp64_fma_floor_us":
+                                                2.0 * (2 * asm.nnz_lower - n) / FP64_TFLOPS / 1e6}},
         "cpu_baseline": {"value": cpu_t, "unit": "s", "cores": cpu_used, "kind": "port",
                          "sample": f"full workload x{a.cpu_steps}: element stiffness + build_csr "
                                    f"+ FP64 Jacobi PCG ({cpu_iters} it, tol {FP64_TOL:g})"},
@@ -318,6 +471,8 @@ def main():
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
     }
+    if extras is not None:
+        line["extra_workloads"] = extras
     print(json.dumps(line))
 
 

@@ -61,6 +61,9 @@ extern "C" {
                                      loop; 1 (default) one batched PCG from 4 cases
                                      (mixed) or 10 cases (FP64) up, where it is faster;
                                      2 always batched */
+#define VSGB_OPT_L2_PERSIST 11    /* 1: mark the operator values persisting in L2 during
+                                     each persistent PCG launch (default 0: measured no
+                                     gain, the solve is not bound by L2 misses) */
 
 typedef struct vsgb_ctx vsgb_ctx;
 
@@ -75,6 +78,10 @@ typedef struct vsgb_stats {
   double solve_ms;       /* device time of the iteration phase (CUDA events) */
   double setup_ms;       /* device time of operator preparation (upload/expand/convert) */
   double spmv_bytes;     /* algorithmic bytes of one SpMV of the operator used */
+  double kernel_ms;      /* device time of the persistent (one launch per solve) PCG
+                            kernels of this solve, CUDA events around each launch;
+                            0 when the launch-per-kernel path ran */
+  double kernel_iterations; /* PCG iterations those launches ran */
 } vsgb_stats;
 
 /* Create a context on `device` (cuda-pcg uses device 0,

@@ -116,3 +116,44 @@ def test_cantilever_84k_full_size(vsgb, oracle):
     um = asm.solve(F)
     assert rel_err(um) <= 1e-6
     be.close()
+
+
+def test_cantilever_84k_jitter_full_size(vsgb, oracle):
+    """Jittered heterogeneous 84 000-element cantilever (interior nodes moved by
+    seeded U(+-0.2 h), log-uniform E per element): DOF map and pattern against
+    the oracle, displacements against the FP64 sparse-direct fingerprint
+    (FP64 PCG <= 1e-8, mixed <= 1e-6), with and without the L2 window."""
+    from vibestran_gb300 import cantilever as C
+    with open(os.path.join(GOLDEN, "cantilever_84k_jitter_direct.json")) as fh:
+        g = json.load(fh)
+    m = C.cantilever_84k_jitter()
+    assert m.seed == g["seed"]
+    eq6, n = vsgb.build_dof_map(m)
+    eq_o, n_o = oracle.dof_map(m)
+    assert n == n_o == g["n"] and np.array_equal(eq6, eq_o)
+    F = vsgb.apply_forces(m, eq6, n)
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-10, 50000)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    K = asm.csr_lower()
+    Ko = oracle.assemble_chexa8(m, eq_o, n_o)
+    assert np.array_equal(K.row_ptr, Ko.row_ptr) and np.array_equal(K.col_ind, Ko.col_ind)
+    assert np.abs(K.values - Ko.values).max() <= 1e-12 * np.abs(Ko.values).max()
+    del K, Ko
+    eqs = np.concatenate([g["tip_eq"], g["sample_eq"]])
+    ref = np.concatenate([g["tip_uz"], g["sample_u"]])
+
+    def rel_err(u):
+        return np.linalg.norm(u[eqs] - ref) / np.linalg.norm(ref)
+
+    u = asm.solve(F)
+    assert be.last_stats.format == 2 and rel_err(u) <= 1e-8
+    be.set_option(vsgb.OPT_PRECISION, vsgb.MIXED)
+    be.set_option(vsgb.OPT_TOLERANCE, 1e-6)
+    be.set_option(vsgb.OPT_INNER_TOL, 1e-3)
+    be.set_option(vsgb.OPT_MAX_SOLVES, 6)
+    for l2 in (1, 0):
+        be.set_option(vsgb.OPT_L2_PERSIST, l2)
+        um = asm.solve(F)
+        assert rel_err(um) <= 1e-6, l2
+    be.close()

@@ -54,6 +54,7 @@ OPT_USE_GRAPH = 7
 OPT_FORMAT = 8
 OPT_RESIDENT = 9
 OPT_BATCHED = 10
+OPT_L2_PERSIST = 11
 
 # The symbols include/vsgb.h declares (checked by tests against the .so).
 EXPORTS = (
@@ -80,7 +81,8 @@ class VsgbStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("inner_solves", ctypes.c_int),
                 ("converged", ctypes.c_int), ("format", ctypes.c_int),
                 ("rel_residual", ctypes.c_double), ("solve_ms", ctypes.c_double),
-                ("setup_ms", ctypes.c_double), ("spmv_bytes", ctypes.c_double)]
+                ("setup_ms", ctypes.c_double), ("spmv_bytes", ctypes.c_double),
+                ("kernel_ms", ctypes.c_double), ("kernel_iterations", ctypes.c_double)]
 
 
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

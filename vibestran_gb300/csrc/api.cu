@@ -55,6 +55,8 @@ struct vsgb_ctx {
   double last_rel = 0.0;
   DevBuf<double> grad;                 // adjoint gradients (2 x n_elem)
   int batched = 1;                     // 0 never, 1 auto, 2 always batch load cases
+  bool csr_ready = false;              // K holds the scalar full CSR
+  bool blocks_prebuilt = false;        // the engine's block operator came from assemble_blocks
   bool last_batched = false;
   std::vector<vsgb::SolveResult> rhs;  // per-load-case results of the last solve
 };
@@ -126,6 +128,31 @@ void reset_assembly_error(vsgb_ctx* c) {
   c->scr.err.reserve(1);
   VSGB_CUDA(cudaMemsetAsync(c->scr.err.ptr, 0, sizeof(vsgb::AssemblyError), c->stream));
   c->scr.flag.reserve(1);
+}
+
+// Scalar full CSR of the resident mesh from the stored element matrices
+// (after a block assembly it is built on first request).
+void ensure_csr(vsgb_ctx* c) {
+  if (c->csr_ready) return;
+  if (!c->mesh_ok) throw Error(VSGB_ERR_STATE, "no mesh uploaded");
+  reset_assembly_error(c);
+  vsgb::assemble_csr(c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof, c->kbuf.ptr,
+                     c->scr, c->K, c->num_sms, c->stream);
+  c->eng->add_launches(18);
+  check_assembly_error(c);
+  c->csr_ready = true;
+}
+
+// (Re)binds the operator to the engine for the current precision and format.
+void prepare_operator(vsgb_ctx* c) {
+  const bool mixed = c->precision == VSGB_MIXED;
+  if (c->blocks_prebuilt && c->format != 1) {
+    c->eng->prepare(c->K, mixed, c->stream, true);
+    return;
+  }
+  ensure_csr(c);
+  c->blocks_prebuilt = false;  // a scalar prepare may rebuild the blocks from the CSR
+  c->eng->prepare(c->K, mixed, c->stream);
 }
 
 std::string not_converged_text(const vsgb_ctx* c, double rel) {
@@ -215,6 +242,8 @@ void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
     ms_total += ms;
     st.iterations = res.iterations > st.iterations ? res.iterations : st.iterations;
     st.inner_solves += res.inner_solves;
+    st.kernel_ms += c->eng->resident_ms();
+    st.kernel_iterations += static_cast<double>(c->eng->resident_iterations());
     st.rel_residual = res.rel > st.rel_residual ? res.rel : st.rel_residual;
     c->last_iters = res.iterations;
     c->last_rel = res.rel;
@@ -308,8 +337,9 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
       case VSGB_OPT_PRECISION: {
         const int p = static_cast<int>(value);
         if (p != VSGB_FP64 && p != VSGB_MIXED) throw Error(VSGB_ERR_INVALID, "bad precision");
-        if (p != c->precision && c->assembled) c->eng->prepare(c->K, p == VSGB_MIXED, c->stream);
+        const bool changed = p != c->precision;
         c->precision = p;
+        if (changed && c->assembled) prepare_operator(c);
         break;
       }
       case VSGB_OPT_INNER_TOL:
@@ -327,11 +357,14 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
       case VSGB_OPT_FORMAT:
         c->format = static_cast<int>(value);
         c->eng->set_format(c->format);
-        if (c->assembled) c->eng->prepare(c->K, c->precision == VSGB_MIXED, c->stream);
+        if (c->assembled) prepare_operator(c);
         break;
       case VSGB_OPT_RESIDENT:
         c->eng->set_resident(value != 0.0);
-        if (c->assembled) c->eng->prepare(c->K, c->precision == VSGB_MIXED, c->stream);
+        if (c->assembled) prepare_operator(c);
+        break;
+      case VSGB_OPT_L2_PERSIST:
+        c->eng->set_l2_persist(value != 0.0);
         break;
       case VSGB_OPT_BATCHED: {
         const int b = static_cast<int>(value);
@@ -391,6 +424,8 @@ int vsgb_solve_csr(vsgb_ctx* c, int n, int nnz, const int* row_ptr, const int* c
     vsgb::prepare_full_csr(n, nnz, c->in_rp.ptr, c->in_ci.ptr, c->in_v.ptr, lower_only != 0,
                            c->scr, c->K, c->num_sms, s);
     check_assembly_error(c);
+    c->csr_ready = true;
+    c->blocks_prebuilt = false;
     c->eng->prepare(c->K, c->precision == VSGB_MIXED, s);
     VSGB_CUDA(cudaEventRecord(c->ev[3], s));
     c->f.reserve(static_cast<size_t>(n) * nrhs);
@@ -464,9 +499,23 @@ int vsgb_assemble_resident(vsgb_ctx* c, long long* nnz_lower_out) {
                                   c->elem_err.ptr, c->num_sms, s);
     c->eng->add_launches(1);
     reset_assembly_error(c);
-    vsgb::assemble_csr(c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof, c->kbuf.ptr,
-                       c->scr, c->K, c->num_sms, s);
-    c->eng->add_launches(18);
+    c->csr_ready = false;
+    c->blocks_prebuilt = false;
+    // Node-aligned equations: assemble the 3x3 block operator directly; the
+    // scalar CSR is built only when asked for (vsgb_copy_csr_lower, or the
+    // scalar format).
+    if (c->format != 1 &&
+        vsgb::assemble_blocks(c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof,
+                              c->kbuf.ptr, c->scr, c->K, c->eng->blocks(),
+                              c->precision == VSGB_MIXED, c->num_sms, s)) {
+      c->blocks_prebuilt = true;
+      c->eng->add_launches(12);
+    } else {
+      vsgb::assemble_csr(c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof, c->kbuf.ptr,
+                         c->scr, c->K, c->num_sms, s);
+      c->csr_ready = true;
+      c->eng->add_launches(18);
+    }
     vsgb::ElementError he{};
     VSGB_CUDA(cudaMemcpyAsync(&he, c->elem_err.ptr, sizeof(he), cudaMemcpyDeviceToHost, s));
     VSGB_CUDA(cudaStreamSynchronize(s));
@@ -477,7 +526,7 @@ int vsgb_assemble_resident(vsgb_ctx* c, long long* nnz_lower_out) {
                       (he.code == 2 ? ": Kaa factorization failed" : ": non-positive Jacobian"));
     }
     check_assembly_error(c);
-    c->eng->prepare(c->K, c->precision == VSGB_MIXED, s);
+    prepare_operator(c);
     c->assembled = true;
     if (nnz_lower_out) *nnz_lower_out = c->K.nnz_lower;
   });
@@ -496,6 +545,7 @@ int vsgb_copy_csr_lower(vsgb_ctx* c, int* row_ptr, int* col_ind, double* values)
   return guarded(c, [&] {
     if (!c->assembled) throw Error(VSGB_ERR_STATE, "nothing assembled");
     cudaStream_t s = c->stream;
+    ensure_csr(c);
     DevBuf<int> lrp, lci;
     DevBuf<double> lv;
     lrp.reserve(static_cast<size_t>(c->K.n) + 1);
@@ -622,7 +672,8 @@ int vsgb_timer_stop(vsgb_ctx* c, double* ms) {
 int vsgb_time_spmv(vsgb_ctx* c, int precision, int reps, double* avg_ms, double* bytes) {
   return guarded(c, [&] {
     if (!c->assembled && c->K.n == 0) throw Error(VSGB_ERR_STATE, "no operator");
-    if (precision == VSGB_MIXED && !c->eng->has32()) c->eng->prepare(c->K, true, c->stream);
+    if (precision == VSGB_MIXED && !c->eng->has32())
+      c->eng->prepare(c->K, true, c->stream, c->blocks_prebuilt && c->format != 1);
     c->eng->time_spmv(precision, reps > 0 ? reps : 20, c->stream, avg_ms);
     if (bytes) *bytes = c->eng->spmv_bytes(precision);
   });

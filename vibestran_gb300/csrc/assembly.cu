@@ -16,6 +16,7 @@
 
 #include <climits>
 
+#include "bsr.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -209,6 +210,88 @@ __device__ __forceinline__ int warp_incl_scan(int v) {
   return v;
 }
 
+// Distinct neighbour nodes of node a (itself included) over its incident
+// elements, those with a free DOF only, ordered by their first free equation
+// into s.nbr.  Returns their number, or -1 (error 3 recorded) when node a
+// exceeds the valence / neighbour limits.  Warp-collective.
+__device__ int gather_neighbors(int a, int pb, int L, const int* __restrict__ conn,
+                                const int* __restrict__ eq3, const int* __restrict__ node_elem,
+                                PatSmem& s, AssemblyError* err) {
+  const int lane = threadIdx.x & 31;
+  if (L > kMaxValence) {
+    if (lane == 0) set_error(err, 3, a);
+    return -1;
+  }
+  const int C = 8 * L;
+  for (int c = lane; c < C; c += 32) {
+    const int slot = node_elem[pb + (c >> 3)];
+    const int b = conn[(slot & ~7) + (c & 7)];
+    s.cand[c] = b;
+    s.key[c] = first_free_eq(eq3, b);
+  }
+  __syncwarp();
+  for (int c = lane; c < C; c += 32) {
+    const int b = s.cand[c];
+    int f = s.key[c] != INT_MAX;
+    for (int m = 0; m < c && f; ++m)
+      if (s.cand[m] == b) f = 0;
+    s.first[c] = f;
+  }
+  __syncwarp();
+  int U = 0;
+  for (int c = lane; c < C; c += 32) {
+    if (s.first[c]) {
+      const int k = s.key[c];
+      int r = 0;
+      for (int m = 0; m < C; ++m) r += (s.first[m] && s.key[m] < k);
+      if (r < kMaxNbr) s.nbr[r] = s.cand[c];
+    }
+  }
+  for (int c = lane; c < C; c += 32) U += s.first[c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) U += __shfl_xor_sync(0xffffffffu, U, o);
+  if (U > kMaxNbr) {
+    if (lane == 0) set_error(err, 3, a);
+    return -1;
+  }
+  __syncwarp();
+  return U;
+}
+
+// The 3x3 block coupling node a (rows) with node b (columns), summed over the
+// incident elements of a in ascending element order; nz marks entries that
+// received a value != 0.0 (add_element_stiffness, src/core/sparse_matrix.cpp:31).
+__device__ __forceinline__ void node_block(int b, int pb, int L, const int* __restrict__ conn,
+                                           const int* __restrict__ node_elem,
+                                           const double* __restrict__ kbuf, double (&sum)[3][3],
+                                           bool (&nz)[3][3]) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      sum[d][q] = 0.0;
+      nz[d][q] = false;
+    }
+  for (int k = 0; k < L; ++k) {
+    const int slot = node_elem[pb + k];
+    const int e = slot >> 3, la = slot & 7;
+    int lb = -1;
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+      if (conn[8 * e + m] == b) lb = m;
+    if (lb < 0) continue;
+    const double* ke = kbuf + static_cast<size_t>(e) * 576 + (3 * la) * 24 + 3 * lb;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const double v = ke[d * 24 + q];
+        sum[d][q] += v;
+        nz[d][q] = nz[d][q] || (v != 0.0);
+      }
+  }
+}
+
 template <bool kFill>
 __global__ void __launch_bounds__(kPatWarps * 32)
 k_pattern(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3,
@@ -226,43 +309,8 @@ k_pattern(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3
     for (int d = 0; d < 3; ++d) row[d] = eq3[3 * a + d];
     if (row[0] < 0 && row[1] < 0 && row[2] < 0) continue;
     const int pb = node_ptr[a], L = node_ptr[a + 1] - pb;
-    if (L > kMaxValence) {
-      if (lane == 0) set_error(err, 3, a);
-      continue;
-    }
-    const int C = 8 * L;
-    for (int c = lane; c < C; c += 32) {
-      const int slot = node_elem[pb + (c >> 3)];
-      const int b = conn[(slot & ~7) + (c & 7)];
-      s.cand[c] = b;
-      s.key[c] = first_free_eq(eq3, b);
-    }
-    __syncwarp();
-    for (int c = lane; c < C; c += 32) {
-      const int b = s.cand[c];
-      int f = s.key[c] != INT_MAX;
-      for (int m = 0; m < c && f; ++m)
-        if (s.cand[m] == b) f = 0;
-      s.first[c] = f;
-    }
-    __syncwarp();
-    int U = 0;
-    for (int c = lane; c < C; c += 32) {
-      if (s.first[c]) {
-        const int k = s.key[c];
-        int r = 0;
-        for (int m = 0; m < C; ++m) r += (s.first[m] && s.key[m] < k);
-        if (r < kMaxNbr) s.nbr[r] = s.cand[c];
-      }
-    }
-    for (int c = lane; c < C; c += 32) U += s.first[c];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) U += __shfl_xor_sync(0xffffffffu, U, o);
-    if (U > kMaxNbr) {
-      if (lane == 0) set_error(err, 3, a);
-      continue;
-    }
-    __syncwarp();
+    const int U = gather_neighbors(a, pb, L, conn, eq3, node_elem, s, err);
+    if (U < 0) continue;
 
     int carry[3] = {0, 0, 0};
     int base[3] = {0, 0, 0};
@@ -278,34 +326,18 @@ k_pattern(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3
       int colq[3] = {-1, -1, -1};
       double sum[3][3];
       bool nz[3][3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d)
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          sum[d][q] = 0.0;
-          nz[d][q] = false;
-        }
       if (act) {
 #pragma unroll
         for (int q = 0; q < 3; ++q) colq[q] = eq3[3 * b + q];
-        for (int k = 0; k < L; ++k) {
-          const int slot = node_elem[pb + k];
-          const int e = slot >> 3, la = slot & 7;
-          int lb = -1;
+        node_block(b, pb, L, conn, node_elem, kbuf, sum, nz);
+      } else {
 #pragma unroll
-          for (int m = 0; m < 8; ++m)
-            if (conn[8 * e + m] == b) lb = m;
-          if (lb < 0) continue;
-          const double* ke = kbuf + static_cast<size_t>(e) * 576 + (3 * la) * 24 + 3 * lb;
+        for (int d = 0; d < 3; ++d)
 #pragma unroll
-          for (int d = 0; d < 3; ++d)
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              const double v = ke[d * 24 + q];
-              sum[d][q] += v;
-              nz[d][q] = nz[d][q] || (v != 0.0);
-            }
-        }
+          for (int q = 0; q < 3; ++q) {
+            sum[d][q] = 0.0;
+            nz[d][q] = false;
+          }
       }
       int cnt[3];
 #pragma unroll
@@ -361,6 +393,138 @@ k_pattern(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3
       for (int d = 0; d < 3; ++d) {
         const bool seen = __any_sync(0xffffffffu, diag_seen[d]);
         if (lane == 0 && row[d] >= 0 && !seen) set_error(err, 5, row[d]);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ── direct 3x3 node-block assembly (node-aligned equations) ───────────────
+//
+// When every node with a free DOF owns the equation triple (3R, 3R+1, 3R+2)
+// (the reference's DofMap with whole-node constraints), block row R is node
+// a's row and block column C is neighbour b's, and the neighbour blocks that
+// k_pattern forms are written straight into the sliced-ELL operator (no
+// scalar CSR, no CSR-to-block conversion).  A block is stored when any of its
+// entries received a value != 0.0, so the block pattern is the one the
+// reference's scalar pattern induces; the scalar counts (full and lower
+// triangle) are totalled for reporting.
+
+__global__ void k_node_aligned(int n_nodes, const int* __restrict__ eq3, int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes) return;
+  const int e0 = eq3[3 * i], e1 = eq3[3 * i + 1], e2 = eq3[3 * i + 2];
+  if (e0 < 0 && e1 < 0 && e2 < 0) return;
+  if (!(e0 >= 0 && e0 % 3 == 0 && e1 == e0 + 1 && e2 == e0 + 2)) atomicOr(flag, 1);
+}
+
+template <bool kFill>
+__global__ void __launch_bounds__(kPatWarps * 32)
+k_block_pattern(int n_nodes, int nb, const int* __restrict__ conn, const int* __restrict__ eq3,
+                const int* __restrict__ node_ptr, const int* __restrict__ node_elem,
+                const double* __restrict__ kbuf, int* __restrict__ blen,
+                unsigned long long* __restrict__ counts, const int* __restrict__ slice_ptr,
+                int* __restrict__ cols, double* __restrict__ v64, float* __restrict__ v32,
+                double* __restrict__ dinv, AssemblyError* err) {
+  __shared__ PatSmem smem_all[kPatWarps];
+  PatSmem& s = smem_all[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * kPatWarps;
+  for (int a = blockIdx.x * kPatWarps + (threadIdx.x >> 5); a < n_nodes; a += warps_total) {
+    const int r0 = eq3[3 * a];
+    if (r0 < 0) continue;  // aligned: all three constrained
+    const int R = r0 / 3;
+    const int pb = node_ptr[a], L = node_ptr[a + 1] - pb;
+    const int U = gather_neighbors(a, pb, L, conn, eq3, node_elem, s, err);
+    if (U < 0) continue;
+    const int sl = R >> 3, ln0 = (R & 7) * 4;
+    const long long sp = kFill ? slice_ptr[sl] : 0;
+    int carry = 0;
+    unsigned long long full = 0, lower = 0;
+    bool diag_seen[3] = {false, false, false};
+    for (int u0 = 0; u0 < U; u0 += 32) {
+      const int u = u0 + lane;
+      const bool act = u < U;
+      const int b = act ? s.nbr[u] : a;
+      double sum[3][3];
+      bool nz[3][3];
+      node_block(b, pb, L, conn, node_elem, kbuf, sum, nz);
+      bool any = false;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) any = any || nz[d][q];
+      any = any && act;
+      const int C = eq3[3 * b] / 3;
+      const unsigned m = __ballot_sync(0xffffffffu, any);
+      if (!kFill) {
+        if (any) {
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              full += nz[d][q];
+              lower += nz[d][q] && (3 * C + q <= 3 * R + d);
+            }
+        }
+      } else if (any) {
+        const int j = carry + __popc(m & ((1u << lane) - 1u));
+        const long long st = sp + (j >> 2);
+        const int ln = ln0 + (j & 3);
+        cols[st * 32 + ln] = C;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const size_t o = static_cast<size_t>((st * 9 + 3 * d + q) * 32 + ln);
+            if (v64) v64[o] = sum[d][q];
+            if (v32) v32[o] = static_cast<float>(sum[d][q]);
+          }
+        if (b == a) {
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            if (nz[d][d]) {
+              diag_seen[d] = true;
+              if (sum[d][d] == 0.0)
+                set_error(err, 4, 3 * R + d);
+              else
+                dinv[3 * R + d] = 1.0 / sum[d][d];
+            }
+          }
+        }
+      }
+      carry += __popc(m);
+    }
+    if (!kFill) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        full += __shfl_xor_sync(0xffffffffu, full, o);
+        lower += __shfl_xor_sync(0xffffffffu, lower, o);
+      }
+      if (lane == 0) {
+        blen[R] = carry;
+        atomicAdd(&counts[0], full);
+        atomicAdd(&counts[1], lower);
+      }
+    } else {
+      // padding slots of this block row: a valid block column (the slice's
+      // first row) and zero values
+      const int slots = 4 * (slice_ptr[sl + 1] - slice_ptr[sl]);
+      for (int j = carry + lane; j < slots; j += 32) {
+        const long long st = sp + (j >> 2);
+        const int ln = ln0 + (j & 3);
+        cols[st * 32 + ln] = 8 * sl;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          const size_t o = static_cast<size_t>((st * 9 + k) * 32 + ln);
+          if (v64) v64[o] = 0.0;
+          if (v32) v32[o] = 0.f;
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const bool seen = __any_sync(0xffffffffu, diag_seen[d]);
+        if (lane == 0 && !seen) set_error(err, 5, 3 * R + d);
       }
     }
     __syncwarp();
@@ -526,9 +690,12 @@ __global__ void k_diag_inverse(int n, const int* __restrict__ rp, const int* __r
 
 }  // namespace
 
-void assemble_csr(int n_nodes, int n_elem, const int* conn, const int* eq3, int n_dof,
-                  const double* kbuf, AssemblyScratch& scr, AssembledCsr& out, int num_sms,
-                  cudaStream_t s) {
+namespace {
+
+// DOF table validation and the node -> element incidence (ascending element
+// order per node), shared by the scalar and the block assembly.
+void build_incidence(int n_nodes, int n_elem, const int* conn, const int* eq3, int n_dof,
+                     AssemblyScratch& scr, cudaStream_t s) {
   const long long slots = 8LL * n_elem;
   scr.node_cnt.reserve(static_cast<size_t>(n_nodes) + 1);
   scr.node_ptr.reserve(static_cast<size_t>(n_nodes) + 1);
@@ -538,9 +705,6 @@ void assemble_csr(int n_nodes, int n_elem, const int* conn, const int* eq3, int 
   const long long scan_n = n_nodes > n_dof ? n_nodes : n_dof;
   scr.scan_tmp.reserve(scan_tmp_size(scan_n + 1));
   scr.total.reserve(1);
-  out.n = n_dof;
-  out.row_ptr.reserve(static_cast<size_t>(n_dof) + 1);
-  out.dinv.reserve(static_cast<size_t>(n_dof > 0 ? n_dof : 1));
 
   // DOF -> node map and validation of the equation table.
   VSGB_CUDA(cudaMemsetAsync(scr.dof_node.ptr, 0xFF, sizeof(int) * (n_dof > 0 ? n_dof : 1), s));
@@ -565,6 +729,17 @@ void assemble_csr(int n_nodes, int n_elem, const int* conn, const int* eq3, int 
   k_node_sort<<<grid_for(n_nodes, 128, 1 << 30), 128, 0, s>>>(n_nodes, scr.node_ptr.ptr,
                                                               scr.node_elem.ptr);
   VSGB_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+void assemble_csr(int n_nodes, int n_elem, const int* conn, const int* eq3, int n_dof,
+                  const double* kbuf, AssemblyScratch& scr, AssembledCsr& out, int num_sms,
+                  cudaStream_t s) {
+  out.n = n_dof;
+  out.row_ptr.reserve(static_cast<size_t>(n_dof) + 1);
+  out.dinv.reserve(static_cast<size_t>(n_dof > 0 ? n_dof : 1));
+  build_incidence(n_nodes, n_elem, conn, eq3, n_dof, scr, s);
 
   // Pattern count -> row_ptr.
   VSGB_CUDA(cudaMemsetAsync(scr.row_cnt.ptr, 0, sizeof(int) * (n_dof + 1), s));
@@ -605,6 +780,82 @@ void assemble_csr(int n_nodes, int n_elem, const int* conn, const int* eq3, int 
   VSGB_CUDA(cudaMemcpyAsync(&nl, scr.total.ptr, sizeof(long long), cudaMemcpyDeviceToHost, s));
   VSGB_CUDA(cudaStreamSynchronize(s));
   out.nnz_lower = nl;
+}
+
+bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, int n_dof,
+                     const double* kbuf, AssemblyScratch& scr, AssembledCsr& out, BsrSell& B,
+                     bool need32, int num_sms, cudaStream_t s) {
+  if (n_dof <= 0 || n_dof % 3 != 0) return false;
+  scr.flag.reserve(1);
+  VSGB_CUDA(cudaMemsetAsync(scr.flag.ptr, 0, sizeof(int), s));
+  k_node_aligned<<<grid_for(n_nodes, kThreads, 1 << 30), kThreads, 0, s>>>(n_nodes, eq3,
+                                                                         scr.flag.ptr);
+  VSGB_LAUNCH_CHECK();
+  int misaligned = 0;
+  VSGB_CUDA(cudaMemcpyAsync(&misaligned, scr.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  if (misaligned) return false;
+
+  build_incidence(n_nodes, n_elem, conn, eq3, n_dof, scr, s);
+  const int nb = n_dof / 3;
+  B.valid = false;
+  B.rowlen.reserve(static_cast<size_t>(nb));
+  VSGB_CUDA(cudaMemsetAsync(B.rowlen.ptr, 0, sizeof(int) * nb, s));
+  scr.counts.reserve(2);
+  VSGB_CUDA(cudaMemsetAsync(scr.counts.ptr, 0, sizeof(unsigned long long) * 2, s));
+  const int pgrid = grid_for(static_cast<long long>(n_nodes) * 32, kPatWarps * 32, num_sms * 16);
+  k_block_pattern<false><<<pgrid, kPatWarps * 32, 0, s>>>(
+      n_nodes, nb, conn, eq3, scr.node_ptr.ptr, scr.node_elem.ptr, kbuf, B.rowlen.ptr,
+      scr.counts.ptr, nullptr, nullptr, nullptr, nullptr, nullptr, scr.err.ptr);
+  VSGB_LAUNCH_CHECK();
+  unsigned long long cnt[2] = {0, 0};
+  VSGB_CUDA(cudaMemcpyAsync(cnt, scr.counts.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  const long long total_steps = bsr_layout(B, nb, s);  // synchronises
+  // stored blocks (the scan of the row lengths)
+  B.h_blen.resize(static_cast<size_t>(nb));
+  VSGB_CUDA(cudaMemcpyAsync(B.h_blen.data(), B.rowlen.ptr, sizeof(int) * nb,
+                            cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  long long blocks = 0;
+  for (int R = 0; R < nb; ++R) blocks += B.h_blen[R];
+  if (cnt[0] >= static_cast<unsigned long long>(INT_MAX))
+    throw Error(VSGB_ERR_LIMIT, "assembled nnz exceeds the int32 CSR limit");
+  if (blocks == 0 || static_cast<double>(cnt[0]) < 0.9 * 9.0 * static_cast<double>(blocks))
+    return false;
+
+  const size_t nstep = static_cast<size_t>(total_steps > 0 ? total_steps : 1);
+  B.cols.reserve(nstep * 32);
+  B.val64.reserve(nstep * 288);
+  if (need32) B.val32.reserve(nstep * 288);
+  if (nb % 8 != 0) {
+    // lanes of the last slice beyond nb belong to no node: block column 0,
+    // zero values (read, never stored)
+    int last = 0;
+    VSGB_CUDA(cudaMemcpyAsync(&last, B.slice_ptr.ptr + B.nslices - 1, sizeof(int),
+                              cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+    const size_t tail = nstep - static_cast<size_t>(last);
+    VSGB_CUDA(cudaMemsetAsync(B.cols.ptr + static_cast<size_t>(last) * 32, 0, sizeof(int) * tail * 32, s));
+    VSGB_CUDA(cudaMemsetAsync(B.val64.ptr + static_cast<size_t>(last) * 288, 0,
+                              sizeof(double) * tail * 288, s));
+    if (need32)
+      VSGB_CUDA(cudaMemsetAsync(B.val32.ptr + static_cast<size_t>(last) * 288, 0,
+                                sizeof(float) * tail * 288, s));
+  }
+  out.n = n_dof;
+  out.dinv.reserve(static_cast<size_t>(n_dof));
+  k_block_pattern<true><<<pgrid, kPatWarps * 32, 0, s>>>(
+      n_nodes, nb, conn, eq3, scr.node_ptr.ptr, scr.node_elem.ptr, kbuf, nullptr, nullptr,
+      B.slice_ptr.ptr, B.cols.ptr, B.val64.ptr, need32 ? B.val32.ptr : nullptr, out.dinv.ptr,
+      scr.err.ptr);
+  VSGB_LAUNCH_CHECK();
+  out.nnz = static_cast<long long>(cnt[0]);
+  out.nnz_lower = static_cast<long long>(cnt[1]);
+  B.nblocks = blocks;
+  B.has64 = true;
+  B.has32 = need32;
+  B.valid = true;
+  return true;
 }
 
 void extract_lower(const AssembledCsr& full, int* d_row_ptr, int* d_col_ind, double* d_values,

@@ -119,6 +119,26 @@ k_bsr_fill(int nb, const int* __restrict__ rp, const int* __restrict__ ci,
 
 }  // namespace
 
+long long bsr_layout(BsrSell& B, int nb, cudaStream_t s) {
+  const int nslices = (nb + 7) / 8;
+  B.nb = nb;
+  B.nslices = nslices;
+  B.slice_ptr.reserve(static_cast<size_t>(nslices) + 1);
+  B.tmp.reserve(scan_tmp_size(nslices + 1));
+  B.total.reserve(1);
+  DevBuf<int> steps;
+  steps.reserve(static_cast<size_t>(nslices) + 1);
+  k_slice_steps<<<grid_for(nslices, kThreads, 1 << 30), kThreads, 0, s>>>(nb, nslices,
+                                                                          B.rowlen.ptr, steps.ptr);
+  VSGB_LAUNCH_CHECK();
+  exclusive_scan_checked(steps.ptr, B.slice_ptr.ptr, nslices, B.tmp.ptr, B.total.ptr, s);
+  long long total_steps = 0;
+  VSGB_CUDA(cudaMemcpyAsync(&total_steps, B.total.ptr, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  B.steps = total_steps;
+  return total_steps;
+}
+
 bool build_bsr(const AssembledCsr& K, BsrSell& B, bool need64, bool need32, int num_sms,
                cudaStream_t s) {
   B.valid = false;

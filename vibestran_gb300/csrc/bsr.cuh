@@ -30,6 +30,18 @@ struct BsrSell {
 bool build_bsr(const AssembledCsr& K, BsrSell& B, bool need64, bool need32, int num_sms,
                cudaStream_t s);
 
+// Slice steps from the block-row lengths in B.rowlen (nb rows), scanned into
+// B.slice_ptr; sets nb, nslices and steps and returns the total steps.
+long long bsr_layout(BsrSell& B, int nb, cudaStream_t s);
+
+// Block operator straight from the element stiffness buffer when the
+// equations are node-aligned triples (no scalar CSR is built); returns false,
+// with nothing changed in B, when they are not or the blocks are < 90%
+// filled.  out receives n, dinv and the scalar nnz (full and lower).
+bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, int n_dof,
+                     const double* kbuf, AssemblyScratch& scr, AssembledCsr& out, BsrSell& B,
+                     bool need32, int num_sms, cudaStream_t s);
+
 // Algorithmic bytes of one block SpMV (values + block indices + x + y).
 double bsr_bytes(const BsrSell& B, int precision);
 

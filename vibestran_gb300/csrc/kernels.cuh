@@ -40,6 +40,7 @@ struct AssemblyError {
 struct AssemblyScratch {
   DevBuf<int> node_cnt, node_ptr, node_elem, dof_node, row_cnt, lower_rp, scan_tmp, flag;
   DevBuf<long long> total;
+  DevBuf<unsigned long long> counts;  // block assembly: scalar nnz full / lower, blocks
   DevBuf<AssemblyError> err;
 };
 

@@ -554,7 +554,7 @@ k_bsr_residual64(BsrView B, const double* __restrict__ vals, const double* __res
 
 // ── host orchestration ─────────────────────────────────────────────────────
 
-void PcgEngine::prepare(const AssembledCsr& op, bool need32, cudaStream_t s) {
+void PcgEngine::prepare(const AssembledCsr& op, bool need32, cudaStream_t s, bool prebuilt) {
   op_ = &op;
   n_ = op.n;
   const size_t n = static_cast<size_t>(n_ > 0 ? n_ : 1);
@@ -562,7 +562,19 @@ void PcgEngine::prepare(const AssembledCsr& op, bool need32, cudaStream_t s) {
   vec_grid_ = vgrid;
   spmv_grid_ = grid_for(static_cast<long long>(n_) * kLpr, kSpmvThreads, num_sms_ * 8);
   use_bsr_ = false;
-  if (format_ != 1) {
+  if (prebuilt) {
+    // blocks assembled directly (assemble_blocks); add the FP32 copy if asked
+    if (!bsr_.valid) throw Error(VSGB_ERR_STATE, "no block operator was assembled");
+    use_bsr_ = true;
+    if (need32 && !bsr_.has32) {
+      const long long cnt = bsr_.steps * 288;
+      bsr_.val32.reserve(static_cast<size_t>(cnt > 0 ? cnt : 1));
+      k_cast_f32<<<num_sms_ * 8, kThreads, 0, s>>>(cnt, bsr_.val64.ptr, bsr_.val32.ptr);
+      VSGB_LAUNCH_CHECK();
+      launches_ += 1;
+      bsr_.has32 = true;
+    }
+  } else if (format_ != 1) {
     use_bsr_ = build_bsr(op, bsr_, true, need32, num_sms_, s);
     if (!use_bsr_ && format_ == 2)
       throw Error(VSGB_ERR_INVALID, "3x3 block format requested but the equations are not "
@@ -761,13 +773,69 @@ void PcgEngine::iterate(cudaStream_t s, bool fp32, PcgScalars* host) {
   }
 }
 
+// The persistent solve sweeps the same operator values every iteration; an
+// access-policy window marks them persisting in L2 for the launch (the
+// context's set-aside is raised to the device maximum for the launch and
+// restored, and persisting lines are released, right after it).
+void PcgEngine::resident_begin(cudaStream_t s, const void* hot, size_t hot_bytes) {
+  if (!rev_[0]) {
+    VSGB_CUDA(cudaEventCreate(&rev_[0]));
+    VSGB_CUDA(cudaEventCreate(&rev_[1]));
+    int dev = 0, pmax = 0, wmax = 0;
+    VSGB_CUDA(cudaGetDevice(&dev));
+    if (cudaDeviceGetAttribute(&pmax, cudaDevAttrMaxPersistingL2CacheSize, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&wmax, cudaDevAttrMaxAccessPolicyWindowSize, dev) != cudaSuccess) {
+      cudaGetLastError();
+      pmax = wmax = 0;
+    }
+    l2_persist_max_ = pmax > 0 ? static_cast<size_t>(pmax) : 0;
+    l2_window_max_ = wmax > 0 ? static_cast<size_t>(wmax) : 0;
+  }
+  if (l2_persist_ && l2_persist_max_ > 0 && l2_window_max_ > 0 && hot && hot_bytes > 0) {
+    VSGB_CUDA(cudaDeviceGetLimit(&l2_prev_limit_, cudaLimitPersistingL2CacheSize));
+    VSGB_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, l2_persist_max_));
+    const size_t bytes = hot_bytes < l2_window_max_ ? hot_bytes : l2_window_max_;
+    cudaStreamAttrValue v{};
+    v.accessPolicyWindow.base_ptr = const_cast<void*>(hot);
+    v.accessPolicyWindow.num_bytes = bytes;
+    const double ratio = static_cast<double>(l2_persist_max_) / static_cast<double>(bytes);
+    v.accessPolicyWindow.hitRatio = ratio < 1.0 ? static_cast<float>(ratio) : 1.0f;
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    VSGB_CUDA(cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &v));
+    l2_window_set_ = true;
+  }
+  VSGB_CUDA(cudaEventRecord(rev_[0], s));
+}
+
+void PcgEngine::resident_end(cudaStream_t s) {
+  VSGB_CUDA(cudaEventRecord(rev_[1], s));
+  VSGB_CUDA(cudaEventSynchronize(rev_[1]));
+  float ms = 0.f;
+  VSGB_CUDA(cudaEventElapsedTime(&ms, rev_[0], rev_[1]));
+  resident_ms_ += ms;
+  if (l2_window_set_) {
+    cudaStreamAttrValue v{};
+    v.accessPolicyWindow.num_bytes = 0;
+    VSGB_CUDA(cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &v));
+    VSGB_CUDA(cudaCtxResetPersistingL2Cache());
+    VSGB_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, l2_prev_limit_));
+    l2_window_set_ = false;
+  }
+}
+
 void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStream_t s,
                            PcgScalars* host, SolveResult& res) {
   ensure_vectors(false);
+  resident_ms_ = 0.0;
+  resident_iters_ = 0;
   if (resident_used(false)) {
+    resident_begin(s, bsr_.val64.ptr, static_cast<size_t>(bsr_.steps) * 288 * sizeof(double));
     resident_solve64(bsr_, res_, d_f, u_.ptr, scal_.ptr, tol, max_iters, s, op_->dinv.ptr);
+    resident_end(s);
     ++launches_;
     read_scalars(s, host, 0);
+    resident_iters_ += host->iter;
     if (host->flags & kFlagResidentAbort)
       throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
     if (host->flags & kFlagNonPosRz)
@@ -809,6 +877,8 @@ void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStr
 void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int max_iters,
                             int max_solves, cudaStream_t s, PcgScalars* host, SolveResult& res) {
   ensure_vectors(true);
+  resident_ms_ = 0.0;
+  resident_iters_ = 0;
   // Outer record (index 1) holds ||f||, the true residual and the RHS scale.
   k_outer_init<<<vec_grid_, kThreads, 0, s>>>(n_, d_f, r_.ptr, u_.ptr, scal_.ptr + 1,
                                               partials_.ptr, counters_.ptr + 3);
@@ -832,10 +902,13 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
     if (resident_used(true)) {
       // One launch: FP32 inner solve of the scaled correction and the FP64
       // accumulation u += delta / scale.
+      resident_begin(s, bsr_.val32.ptr, static_cast<size_t>(bsr_.steps) * 288 * sizeof(float));
       resident_solve32(bsr_, res_, r_.ptr, u_.ptr, scal_.ptr, scal_.ptr + 1, inner_tol,
                        max_iters, s, op_->dinv.ptr);
+      resident_end(s);
       ++launches_;
       read_scalars(s, host, 0);
+      resident_iters_ += host->iter;
       if (host->flags & kFlagResidentAbort)
         throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
       if (host->flags & kFlagNonPosRz)
@@ -960,6 +1033,8 @@ double PcgEngine::spmv_bytes(int precision) const {
 PcgEngine::~PcgEngine() {
   for (auto& g : graph_exec_)
     if (g) cudaGraphExecDestroy(g);
+  for (auto& e : rev_)
+    if (e) cudaEventDestroy(e);
   destroy_multi(multi_);
 }
 

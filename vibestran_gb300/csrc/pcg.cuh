@@ -28,8 +28,11 @@ class PcgEngine {
   PcgEngine(const PcgEngine&) = delete;
   PcgEngine& operator=(const PcgEngine&) = delete;
 
-  // Binds the operator; builds the FP32 copy when need32.
-  void prepare(const AssembledCsr& op, bool need32, cudaStream_t s);
+  // Binds the operator; builds the FP32 copy when need32.  With prebuilt the
+  // block operator in blocks() was assembled directly and op holds n, dinv
+  // and the nnz counts only (no scalar CSR).
+  void prepare(const AssembledCsr& op, bool need32, cudaStream_t s, bool prebuilt = false);
+  BsrSell& blocks() { return bsr_; }
   bool has32() const { return has32_; }
 
   // FP64 PCG on d_f; the solution is left in solution().
@@ -50,9 +53,15 @@ class PcgEngine {
   int format_used() const { return use_bsr_ ? 2 : 1; }
   // Persistent one-launch-per-solve kernels on the block operator (default on).
   void set_resident(bool r) { resident_ = r; }
+  // Mark the operator values as persisting in L2 around each persistent
+  // launch (CUDA access-policy window, reset after the launch).
+  void set_l2_persist(bool on) { l2_persist_ = on; }
   bool resident_used(bool mixed) const {
     return resident_ && use_bsr_ && (mixed ? res_.ok32 : res_.ok64);
   }
+  // Device time and iterations of the persistent launches of the last solve.
+  double resident_ms() const { return resident_ms_; }
+  long long resident_iterations() const { return resident_iters_; }
   long long launches() const { return launches_; }
   void add_launches(long long k) { launches_ += k; }
   int num_sms() const { return num_sms_; }
@@ -107,6 +116,19 @@ class PcgEngine {
   PcgScalars* graph_host_[2] = {nullptr, nullptr};
 
   MultiWork* multi_ = nullptr;  // batched-solve buffers (multi.cu)
+
+  // Events around each persistent launch; the host syncs after every launch
+  // anyway to read the scalar record.
+  cudaEvent_t rev_[2] = {nullptr, nullptr};
+  double resident_ms_ = 0.0;
+  long long resident_iters_ = 0;
+  void resident_begin(cudaStream_t s, const void* hot, size_t hot_bytes);  // before the launch
+  void resident_end(cudaStream_t s);    // right after it (waits for it)
+  bool l2_persist_ = false;
+  bool l2_window_set_ = false;
+  size_t l2_persist_max_ = 0;   // device limit (0: not supported)
+  size_t l2_window_max_ = 0;
+  size_t l2_prev_limit_ = 0;
 };
 
 }  // namespace vsgb

@@ -137,6 +137,13 @@ __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned*
   return ok;
 }
 
+// Per-slice sum slots between the own-row vectors and the window: one per
+// slice of the largest CTA range (rows_max = 24 * max_slices), padded so the
+// window stays 16/32-byte aligned.
+__host__ __device__ __forceinline__ int slot_count(int rows_max) {
+  return ((rows_max / 24) + 3) & ~3;
+}
+
 __device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double rfma(double a, double b, double c) { return fma(a, b, c); }
 
@@ -193,7 +200,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   T* P = U + a.rows_max;
   T* AP = P + a.rows_max;
   T* D = AP + a.rows_max;
-  T* win = D + a.rows_max;  // 4 per node when kWindow
+  T* SL = D + a.rows_max;   // per-slice p.Ap sums (slices are handed out dynamically)
+  T* win = SL + slot_count(a.rows_max);  // 4 per node when kWindow
   const int wb = a.cta_win[2 * c], we = a.cta_win[2 * c + 1];
   unsigned target = 0;
   int slot = 0;
@@ -331,6 +339,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       }
       const int r = lane >> 2, q = lane & 3;
       const int R = 8 * sl + r;
+      T part = T(0);
       if (q < 3 && R < a.nb) {
         const int lr = 24 * ls + 3 * r + q;
         const T yq = q == 0 ? y0 : (q == 1 ? y1 : y2);
@@ -338,11 +347,23 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         P[lr] = pn;
         AP[lr] = yq;
         p_new[4 * R + q] = pn;
-        accp[0] = rfma(pn, yq, accp[0]);
+        part = pn * yq;
       }
+      part = warp_sum(part);
       int nxt = 0;
-      if (lane == 0) nxt = atomicAdd(&s_next, 1);
+      if (lane == 0) {
+        SL[ls] = part;
+        nxt = atomicAdd(&s_next, 1);
+      }
       ls = __shfl_sync(0xffffffffu, nxt, 0);
+    }
+    // p.Ap of the CTA in slice order, whichever warp computed each slice.
+    __syncthreads();
+    if (warp == 0) {
+      T s = T(0);
+      for (int k = lane; k < ns; k += 32) s += SL[k];
+      s = warp_sum(s);
+      if (lane == 0) accp[0] = s;
     }
     double totp[1];
     ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok, totp);
@@ -592,7 +613,7 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
   auto fit = [&](size_t bytes) { return bytes <= static_cast<size_t>(smem_optin); };
   // FP64
   {
-    const size_t own = 6 * rows * sizeof(double);
+    const size_t own = (6 * rows + slot_count(static_cast<int>(rows))) * sizeof(double);
     const size_t w = 4 * static_cast<size_t>(max_win) * sizeof(double);
     int blocks = 0;
     if (fit(own + w) && configure<double, true, false>(own + w, &blocks)) {
@@ -614,7 +635,7 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
     }
   }
   if (need32 && B.has32) {
-    const size_t own = 6 * rows * sizeof(float);
+    const size_t own = (6 * rows + slot_count(static_cast<int>(rows))) * sizeof(float);
     const size_t w = 4 * static_cast<size_t>(max_win) * sizeof(float);
     int blocks = 0;
     if (fit(own + w) && configure<float, true, true>(own + w, &blocks)) {
