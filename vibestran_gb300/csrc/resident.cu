@@ -62,29 +62,45 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   return v;
 }
 
+// Cost of a slice beyond its steps, in steps, when slice ranges are split
+// across CTAs: starting a slice costs dependent loads (its extent, then its
+// first blocks) and ending it a reduction, so CTAs at the mesh ends, whose
+// rows have fewer blocks and whose slices are therefore more numerous, ran
+// slower with a weight of 1.  Measured per iteration on GB300 (FP32 / FP64,
+// 265k and 504k equations): weight 1: 25.5 / 75.5 and 50.3 / 156 us;
+// 3: 24.1 / 72.5 and 46.8 / 146 us; 5: 23.8 / 72.9 and 46.4 / 144 us.
+constexpr int kSliceWeight = 4;
+
+__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Grid barrier over a monotonic counter; false when it gave up (the abort flag
-// is then set for every CTA).
+// is then set for every CTA).  Arrival is a release reduction by thread 0
+// after the CTA barrier (it orders every write the CTA made before it), the
+// wait an acquire load; the CTA barrier after the wait hands the acquired
+// writes to the other threads.  The abort flag is polled every 64 spins and
+// the loop backs off only after the first 4096.
 __device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, int* s_ok) {
   target += gridDim.x;
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(count, 1u);
+    red_release_add_u32(count, 1u);
     int ok = 1;
     long long spins = 0;
     while (ld_acquire_u32(count) < target) {
-      if (*reinterpret_cast<volatile int*>(abort_flag)) {
+      ++spins;
+      if ((spins & 63) == 0 && *reinterpret_cast<volatile int*>(abort_flag)) {
         ok = 0;
         break;
       }
-      if (++spins > kSpinLimit) {
+      if (spins > kSpinLimit) {
         atomicExch(abort_flag, 1);
         ok = 0;
         break;
       }
-      __nanosleep(32);
+      if (spins > 4096) __nanosleep(64);
     }
-    __threadfence();
     *s_ok = ok;
   }
   __syncthreads();
@@ -118,12 +134,26 @@ __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned*
   }
   const bool ok = grid_sync(count, target, abort_flag, s_ok);
   if (threadIdx.x < 32) {
+    // Lane l adds the partials of CTAs l, l+32, ... in that order; the loads
+    // of a round are all issued before the first add (one L2 round trip per
+    // round of 8 instead of one per CTA).
+    constexpr int kRound = 8;
     double acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = 0.0;
-    for (unsigned c = threadIdx.x; c < gridDim.x; c += 32)
+    for (unsigned c0 = threadIdx.x; c0 < gridDim.x; c0 += 32 * kRound) {
+      double v[kRound][NV];
 #pragma unroll
-      for (int k = 0; k < NV; ++k) acc[k] += __ldcg(&part[c * NV + k]);
+      for (int u = 0; u < kRound; ++u) {
+        const unsigned c = c0 + 32u * u;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[u][k] = c < gridDim.x ? __ldcg(&part[c * NV + k]) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kRound; ++u)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += v[u][k];
+    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = warp_sum(acc[k]);
     if (threadIdx.x == 0)
@@ -560,7 +590,7 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
       const int R = 8 * sl + r;
       if (R < nb) mx = std::max(mx, B.h_blen[R]);
     }
-    pre[sl + 1] = pre[sl] + (mx + 3) / 4 + 1;  // +1: per-slice epilogue cost
+    pre[sl + 1] = pre[sl] + (mx + 3) / 4 + kSliceWeight;
   }
   const int G = num_sms;
   std::vector<int> cs(static_cast<size_t>(G) + 1, 0);
