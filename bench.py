@@ -36,6 +36,7 @@ FP64_TOL = 1e-4          # sqrt(r.r)/||F|| of the FP64 PCG recursion
 MIXED_TOL = 1e-4         # true FP64 residual after refinement
 MIXED_INNER_TOL = 1e-3   # FP32 inner solves (the FP32 operator limits each to ~2e-3)
 MIXED_MAX_SOLVES = 4
+JITTER_MIXED_TOL = 2e-5  # jittered heterogeneous mesh: <= 1e-6 error needs a tighter residual
 # FP64 FMA rate of a GB300 measured with an FMA-chain kernel (1.91 DFMA/clk/SM
 # at 2.07 GHz): the compute floor of the FP64 SpMV.
 FP64_TFLOPS = 1.20
@@ -230,13 +231,15 @@ def extra_adjoint(B, C, device, n_fd=4):
 
 def extra_jitter(B, C, device, uniform):
     """Jittered (U(+-0.2 h) interior nodes) heterogeneous (log-uniform E)
-    84 000-element cantilever: FP64 and mixed iteration counts at the headline
-    tolerances against the uniform mesh's, and the error against the FP64
-    sparse-direct fingerprint."""
+    84 000-element cantilever: FP64 and mixed iteration counts against the
+    uniform mesh's, and the error against the FP64 sparse-direct fingerprint.
+    FP64 runs at the headline tolerance; the mixed true-residual tolerance is
+    JITTER_MIXED_TOL, which keeps the error <= 1e-6 on this worse-conditioned
+    mesh (the headline 1e-4 gives ~1.4e-6 here)."""
     m = C.cantilever_84k_jitter()
     eq6, n = B.build_dof_map(m)
     F = B.apply_forces(m, eq6, n)
-    be = _mixed_backend(B, device)
+    be = _mixed_backend(B, device, tol=JITTER_MIXED_TOL)
     asm = B.ChexaAssembler(be)
     asm.assemble(m, eq6, n)
     asm.upload_rhs(F)
@@ -251,7 +254,8 @@ def extra_jitter(B, C, device, uniform):
     be.close()
     out = {"workload": "cantilever_84k_jitter", "dofs": n, "seed": m.seed,
            "fp64": {"iterations": st_d.iterations, "solve_s": st_d.solve_ms / 1e3},
-           "mixed": {"iterations_fp32": st_m.iterations, "inner_solves": st_m.inner_solves,
+           "mixed": {"tolerance": JITTER_MIXED_TOL,
+                     "iterations_fp32": st_m.iterations, "inner_solves": st_m.inner_solves,
                      "solve_s": st_m.solve_ms / 1e3},
            "iteration_growth_vs_uniform": {
                "fp64": st_d.iterations / uniform["fp64"],

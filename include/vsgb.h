@@ -61,6 +61,11 @@ extern "C" {
                                      loop; 1 (default) one batched PCG from 4 cases
                                      (mixed) or 10 cases (FP64) up, where it is faster;
                                      2 always batched */
+#define VSGB_OPT_ADAPTIVE_INNER 12 /* mixed: 1 (default) lets a refinement step's inner
+                                     solve stop at 0.5*tol/(current true residual) when
+                                     that is looser than the inner tolerance; 0: every
+                                     inner solve runs to the inner tolerance, as
+                                     cuda-pcg-mixed */
 #define VSGB_OPT_L2_PERSIST 11    /* 1: mark the operator values persisting in L2 during
                                      each persistent PCG launch (default 0: measured no
                                      gain, the solve is not bound by L2 misses) */

@@ -55,6 +55,7 @@ OPT_FORMAT = 8
 OPT_RESIDENT = 9
 OPT_BATCHED = 10
 OPT_L2_PERSIST = 11
+OPT_ADAPTIVE_INNER = 12
 
 # The symbols include/vsgb.h declares (checked by tests against the .so).
 EXPORTS = (

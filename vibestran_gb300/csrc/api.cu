@@ -366,6 +366,9 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
       case VSGB_OPT_L2_PERSIST:
         c->eng->set_l2_persist(value != 0.0);
         break;
+      case VSGB_OPT_ADAPTIVE_INNER:
+        c->eng->set_adaptive_inner(value != 0.0);
+        break;
       case VSGB_OPT_BATCHED: {
         const int b = static_cast<int>(value);
         if (b < 0 || b > 2) throw Error(VSGB_ERR_INVALID, "batched mode must be 0, 1 or 2");

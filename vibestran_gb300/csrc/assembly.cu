@@ -187,6 +187,7 @@ struct PatSmem {
   int key[kMaxCand];
   int first[kMaxCand];
   int nbr[kMaxNbr];
+  int nkey[kMaxNbr];  // first free equation of nbr[r] (ascending)
 };
 
 __device__ __forceinline__ int first_free_eq(const int* eq3, int b) {
@@ -244,7 +245,10 @@ __device__ int gather_neighbors(int a, int pb, int L, const int* __restrict__ co
       const int k = s.key[c];
       int r = 0;
       for (int m = 0; m < C; ++m) r += (s.first[m] && s.key[m] < k);
-      if (r < kMaxNbr) s.nbr[r] = s.cand[c];
+      if (r < kMaxNbr) {
+        s.nbr[r] = s.cand[c];
+        s.nkey[r] = k;
+      }
     }
   }
   for (int c = lane; c < C; c += 32) U += s.first[c];
@@ -418,14 +422,13 @@ __global__ void k_node_aligned(int n_nodes, const int* __restrict__ eq3, int* __
   if (!(e0 >= 0 && e0 % 3 == 0 && e1 == e0 + 1 && e2 == e0 + 2)) atomicOr(flag, 1);
 }
 
-template <bool kFill>
+// Block-row lengths: the structural neighbour count of every free node (a
+// block is stored for every neighbour; entries that received no value != 0.0
+// are zeros in the block and are not counted as scalar nonzeros).
 __global__ void __launch_bounds__(kPatWarps * 32)
-k_block_pattern(int n_nodes, int nb, const int* __restrict__ conn, const int* __restrict__ eq3,
-                const int* __restrict__ node_ptr, const int* __restrict__ node_elem,
-                const double* __restrict__ kbuf, int* __restrict__ blen,
-                unsigned long long* __restrict__ counts, const int* __restrict__ slice_ptr,
-                int* __restrict__ cols, double* __restrict__ v64, float* __restrict__ v32,
-                double* __restrict__ dinv, AssemblyError* err) {
+k_block_count(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3,
+              const int* __restrict__ node_ptr, const int* __restrict__ node_elem,
+              int* __restrict__ blen, AssemblyError* err) {
   __shared__ PatSmem smem_all[kPatWarps];
   PatSmem& s = smem_all[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
@@ -433,99 +436,153 @@ k_block_pattern(int n_nodes, int nb, const int* __restrict__ conn, const int* __
   for (int a = blockIdx.x * kPatWarps + (threadIdx.x >> 5); a < n_nodes; a += warps_total) {
     const int r0 = eq3[3 * a];
     if (r0 < 0) continue;  // aligned: all three constrained
-    const int R = r0 / 3;
     const int pb = node_ptr[a], L = node_ptr[a + 1] - pb;
     const int U = gather_neighbors(a, pb, L, conn, eq3, node_elem, s, err);
+    if (U >= 0 && lane == 0) blen[r0 / 3] = U;
+    __syncwarp();
+  }
+}
+
+constexpr int kFillWarps = 2;
+
+struct FillSmem {
+  PatSmem p;
+  double acc[kMaxNbr][9];            // block sums per neighbour slot
+  unsigned char nz[kMaxNbr][9];      // entry received a value != 0.0
+  short slot[kMaxCand];              // neighbour slot of candidate c (-1: constrained)
+};
+
+// Block row of node a: for each incident element (ascending, the reference's
+// summation order), its three rows of K_e (576 contiguous bytes, one
+// coalesced read) are added into the neighbour blocks in shared memory, then
+// the row is written to the sliced-ELL operator with its padding, the inverse
+// diagonal and the scalar nonzero counts (full and lower triangle).
+__global__ void __launch_bounds__(kFillWarps * 32)
+k_block_fill(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3,
+             const int* __restrict__ node_ptr, const int* __restrict__ node_elem,
+             const double* __restrict__ kbuf, unsigned long long* __restrict__ counts,
+             const int* __restrict__ slice_ptr, int* __restrict__ cols,
+             double* __restrict__ v64, float* __restrict__ v32, double* __restrict__ dinv,
+             AssemblyError* err) {
+  __shared__ FillSmem smem_all[kFillWarps];
+  FillSmem& s = smem_all[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * kFillWarps;
+  for (int a = blockIdx.x * kFillWarps + (threadIdx.x >> 5); a < n_nodes; a += warps_total) {
+    const int r0 = eq3[3 * a];
+    if (r0 < 0) continue;
+    const int R = r0 / 3;
+    const int pb = node_ptr[a], L = node_ptr[a + 1] - pb;
+    const int U = gather_neighbors(a, pb, L, conn, eq3, node_elem, s.p, err);
     if (U < 0) continue;
+    const int C = 8 * L;
+    for (int c = lane; c < C; c += 32) {
+      const int key = s.p.key[c];
+      int slot = -1;
+      if (key != INT_MAX) {
+        int lo = 0, hi = U - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (s.p.nkey[mid] < key) lo = mid + 1; else hi = mid;
+        }
+        slot = lo;
+      }
+      s.slot[c] = static_cast<short>(slot);
+    }
+    for (int t = lane; t < 9 * U; t += 32) {
+      (&s.acc[0][0])[t] = 0.0;
+      (&s.nz[0][0])[t] = 0;
+    }
+    __syncwarp();
+    // Incident elements in one load (L <= 32), then their rows of K_e four
+    // elements at a time: 12 loads per lane in flight before any is added,
+    // the adds in ascending element order.
+    const int ek_lane = lane < L ? node_elem[pb + lane] : 0;
+    for (int k0 = 0; k0 < L; k0 += 4) {
+      double v[4][3];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int ek = __shfl_sync(0xffffffffu, ek_lane, (k0 + j) & 31);
+        const double* rows = kbuf + static_cast<size_t>(ek >> 3) * 576 + 3 * (ek & 7) * 24;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          const int idx = lane + 32 * r;
+          v[j][r] = (k0 + j < L && idx < 72) ? __ldg(rows + idx) : 0.0;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int k = k0 + j;
+        if (k < L) {
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            const int idx = lane + 32 * r;
+            if (idx < 72) {
+              const int d = idx / 24, col = idx - 24 * d, m = col / 3, q = col - 3 * m;
+              const int slot = s.slot[8 * k + m];
+              if (slot >= 0) {
+                s.acc[slot][3 * d + q] += v[j][r];
+                if (v[j][r] != 0.0) s.nz[slot][3 * d + q] = 1;
+              }
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
     const int sl = R >> 3, ln0 = (R & 7) * 4;
-    const long long sp = kFill ? slice_ptr[sl] : 0;
-    int carry = 0;
+    const long long sp = slice_ptr[sl];
     unsigned long long full = 0, lower = 0;
-    bool diag_seen[3] = {false, false, false};
-    for (int u0 = 0; u0 < U; u0 += 32) {
-      const int u = u0 + lane;
-      const bool act = u < U;
-      const int b = act ? s.nbr[u] : a;
-      double sum[3][3];
-      bool nz[3][3];
-      node_block(b, pb, L, conn, node_elem, kbuf, sum, nz);
-      bool any = false;
+    for (int u = lane; u < U; u += 32) {
+      const int b = s.p.nbr[u], Cb = s.p.nkey[u] / 3;
+      const long long st = sp + (u >> 2);
+      const int ln = ln0 + (u & 3);
+      cols[st * 32 + ln] = Cb;
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int q = 0; q < 3; ++q) any = any || nz[d][q];
-      any = any && act;
-      const int C = eq3[3 * b] / 3;
-      const unsigned m = __ballot_sync(0xffffffffu, any);
-      if (!kFill) {
-        if (any) {
-#pragma unroll
-          for (int d = 0; d < 3; ++d)
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              full += nz[d][q];
-              lower += nz[d][q] && (3 * C + q <= 3 * R + d);
-            }
+        for (int q = 0; q < 3; ++q) {
+          const double v = s.acc[u][3 * d + q];
+          const size_t o = static_cast<size_t>((st * 9 + 3 * d + q) * 32 + ln);
+          v64[o] = v;
+          if (v32) v32[o] = static_cast<float>(v);
+          const bool z = s.nz[u][3 * d + q] != 0;
+          full += z;
+          lower += z && (3 * Cb + q <= 3 * R + d);
         }
-      } else if (any) {
-        const int j = carry + __popc(m & ((1u << lane) - 1u));
-        const long long st = sp + (j >> 2);
-        const int ln = ln0 + (j & 3);
-        cols[st * 32 + ln] = C;
+      if (b == a) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d)
-#pragma unroll
-          for (int q = 0; q < 3; ++q) {
-            const size_t o = static_cast<size_t>((st * 9 + 3 * d + q) * 32 + ln);
-            if (v64) v64[o] = sum[d][q];
-            if (v32) v32[o] = static_cast<float>(sum[d][q]);
-          }
-        if (b == a) {
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            if (nz[d][d]) {
-              diag_seen[d] = true;
-              if (sum[d][d] == 0.0)
-                set_error(err, 4, 3 * R + d);
-              else
-                dinv[3 * R + d] = 1.0 / sum[d][d];
-            }
-          }
+        for (int d = 0; d < 3; ++d) {
+          if (!s.nz[u][4 * d])
+            set_error(err, 5, 3 * R + d);
+          else if (s.acc[u][4 * d] == 0.0)
+            set_error(err, 4, 3 * R + d);
+          else
+            dinv[3 * R + d] = 1.0 / s.acc[u][4 * d];
         }
       }
-      carry += __popc(m);
     }
-    if (!kFill) {
+    // padding slots: a valid block column (the slice's first row), zeros
+    const int slots = 4 * (slice_ptr[sl + 1] - slice_ptr[sl]);
+    for (int j = U + lane; j < slots; j += 32) {
+      const long long st = sp + (j >> 2);
+      const int ln = ln0 + (j & 3);
+      cols[st * 32 + ln] = 8 * sl;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        full += __shfl_xor_sync(0xffffffffu, full, o);
-        lower += __shfl_xor_sync(0xffffffffu, lower, o);
+      for (int k = 0; k < 9; ++k) {
+        const size_t o = static_cast<size_t>((st * 9 + k) * 32 + ln);
+        v64[o] = 0.0;
+        if (v32) v32[o] = 0.f;
       }
-      if (lane == 0) {
-        blen[R] = carry;
-        atomicAdd(&counts[0], full);
-        atomicAdd(&counts[1], lower);
-      }
-    } else {
-      // padding slots of this block row: a valid block column (the slice's
-      // first row) and zero values
-      const int slots = 4 * (slice_ptr[sl + 1] - slice_ptr[sl]);
-      for (int j = carry + lane; j < slots; j += 32) {
-        const long long st = sp + (j >> 2);
-        const int ln = ln0 + (j & 3);
-        cols[st * 32 + ln] = 8 * sl;
+    }
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-          const size_t o = static_cast<size_t>((st * 9 + k) * 32 + ln);
-          if (v64) v64[o] = 0.0;
-          if (v32) v32[o] = 0.f;
-        }
-      }
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const bool seen = __any_sync(0xffffffffu, diag_seen[d]);
-        if (lane == 0 && !seen) set_error(err, 5, 3 * R + d);
-      }
+    for (int o = 16; o > 0; o >>= 1) {
+      full += __shfl_xor_sync(0xffffffffu, full, o);
+      lower += __shfl_xor_sync(0xffffffffu, lower, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&counts[0], full);
+      atomicAdd(&counts[1], lower);
     }
     __syncwarp();
   }
@@ -804,24 +861,18 @@ bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, i
   scr.counts.reserve(2);
   VSGB_CUDA(cudaMemsetAsync(scr.counts.ptr, 0, sizeof(unsigned long long) * 2, s));
   const int pgrid = grid_for(static_cast<long long>(n_nodes) * 32, kPatWarps * 32, num_sms * 16);
-  k_block_pattern<false><<<pgrid, kPatWarps * 32, 0, s>>>(
-      n_nodes, nb, conn, eq3, scr.node_ptr.ptr, scr.node_elem.ptr, kbuf, B.rowlen.ptr,
-      scr.counts.ptr, nullptr, nullptr, nullptr, nullptr, nullptr, scr.err.ptr);
+  k_block_count<<<pgrid, kPatWarps * 32, 0, s>>>(n_nodes, conn, eq3, scr.node_ptr.ptr,
+                                                 scr.node_elem.ptr, B.rowlen.ptr, scr.err.ptr);
   VSGB_LAUNCH_CHECK();
-  unsigned long long cnt[2] = {0, 0};
-  VSGB_CUDA(cudaMemcpyAsync(cnt, scr.counts.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
   const long long total_steps = bsr_layout(B, nb, s);  // synchronises
-  // stored blocks (the scan of the row lengths)
+  // stored blocks (the sum of the row lengths)
   B.h_blen.resize(static_cast<size_t>(nb));
   VSGB_CUDA(cudaMemcpyAsync(B.h_blen.data(), B.rowlen.ptr, sizeof(int) * nb,
                             cudaMemcpyDeviceToHost, s));
   VSGB_CUDA(cudaStreamSynchronize(s));
   long long blocks = 0;
   for (int R = 0; R < nb; ++R) blocks += B.h_blen[R];
-  if (cnt[0] >= static_cast<unsigned long long>(INT_MAX))
-    throw Error(VSGB_ERR_LIMIT, "assembled nnz exceeds the int32 CSR limit");
-  if (blocks == 0 || static_cast<double>(cnt[0]) < 0.9 * 9.0 * static_cast<double>(blocks))
-    return false;
+  if (blocks == 0) return false;
 
   const size_t nstep = static_cast<size_t>(total_steps > 0 ? total_steps : 1);
   B.cols.reserve(nstep * 32);
@@ -844,11 +895,19 @@ bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, i
   }
   out.n = n_dof;
   out.dinv.reserve(static_cast<size_t>(n_dof));
-  k_block_pattern<true><<<pgrid, kPatWarps * 32, 0, s>>>(
-      n_nodes, nb, conn, eq3, scr.node_ptr.ptr, scr.node_elem.ptr, kbuf, nullptr, nullptr,
+  const int fgrid = grid_for(static_cast<long long>(n_nodes) * 32, kFillWarps * 32, num_sms * 32);
+  k_block_fill<<<fgrid, kFillWarps * 32, 0, s>>>(
+      n_nodes, conn, eq3, scr.node_ptr.ptr, scr.node_elem.ptr, kbuf, scr.counts.ptr,
       B.slice_ptr.ptr, B.cols.ptr, B.val64.ptr, need32 ? B.val32.ptr : nullptr, out.dinv.ptr,
       scr.err.ptr);
   VSGB_LAUNCH_CHECK();
+  unsigned long long cnt[2] = {0, 0};
+  VSGB_CUDA(cudaMemcpyAsync(cnt, scr.counts.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  if (cnt[0] >= static_cast<unsigned long long>(INT_MAX))
+    throw Error(VSGB_ERR_LIMIT, "assembled nnz exceeds the int32 CSR limit");
+  // blocks much emptier than 3x3 (< 90% of the entries nonzero): scalar CSR
+  if (static_cast<double>(cnt[0]) < 0.9 * 9.0 * static_cast<double>(blocks)) return false;
   out.nnz = static_cast<long long>(cnt[0]);
   out.nnz_lower = static_cast<long long>(cnt[1]);
   B.nblocks = blocks;

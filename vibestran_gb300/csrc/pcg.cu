@@ -20,6 +20,7 @@
 // Roofline: HBM (12 B/nnz FP64, 8 B/nnz FP32 + vectors) and, on GB300, the
 // FP64 FMA rate for the FP64 path.
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -895,15 +896,22 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
     res.rel = 0.0;
     return;
   }
-  set_limits(s, 0, inner_tol, max_iters);
   double prev = 0.0;
   bool have_prev = false;
   for (int step = 0; step < max_solves; ++step) {
+    // Inexact refinement: the correction only has to bring the true residual
+    // (outer.rel, relative to ||f||) below tol, so its inner solve may stop
+    // at 0.5 * tol / outer.rel instead of inner_tol when that is looser.
+    double itol = inner_tol;
+    if (adaptive_inner_ && outer.rel > 0.0) {
+      const double want = 0.5 * tol / outer.rel;
+      itol = std::max(inner_tol, std::min(0.5, want));
+    }
     if (resident_used(true)) {
       // One launch: FP32 inner solve of the scaled correction and the FP64
       // accumulation u += delta / scale.
       resident_begin(s, bsr_.val32.ptr, static_cast<size_t>(bsr_.steps) * 288 * sizeof(float));
-      resident_solve32(bsr_, res_, r_.ptr, u_.ptr, scal_.ptr, scal_.ptr + 1, inner_tol,
+      resident_solve32(bsr_, res_, r_.ptr, u_.ptr, scal_.ptr, scal_.ptr + 1, itol,
                        max_iters, s, op_->dinv.ptr);
       resident_end(s);
       ++launches_;
@@ -940,6 +948,7 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       have_prev = true;
       continue;
     }
+    set_limits(s, 0, itol, max_iters);
     k_init32<<<vec_grid_, kThreads, 0, s>>>(n_, r_.ptr, 0.0, dinv32_.ptr, r32_.ptr, u32_.ptr,
                                             z32_.ptr, p32a_.ptr, scal_.ptr, scal_.ptr + 1,
                                             partials_.ptr, counters_.ptr);

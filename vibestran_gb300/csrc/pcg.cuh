@@ -56,6 +56,9 @@ class PcgEngine {
   // Mark the operator values as persisting in L2 around each persistent
   // launch (CUDA access-policy window, reset after the launch).
   void set_l2_persist(bool on) { l2_persist_ = on; }
+  // Mixed refinement: loosen later inner tolerances to what the outer
+  // tolerance still needs (never tighter than the inner tolerance).
+  void set_adaptive_inner(bool on) { adaptive_inner_ = on; }
   bool resident_used(bool mixed) const {
     return resident_ && use_bsr_ && (mixed ? res_.ok32 : res_.ok64);
   }
@@ -125,6 +128,7 @@ class PcgEngine {
   void resident_begin(cudaStream_t s, const void* hot, size_t hot_bytes);  // before the launch
   void resident_end(cudaStream_t s);    // right after it (waits for it)
   bool l2_persist_ = false;
+  bool adaptive_inner_ = true;
   bool l2_window_set_ = false;
   size_t l2_persist_max_ = 0;   // device limit (0: not supported)
   size_t l2_window_max_ = 0;
