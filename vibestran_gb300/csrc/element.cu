@@ -12,11 +12,13 @@
 // reference's row-of-inverse form, solid_elements.cpp:1131-1133, :1109).
 // Accumulating the 66 M_AB (594 FP64 values) replaces the 24x24 / 24x9 / 9x9
 // B^T D B products, then Ke = Kuu - Kua Kaa^-1 Kau is condensed with a 9x9
-// Cholesky (Eigen::LLT at :1201-1204).  Ke is written exactly symmetric
-// (entry (c,r) is a copy of (r,c)).
+// Cholesky (Eigen::LLT at :1201-1204), as Kuu - Y^T Y with Y = L^-1 Kau.
+// Ke is written exactly symmetric (entry (c,r) is a copy of (r,c)).
 //
-// Roofline: FP64-compute bound (~10k DFMA per EAS element); inputs 8 node
-// coordinates + E, nu (≈ 220 B), output 576 doubles (4.6 kB) per element.
+// Roofline: FP64-pipe bound (ncu: FP64 pipe ~90% busy; GB300 issues one FP64
+// warp instruction per ~17 cycles per SM whatever its active lanes, so the
+// work is spread over the warp wherever it can be).  Inputs 8 node
+// coordinates + E, nu (~220 B), output 576 doubles (4.6 kB) per element.
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -30,9 +32,6 @@ constexpr int kVN = 11;        // virtual nodes: 8 element nodes + 3 enhancement
 constexpr int kPairs = 66;     // A <= B over 11 virtual nodes
 constexpr int kPairsSri = 36;  // A <= B over the 8 element nodes
 
-__constant__ signed char c_xn[8] = {-1, +1, +1, -1, -1, +1, +1, -1};
-__constant__ signed char c_en[8] = {-1, -1, +1, +1, -1, -1, +1, +1};
-__constant__ signed char c_zn[8] = {-1, -1, -1, -1, +1, +1, +1, +1};
 
 struct WarpSmem {
   double g[9][kVN][3];    // gradients at the 8 Gauss points + centroid (index 8)
@@ -41,7 +40,7 @@ struct WarpSmem {
   double L[9][9];         // Cholesky factor of Kaa
   double Linv[9];         // 1 / L[i][i]
   double Kua[24][9];
-  double X[9][24];        // Kaa^-1 Kau
+  double X[9][24];        // L^-1 Kau (Kaa = L L^T)
   double j0[12];          // J0^-1 (9), detJ0
 };
 // Ke staging aliases g/wg (dead after the moment accumulation): 594 >= 576.
@@ -121,85 +120,105 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
 #pragma unroll
       for (int c = 0; c < 3; ++c) X[n][c] = __ldg(&xyz[3 * nd + c]);
     }
-    int bad = 0;
-    double detJ = 1.0;
-    double Ji[3][3];
-    double dN[3][8];
+    // Three lanes per point (lane = 3*gp + r; gp 8 = centroid, lanes 27-31
+    // mirror it and store nothing): lane r forms row r of dN/dxi and of J,
+    // gets the other rows from its two partner lanes by shuffles, and forms
+    // component r of every gradient.  Every lane runs the same FP64
+    // instructions (row / axis choices are operand selects, not branches),
+    // each value with the operation order of the one-lane-per-point form.
+    const bool act = lane < 27;
+    const int gp = act ? lane / 3 : 8, rr = act ? lane - 3 * (lane / 3) : lane - 27 < 3 ? lane - 27 : 0;
+    const int l0 = 3 * gp;  // lane holding row 0 of this point
     double par[3] = {0.0, 0.0, 0.0};
-    if (lane < 9) {
-      if (lane < 8) {
-        // Gauss point order of the reference loops: xi slowest, zeta fastest.
-        par[0] = (lane & 4) ? gpt : -gpt;
-        par[1] = (lane & 2) ? gpt : -gpt;
-        par[2] = (lane & 1) ? gpt : -gpt;
-      }
+    if (gp < 8) {
+      // Gauss point order of the reference loops: xi slowest, zeta fastest.
+      par[0] = (gp & 4) ? gpt : -gpt;
+      par[1] = (gp & 2) ? gpt : -gpt;
+      par[2] = (gp & 1) ? gpt : -gpt;
+    }
+    // dN_n/dxi_r = (0.125 s_r(n)) (1 + s_a(n) xi_a) (1 + s_b(n) xi_b), (a, b)
+    // the other two axes in increasing order.  Node signs s_k(n) of the CHEXA8
+    // node order (src/elements/solid_elements.cpp:76-93) as bit masks, bit n
+    // set for +1: xi {-,+,+,-,-,+,+,-}, eta {-,-,+,+,-,-,+,+}, zeta {-,-,-,-,+,+,+,+}.
+    constexpr unsigned kPos[3] = {0x66u, 0xCCu, 0xF0u};
+    const int ax1 = rr == 0 ? 1 : 0, ax2 = rr == 2 ? 1 : 2;
+    const unsigned m0 = kPos[0], m1 = kPos[1], m2 = kPos[2];
+    const unsigned ms = rr == 0 ? m0 : (rr == 1 ? m1 : m2);
+    const unsigned ma = ax1 == 0 ? m0 : m1;
+    const unsigned mb = ax2 == 1 ? m1 : m2;
+    const double pa = ax1 == 0 ? par[0] : par[1];
+    const double pb = ax2 == 1 ? par[1] : par[2];
+    double dNr[8];
 #pragma unroll
-      for (int n = 0; n < 8; ++n) {
-        const double xn = c_xn[n], en = c_en[n], zn = c_zn[n];
-        const double a = 1 + xn * par[0], b = 1 + en * par[1], c = 1 + zn * par[2];
-        dN[0][n] = 0.125 * xn * b * c;
-        dN[1][n] = 0.125 * en * a * c;
-        dN[2][n] = 0.125 * zn * a * b;
-      }
-      double J[3][3];
+    for (int n = 0; n < 8; ++n) {
+      const double fa = fma(((ma >> n) & 1u) ? 1.0 : -1.0, pa, 1.0);
+      const double fb = fma(((mb >> n) & 1u) ? 1.0 : -1.0, pb, 1.0);
+      dNr[n] = (((ms >> n) & 1u) ? 0.125 : -0.125) * fa * fb;
+    }
+    double Jr[3];
 #pragma unroll
-      for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      double acc = 0.0;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          double acc = 0.0;
+      for (int n = 0; n < 8; ++n) acc = fma(dNr[n], X[n][c], acc);
+      Jr[c] = acc;
+    }
+    double J[3][3];
 #pragma unroll
-          for (int n = 0; n < 8; ++n) acc = fma(dN[r][n], X[n][c], acc);
-          J[r][c] = acc;
-        }
-      const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-      const double c01 = J[0][2] * J[2][1] - J[0][1] * J[2][2];
-      const double c02 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
-      detJ = J[0][0] * c00 + J[1][0] * c01 + J[2][0] * c02;
-      if (!(detJ > 0.0)) bad = 1;
-      const double id = 1.0 / detJ;
-      Ji[0][0] = c00 * id;
-      Ji[0][1] = c01 * id;
-      Ji[0][2] = c02 * id;
-      Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
-      Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-      Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-      Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * id;
-      Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-      Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-      if (lane == 8) {
+    for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) J[k][c] = __shfl_sync(0xffffffffu, Jr[c], l0 + k);
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const double c01 = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    const double c02 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    const double detJ = J[0][0] * c00 + J[1][0] * c01 + J[2][0] * c02;
+    const int bad = act && !(detJ > 0.0);
+    const double id = 1.0 / detJ;
+    // row rr of J^-1: (J[c+1][rr+1] J[c+2][rr+2] - J[c+1][rr+2] J[c+2][rr+1]) / det
+    const int q1 = rr == 2 ? 0 : rr + 1, q2 = rr == 0 ? 2 : rr - 1;
+    double Jir[3];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) s.j0[3 * r + c] = Ji[r][c];
-        s.j0[9] = detJ;
-      }
+    for (int c = 0; c < 3; ++c) {
+      const int i1 = (c + 1) % 3, i2 = (c + 2) % 3;
+      const double a1 = q1 == 0 ? J[i1][0] : (q1 == 1 ? J[i1][1] : J[i1][2]);
+      const double b2 = q2 == 0 ? J[i2][0] : (q2 == 1 ? J[i2][1] : J[i2][2]);
+      const double a2 = q2 == 0 ? J[i1][0] : (q2 == 1 ? J[i1][1] : J[i1][2]);
+      const double b1 = q1 == 0 ? J[i2][0] : (q1 == 1 ? J[i2][1] : J[i2][2]);
+      Jir[c] = (a1 * b2 - a2 * b1) * id;
+    }
+    if (gp == 8 && act) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) s.j0[3 * rr + c] = Jir[c];
+      if (rr == 0) s.j0[9] = detJ;
     }
     if (__any_sync(0xffffffffu, bad)) {
       if (lane == 0) record_element_error(err, e, 1);
       continue;
     }
+    // dN rows of the partner lanes
+    double dN[3][8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int n = 0; n < 8; ++n) dN[k][n] = __shfl_sync(0xffffffffu, dNr[n], l0 + k);
     __syncwarp();
-    if (lane < 9) {
-      const double w = (lane == 8) ? 8.0 * detJ : detJ;
+    const double w = (gp == 8) ? 8.0 * detJ : detJ;
+    if (act) {
 #pragma unroll
-      for (int n = 0; n < 8; ++n)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const double gv = Ji[c][0] * dN[0][n] + Ji[c][1] * dN[1][n] + Ji[c][2] * dN[2][n];
-          s.g[lane][n][c] = gv;
-          s.wg[lane][n][c] = w * gv;
-        }
-      if (lane < 8) {
+      for (int n = 0; n < 8; ++n) {
+        const double gv = Jir[0] * dN[0][n] + Jir[1] * dN[1][n] + Jir[2] * dN[2][n];
+        s.g[gp][n][rr] = gv;
+        s.wg[gp][n][rr] = w * gv;
+      }
+      if (gp < 8) {
         // Enhancement gradients: J0^-1.row(p) * xi_p * detJ0/detJ.
         const double scale = s.j0[9] / detJ;
 #pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const double hv = s.j0[3 * p + c] * par[p] * scale;
-            s.g[lane][8 + p][c] = hv;
-            s.wg[lane][8 + p][c] = w * hv;
-          }
+        for (int p = 0; p < 3; ++p) {
+          const double hv = s.j0[3 * p + rr] * par[p] * scale;
+          s.g[gp][8 + p][rr] = hv;
+          s.wg[gp][8 + p][rr] = w * hv;
+        }
       }
     }
     __syncwarp();
@@ -282,7 +301,9 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
       }
       if (lane == 0 && fail) record_element_error(err, e, 2);
       __syncwarp();
-      // X[:, c] = Kaa^-1 Kau[:, c] for the 24 columns (one lane each).
+      // Kua Kaa^-1 Kau = (L^-1 Kau)^T (L^-1 Kau) with Kaa = L L^T, so only the
+      // forward substitution is needed: X[:, c] = L^-1 Kau[:, c] for the 24
+      // columns (one lane each).
       if (lane < 24) {
         double y[9];
 #pragma unroll
@@ -293,17 +314,10 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
           y[i] = v * s.Linv[i];
         }
 #pragma unroll
-        for (int i = 8; i >= 0; --i) {
-          double v = y[i];
-#pragma unroll
-          for (int k = i + 1; k < 9; ++k) v -= s.L[k][i] * y[k];
-          y[i] = v * s.Linv[i];
-        }
-#pragma unroll
         for (int i = 0; i < 9; ++i) s.X[i][lane] = y[i];
       }
       __syncwarp();
-      // ── Phase D: Ke = Kuu - Kua X (lower triangle, mirrored) ──
+      // ── Phase D: Ke = Kuu - X^T X (lower triangle, mirrored) ──
       for (int t = lane; t < 300; t += 32) {
         // t -> (r, c) with c <= r in row order
         int r = static_cast<int>((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f);
@@ -313,7 +327,7 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
         double v = kval(s, lam, mu, r / 3, r % 3, c / 3, c % 3);
         double corr = 0.0;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) corr = fma(s.Kua[r][k], s.X[k][c], corr);
+        for (int k = 0; k < 9; ++k) corr = fma(s.X[k][r], s.X[k][c], corr);
         v -= corr;
         ke_s[r * 24 + c] = v;
         ke_s[c * 24 + r] = v;
