@@ -44,6 +44,7 @@ struct MultiState {
   int ncols;
   double tol;
   double rz[kP], pAp[kP], alpha[kP], beta[kP], rr[kP], rel[kP], norm_b[kP];
+  double tolk[kP];  // per-column stopping tolerance of this solve
   int flags[kP];
   int iters[kP];  // iteration count at which the column finished
 };
@@ -453,7 +454,8 @@ template <typename T>
 __global__ void __launch_bounds__(kVT, 1)
 k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
         const T* __restrict__ dinv, T* __restrict__ r, T* __restrict__ u, T* __restrict__ p,
-        MultiState* S, double tol, int max_iters, double* partials, unsigned* counter) {
+        MultiState* S, double tol, double outer_tol, int max_iters, double* partials,
+        unsigned* counter) {
   __shared__ double s_red[kVT];
   __shared__ double s_tot[2 * kP];
   const int cb = 4 * (threadIdx.x & 3);
@@ -504,6 +506,15 @@ k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
         fl = kFlagDone | kFlagZeroRhs | kFlagConverged;
       else if (!(rzk > 0.0))  // cuda_pcg_backend_impl.hpp:1859-1862
         fl = kFlagDone | kFlagNonPosRz;
+      // Inexact refinement per load case (as the single-case solve): with
+      // outer_tol > 0 a correction stops at 0.5 * outer_tol / (its case's
+      // true residual) when that is looser than tol.
+      double tk = tol;
+      if (O && outer_tol > 0.0 && O->rel[k] > 0.0) {
+        const double want = 0.5 * outer_tol / O->rel[k];
+        tk = fmax(tol, fmin(0.5, want));
+      }
+      S->tolk[k] = tk;
       S->rz[k] = rzk;
       S->rr[k] = rrk;
       S->norm_b[k] = nb;
@@ -577,7 +588,7 @@ k_mupdate(int n, T* __restrict__ u, T* __restrict__ r, const T* __restrict__ p,
         const int it = S->iter + 1;
         S->rr[k] = rrk;
         S->rel[k] = rel;
-        if (rel < S->tol) {
+        if (rel < S->tolk[k]) {
           fl |= kFlagDone | kFlagConverged;
           S->beta[k] = 0.0;
           S->iters[k] = it;
@@ -819,7 +830,7 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
     ++launches_;
     if (!mixed) {
       k_minit<double><<<vgrid, kVT, 0, s>>>(n_, nc, W.f.ptr, nullptr, op_->dinv.ptr, W.r64.ptr,
-                                            W.u64.ptr, W.p64.ptr, W.S.ptr, tol, max_iters,
+                                            W.u64.ptr, W.p64.ptr, W.S.ptr, tol, 0.0, max_iters,
                                             W.partials.ptr, W.counters.ptr);
       VSGB_LAUNCH_CHECK();
       ++launches_;
@@ -844,7 +855,8 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
       for (int k = 0; k < nc; ++k) res[static_cast<size_t>(k0 + k)].inner_solves = 0;
       for (int step = 0; step < max_solves && !W.hO->done; ++step) {
         k_minit<float><<<vgrid, kVT, 0, s>>>(n_, nc, W.r64.ptr, W.O.ptr, dinv32_.ptr, W.r32.ptr,
-                                             W.u32.ptr, W.p32.ptr, W.S.ptr, inner_tol, max_iters,
+                                             W.u32.ptr, W.p32.ptr, W.S.ptr, inner_tol,
+                                             adaptive_inner_ ? tol : 0.0, max_iters,
                                              W.partials.ptr, W.counters.ptr);
         VSGB_LAUNCH_CHECK();
         ++launches_;
