@@ -52,13 +52,13 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum + dram__bytes_write.sum)
-    from the committed ncu capture on block_160k, scaled to this workload by
-    its algorithmic bytes (traffic tracks the stored blocks; see profiles/)."""
+def _traffic_per_iteration(kernel: str):
+    """DRAM bytes per PCG iteration of the persistent `kernel`
+    (dram__bytes_read.sum + dram__bytes_write.sum of one captured launch over
+    its iterations), from the committed ncu summary in profiles/."""
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as fh:
-            return json.load(fh)[kernel]["cantilever_84k_scaled"]
+            return float(json.load(fh)[kernel]["dram_bytes_per_iteration"])
     except Exception:
         return None
 
@@ -283,6 +283,42 @@ def extra_jitter(B, C, device, uniform):
     return out
 
 
+def profile_case(which):
+    """Small, self-contained runs of the hot kernels for ncu captures."""
+    from vibestran_gb300 import backend as B
+    from vibestran_gb300 import cantilever as C
+    B.load_library(build_if_missing=True)
+    if which == "multi":
+        m = C.block_160k_16rhs()
+        eq6, n = B.build_dof_map(m)
+        F = np.stack([B.apply_forces(m, eq6, n, k) for k in range(16)], axis=1)
+        be = _mixed_backend(B, 0)
+        be.set_option(B.OPT_BATCHED, 2)
+        be.set_option(B.OPT_MAX_ITERS, 48)
+        asm = B.ChexaAssembler(be)
+        asm.assemble(m, eq6, n)
+        try:
+            asm.solve(F)
+        except B.SolverError as e:  # stops at 48 iterations by design
+            print("stopped:", str(e)[:60])
+        return
+    m = C.cantilever_84k()
+    eq6, n = B.build_dof_map(m)
+    F = B.apply_forces(m, eq6, n)
+    be = _mixed_backend(B, 0, max_solves=1 if which == "solve" else None)
+    asm = B.ChexaAssembler(be)
+    asm.upload(m, eq6, n)
+    reps = 3 if which == "assemble" else 1
+    for _ in range(reps):
+        B.timer_start(be)
+        asm.assemble_resident()
+        print(f"assemble {B.timer_stop(be):.3f} ms")
+    if which == "solve":
+        asm.upload_rhs(F)
+        st = asm.solve_resident()
+        print(f"inner solve: {st.kernel_iterations:.0f} iterations, {st.kernel_ms:.3f} ms")
+
+
 def cpu_reference(model, eq6, n, F, steps, warmup, threads):
     """CPU restatement of the reference path on the host cores (oracle port)."""
     from oracle import oracle as O
@@ -307,7 +343,16 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 16-load-case, adjoint and jittered-mesh measurements")
+    ap.add_argument("--profile", choices=["assemble", "solve", "multi"], default=None,
+                    help="run one small case of a hot kernel for a profiler and exit "
+                         "(no JSON line): assemble = 3 x element stiffness + block assembly "
+                         "of cantilever_84k; solve = one FP32 inner solve (persistent "
+                         "kernel) of cantilever_84k; multi = 48 batched iterations of the "
+                         "16-load-case block")
     a = ap.parse_args()
+    if a.profile:
+        profile_case(a.profile)
+        return
 
     from vibestran_gb300 import cantilever as C
     dist, rank, world = _dist()
@@ -467,7 +512,9 @@ def main():
         "roofline": {"kernel": "k_resident_pcg<float> (persistent FP32 inner solve)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
-                     "traffic": _traffic("k_resident_pcg_f32"),
+                     "traffic": (_traffic_per_iteration("k_resident_pcg_f32") * res_it
+                                 / max(res_launches, 1)
+                                 if _traffic_per_iteration("k_resident_pcg_f32") else None),
                      "algorithmic_bytes": res_it * res_bytes_it / max(res_launches, 1),
                      "avg_launch_us": 1e3 * res_ms / max(res_launches, 1),
                      "iterations_per_launch": res_it / max(res_launches, 1),
