@@ -450,13 +450,15 @@ struct FillSmem {
   double acc[kMaxNbr][9];            // block sums per neighbour slot
   unsigned char nz[kMaxNbr][9];      // entry received a value != 0.0
   short slot[kMaxCand];              // neighbour slot of candidate c (-1: constrained)
+  double rsum[9];                    // FP64 sum of the row's blocks (FP32 diagonal slot)
 };
 
 // Block row of node a: for each incident element (ascending, the reference's
 // summation order), its three rows of K_e (576 contiguous bytes, one
 // coalesced read) are added into the neighbour blocks in shared memory, then
-// the row is written to the sliced-ELL operator with its padding, the inverse
-// diagonal and the scalar nonzero counts (full and lower triangle).
+// the row is written to the sliced-ELL operator (FP64, and FP32 in difference
+// form) with its padding, the inverse diagonal and the scalar nonzero counts
+// (full and lower triangle).
 __global__ void __launch_bounds__(kFillWarps * 32)
 k_block_fill(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3,
              const int* __restrict__ node_ptr, const int* __restrict__ node_elem,
@@ -530,6 +532,14 @@ k_block_fill(int n_nodes, const int* __restrict__ conn, const int* __restrict__ 
         __syncwarp();
       }
     }
+    // FP32 difference form: the diagonal slot holds the sum of the row's
+    // blocks (ascending neighbour order).
+    if (v32 && lane < 9) {
+      double t = 0.0;
+      for (int u = 0; u < U; ++u) t += s.acc[u][lane];
+      s.rsum[lane] = t;
+    }
+    __syncwarp();
     const int sl = R >> 3, ln0 = (R & 7) * 4;
     const long long sp = slice_ptr[sl];
     unsigned long long full = 0, lower = 0;
@@ -545,7 +555,7 @@ k_block_fill(int n_nodes, const int* __restrict__ conn, const int* __restrict__ 
           const double v = s.acc[u][3 * d + q];
           const size_t o = static_cast<size_t>((st * 9 + 3 * d + q) * 32 + ln);
           v64[o] = v;
-          if (v32) v32[o] = static_cast<float>(v);
+          if (v32) v32[o] = static_cast<float>(b == a ? s.rsum[3 * d + q] : v);
           const bool z = s.nz[u][3 * d + q] != 0;
           full += z;
           lower += z && (3 * Cb + q <= 3 * R + d);

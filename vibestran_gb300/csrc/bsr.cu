@@ -117,7 +117,62 @@ k_bsr_fill(int nb, const int* __restrict__ rp, const int* __restrict__ ci,
   }
 }
 
+// FP32 copy in difference form: every stored block is rounded from val64,
+// except the diagonal block of each block row, which holds the FP64 sum of
+// all blocks of that row (R_I = sum_J K_IJ).  One warp per slice; lane
+// 4r+q accumulates its slots of row r over the steps, the quad adds its four
+// sums (the same value in all four lanes), and the slot whose column is the
+// row itself (a stored slot, not padding) receives the sum.
+__global__ void __launch_bounds__(kBsrWarps * 32)
+k_bsr_diff32(int nb, int nslices, const int* __restrict__ slice_ptr,
+             const int* __restrict__ rowlen, const int* __restrict__ cols,
+             const double* __restrict__ v64, float* __restrict__ v32) {
+  const int lane = threadIdx.x & 31;
+  for (int sl = blockIdx.x * kBsrWarps + (threadIdx.x >> 5); sl < nslices;
+       sl += gridDim.x * kBsrWarps) {
+    const long long base = slice_ptr[sl];
+    const int steps = static_cast<int>(slice_ptr[sl + 1] - base);
+    const int R = 8 * sl + (lane >> 2), q = lane & 3;
+    const int len = R < nb ? rowlen[R] : 0;
+    double rs[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) rs[k] = 0.0;
+    for (int t = 0; t < steps; ++t)
+#pragma unroll
+      for (int k = 0; k < 9; ++k) rs[k] += v64[((base + t) * 9 + k) * 32 + lane];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      rs[k] += __shfl_xor_sync(0xffffffffu, rs[k], 1);
+      rs[k] += __shfl_xor_sync(0xffffffffu, rs[k], 2);
+    }
+    for (int t = 0; t < steps; ++t) {
+      const long long st = base + t;
+      const bool diag = 4 * t + q < len && cols[st * 32 + lane] == R;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        const long long o = (st * 9 + k) * 32 + lane;
+        v32[o] = static_cast<float>(diag ? rs[k] : v64[o]);
+      }
+    }
+  }
+}
+
 }  // namespace
+
+void bsr_make_f32(BsrSell& B, int num_sms, cudaStream_t s) {
+  if (!B.has64) throw Error(VSGB_ERR_STATE, "the FP32 block operator is made from the FP64 one");
+  const size_t nstep = static_cast<size_t>(B.steps > 0 ? B.steps : 1);
+  B.val32.reserve(nstep * 288);
+  if (B.nslices > 0) {
+    const int grid = grid_for(static_cast<long long>(B.nslices) * 32, kBsrWarps * 32,
+                              num_sms * 16);
+    k_bsr_diff32<<<grid, kBsrWarps * 32, 0, s>>>(B.nb, B.nslices, B.slice_ptr.ptr,
+                                                 B.rowlen.ptr, B.cols.ptr, B.val64.ptr,
+                                                 B.val32.ptr);
+    VSGB_LAUNCH_CHECK();
+  }
+  B.has32 = true;
+}
 
 long long bsr_layout(BsrSell& B, int nb, cudaStream_t s) {
   const int nslices = (nb + 7) / 8;
@@ -180,7 +235,7 @@ bool build_bsr(const AssembledCsr& K, BsrSell& B, bool need64, bool need32, int 
   const size_t nstep = static_cast<size_t>(total_steps > 0 ? total_steps : 1);
   B.cols.reserve(nstep * 32);
   VSGB_CUDA(cudaMemsetAsync(B.cols.ptr, 0, sizeof(int) * nstep * 32, s));
-  if (need64) {
+  if (need64 || need32) {
     B.val64.reserve(nstep * 32 * 9);
     VSGB_CUDA(cudaMemsetAsync(B.val64.ptr, 0, sizeof(double) * nstep * 32 * 9, s));
     k_bsr_fill<double><<<wgrid, kBsrWarps * 32, 0, s>>>(nb, K.row_ptr.ptr, K.col_ind.ptr,
@@ -188,16 +243,9 @@ bool build_bsr(const AssembledCsr& K, BsrSell& B, bool need64, bool need32, int 
                                                         B.cols.ptr, B.val64.ptr);
     VSGB_LAUNCH_CHECK();
   }
-  if (need32) {
-    B.val32.reserve(nstep * 32 * 9);
-    VSGB_CUDA(cudaMemsetAsync(B.val32.ptr, 0, sizeof(float) * nstep * 32 * 9, s));
-    k_bsr_fill<float><<<wgrid, kBsrWarps * 32, 0, s>>>(nb, K.row_ptr.ptr, K.col_ind.ptr,
-                                                       K.values.ptr, B.slice_ptr.ptr,
-                                                       B.cols.ptr, B.val32.ptr);
-    VSGB_LAUNCH_CHECK();
-  }
-  B.has64 = need64;
-  B.has32 = need32;
+  B.has64 = true;  // the FP32 copy is made from it
+  B.has32 = false;
+  if (need32) bsr_make_f32(B, num_sms, s);
   B.valid = true;
   return true;
 }

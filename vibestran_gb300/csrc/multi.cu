@@ -239,6 +239,19 @@ __device__ __forceinline__ void mspmm_slice(const MView& B, const T* __restrict_
   const T* vp = vals + static_cast<size_t>(base) * 288 + lane;
   const T* xq = x + g0 + RN * (lane & 3);
   const int quad = lane & ~3;
+  // FP32: difference form (the diagonal slot holds the block-row sum), so
+  // non-diagonal blocks multiply x_J - x_I; xi holds the row's own panel rows.
+  constexpr bool kDiff = sizeof(T) == 4;
+  const int Rrow = 8 * sl + (lane >> 2);
+  T xi[3][RN];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int r = 0; r < RN; ++r) xi[j][r] = T(0);
+  if (kDiff && Rrow < B.nb) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ldn<RN>(xq + static_cast<size_t>(Rrow) * (3 * kP) + j * kP, xi[j]);
+  }
   int cn = 0;
   T an[9];
 #pragma unroll
@@ -266,10 +279,15 @@ __device__ __forceinline__ void mspmm_slice(const MView& B, const T* __restrict_
 #pragma unroll
       for (int k = 0; k < 9; ++k) a[k] = __shfl_sync(0xffffffffu, aown[k], src);
       const T* xc = xq + static_cast<size_t>(c) * (3 * kP);
+      const T m = kDiff && c != Rrow ? T(1) : T(0);
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         T xv[RN];
         ldn<RN>(xc + j * kP, xv);
+        if (kDiff) {
+#pragma unroll
+          for (int r = 0; r < RN; ++r) xv[r] = fmaT(-m, xi[j][r], xv[r]);
+        }
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll

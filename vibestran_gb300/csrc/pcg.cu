@@ -389,10 +389,29 @@ struct BsrView {
   const int* __restrict__ cols;
 };
 
+// The FP32 operator is in difference form (bsr.cuh): block columns other
+// than the row itself multiply x_J - x_I, the diagonal slot (holding the row
+// sum R_I) multiplies x_I.  With m = 0 on the diagonal and 1 elsewhere,
+// fma(-m, x_I, x_J) is exactly that operand.
+template <typename T>
+__device__ __forceinline__ void diff_operand(bool on, int c, int R, T i0, T i1, T i2, T& x0,
+                                             T& x1, T& x2) {
+  if (on) {
+    const T m = c != R ? T(1) : T(0);
+    x0 = fmat(-m, i0, x0);
+    x1 = fmat(-m, i1, x1);
+    x2 = fmat(-m, i2, x2);
+  }
+}
+
 template <typename T, typename Gather>
 __device__ __forceinline__ void bsr_row_block(const BsrView& B, const T* __restrict__ vals,
                                               int sl, int lane, Gather gx, T& y0, T& y1, T& y2) {
+  constexpr bool kDiff = sizeof(T) == 4;
   const int base = B.slice_ptr[sl], steps = B.slice_ptr[sl + 1] - base;
+  const int R = 8 * sl + (lane >> 2);
+  T i0 = T(0), i1 = T(0), i2 = T(0);
+  if (kDiff && R < B.nb) gx(R, i0, i1, i2);
   y0 = y1 = y2 = T(0);
   // Branch-free over the slice's steps: padding slots hold block column 0 and
   // zero values (allocated and zero-filled), so they add nothing, and the
@@ -411,6 +430,8 @@ __device__ __forceinline__ void bsr_row_block(const BsrView& B, const T* __restr
     T x0, x1, x2, w0, w1, w2;
     gx(c0, x0, x1, x2);
     gx(c1, w0, w1, w2);
+    diff_operand(kDiff, c0, R, i0, i1, i2, x0, x1, x2);
+    diff_operand(kDiff, c1, R, i0, i1, i2, w0, w1, w2);
     y0 = fmat(a[0][0], x0, fmat(a[0][1], x1, fmat(a[0][2], x2, y0)));
     y1 = fmat(a[0][3], x0, fmat(a[0][4], x1, fmat(a[0][5], x2, y1)));
     y2 = fmat(a[0][6], x0, fmat(a[0][7], x1, fmat(a[0][8], x2, y2)));
@@ -425,6 +446,7 @@ __device__ __forceinline__ void bsr_row_block(const BsrView& B, const T* __restr
     for (int k = 0; k < 9; ++k) a[k] = __ldcg(vp + 288 * t + 32 * k);
     T x0, x1, x2;
     gx(c0, x0, x1, x2);
+    diff_operand(kDiff, c0, R, i0, i1, i2, x0, x1, x2);
     y0 = fmat(a[0], x0, fmat(a[1], x1, fmat(a[2], x2, y0)));
     y1 = fmat(a[3], x0, fmat(a[4], x1, fmat(a[5], x2, y1)));
     y2 = fmat(a[6], x0, fmat(a[7], x1, fmat(a[8], x2, y2)));
@@ -568,12 +590,8 @@ void PcgEngine::prepare(const AssembledCsr& op, bool need32, cudaStream_t s, boo
     if (!bsr_.valid) throw Error(VSGB_ERR_STATE, "no block operator was assembled");
     use_bsr_ = true;
     if (need32 && !bsr_.has32) {
-      const long long cnt = bsr_.steps * 288;
-      bsr_.val32.reserve(static_cast<size_t>(cnt > 0 ? cnt : 1));
-      k_cast_f32<<<num_sms_ * 8, kThreads, 0, s>>>(cnt, bsr_.val64.ptr, bsr_.val32.ptr);
-      VSGB_LAUNCH_CHECK();
+      bsr_make_f32(bsr_, num_sms_, s);
       launches_ += 1;
-      bsr_.has32 = true;
     }
   } else if (format_ != 1) {
     use_bsr_ = build_bsr(op, bsr_, true, need32, num_sms_, s);

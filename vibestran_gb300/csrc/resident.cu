@@ -54,6 +54,7 @@ struct ResArgs {
   double tol;
   int max_iters;
   int rows_max;  // own-row stride of the shared-memory vectors
+  T* u_glob;     // solution accumulator in global memory (null: in shared memory)
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -224,13 +225,14 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   const int s0 = a.cta_slice[c], s1 = a.cta_slice[c + 1], ns = s1 - s0;
   const int g0 = 24 * s0;
   const int nrows = max(0, min(24 * s1, a.n) - g0);
+  // Own-row vectors r, p, Ap, diag^-1 (and the solution accumulator u unless
+  // it lives in global memory; z = r diag^-1 is recomputed where needed).
   T* RR = reinterpret_cast<T*>(smem);
-  T* Z = RR + a.rows_max;
-  T* U = Z + a.rows_max;
-  T* P = U + a.rows_max;
+  T* P = RR + a.rows_max;
   T* AP = P + a.rows_max;
   T* D = AP + a.rows_max;
-  T* SL = D + a.rows_max;   // per-slice p.Ap sums (slices are handed out dynamically)
+  T* U = a.u_glob ? a.u_glob + g0 : D + a.rows_max;
+  T* SL = D + (a.u_glob ? 1 : 2) * a.rows_max;  // per-slice p.Ap sums (slices are handed out dynamically)
   T* win = SL + slot_count(a.rows_max);  // 4 per node when kWindow
   const int wb = a.cta_win[2 * c], we = a.cta_win[2 * c + 1];
   unsigned target = 0;
@@ -249,7 +251,6 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     const T zv = rv * dv;
     RR[lr] = rv;
     U[lr] = T(0);
-    Z[lr] = zv;
     P[lr] = T(0);
     AP[lr] = T(0);
     D[lr] = dv;
@@ -327,6 +328,25 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       const int* cp = a.cols + static_cast<size_t>(base) * 32 + lane;
       const T* vp = a.vals + static_cast<size_t>(base) * 288 + lane;
       T y0 = T(0), y1 = T(0), y2 = T(0);
+      // FP32: the operator is in difference form (the diagonal slot holds the
+      // block-row sum): non-diagonal blocks multiply x_J - x_I.
+      constexpr bool kDiff = sizeof(T) == 4;
+      const int Rrow = 8 * sl + (lane >> 2);
+      T i0 = T(0), i1 = T(0), i2 = T(0);
+      if (kDiff && Rrow < a.nb) {
+        if (kWindow) {
+          // the diagonal block column is one of the slice's columns, so it
+          // lies in the window; the test only guards the shared-memory read
+          if (Rrow >= wb && Rrow <= we) lds3(win + 4 * (Rrow - wb), i0, i1, i2);
+        } else {
+          T z0, z1, z2, q0, q1, q2;
+          ld3(a.z4 + 4 * static_cast<size_t>(Rrow), z0, z1, z2);
+          ld3(p_old + 4 * static_cast<size_t>(Rrow), q0, q1, q2);
+          i0 = rfma(tb, q0, z0);
+          i1 = rfma(tb, q1, z1);
+          i2 = rfma(tb, q2, z2);
+        }
+      }
       // Up to kAhead steps of operator loads are issued before any of them is
       // consumed, so each warp keeps ~kAhead*40 B (FP32) per lane in flight.
       constexpr int kAhead = sizeof(T) == 4 ? 4 : 2;
@@ -355,6 +375,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
               x1 = rfma(tb, q1, z1);
               x2 = rfma(tb, q2, z2);
             }
+            if (kDiff) {
+              const T m = col[u] != Rrow ? T(1) : T(0);
+              x0 = rfma(-m, i0, x0);
+              x1 = rfma(-m, i1, x1);
+              x2 = rfma(-m, i2, x2);
+            }
             y0 = rfma(v[u][0], x0, rfma(v[u][1], x1, rfma(v[u][2], x2, y0)));
             y1 = rfma(v[u][3], x0, rfma(v[u][4], x1, rfma(v[u][5], x2, y1)));
             y2 = rfma(v[u][6], x0, rfma(v[u][7], x1, rfma(v[u][8], x2, y2)));
@@ -373,7 +399,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       if (q < 3 && R < a.nb) {
         const int lr = 24 * ls + 3 * r + q;
         const T yq = q == 0 ? y0 : (q == 1 ? y1 : y2);
-        const T pn = rfma(tb, P[lr], Z[lr]);
+        const T pn = rfma(tb, P[lr], RR[lr] * D[lr]);  // z = r diag^-1, as stored in z4
         P[lr] = pn;
         AP[lr] = yq;
         p_new[4 * R + q] = pn;
@@ -423,7 +449,6 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       const T rv = rfma(-ta, AP[lr], RR[lr]);
       const T zv = rv * D[lr];
       RR[lr] = rv;
-      Z[lr] = zv;
       a.z4[4 * R + q] = zv;
       acc2[0] = rfma(rv, zv, acc2[0]);
       acc2[1] = rfma(rv, rv, acc2[1]);
@@ -519,7 +544,8 @@ __global__ void k_slice_minmax(int nslices, const int* __restrict__ slice_ptr,
 template <typename T, bool kWindow, bool kMixed>
 void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const double* rhs,
                      double* u, PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
-                     T* z4, T* p4a, T* p4b, const double* dinv, size_t smem, cudaStream_t s) {
+                     T* z4, T* p4a, T* p4b, const double* dinv, size_t smem, T* u_glob,
+                     cudaStream_t s) {
   ResArgs<T> a;
   a.nb = B.nb;
   a.n = 3 * B.nb;
@@ -542,6 +568,7 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   a.tol = tol;
   a.max_iters = max_iters;
   a.rows_max = 24 * P.max_slices;
+  a.u_glob = u_glob;
   VSGB_CUDA(cudaMemsetAsync(P.barrier.ptr, 0, sizeof(unsigned), s));
   VSGB_CUDA(cudaMemsetAsync(P.abort_flag.ptr, 0, sizeof(int), s));
   void* args[] = {&a};
@@ -641,42 +668,39 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
   const size_t rows = 24 * static_cast<size_t>(max_slices);
   const size_t nodes4 = 4 * static_cast<size_t>(nb);
   auto fit = [&](size_t bytes) { return bytes <= static_cast<size_t>(smem_optin); };
-  // FP64
-  {
-    const size_t own = (6 * rows + slot_count(static_cast<int>(rows))) * sizeof(double);
-    const size_t w = 4 * static_cast<size_t>(max_win) * sizeof(double);
+  // Shared memory per CTA: own-row vectors r, p, Ap, diag^-1 (+ the solution
+  // accumulator when it fits), the per-slice sums and the x window.  Tried in
+  // order: window with u in shared memory, window with u in global memory,
+  // then the same two without the window.
+  auto plan = [&](size_t elem, auto cfg_win, auto cfg_nowin, bool& ok, bool& win, bool& ug,
+                  size_t& smem) {
+    const size_t slots = slot_count(static_cast<int>(rows));
+    const size_t w = 4 * static_cast<size_t>(max_win) * elem;
     int blocks = 0;
-    if (fit(own + w) && configure<double, true, false>(own + w, &blocks)) {
-      P.win64 = true;
-      P.smem64 = own + w;
-      P.ok64 = true;
-    } else if (fit(own) && configure<double, false, false>(own, &blocks)) {
-      P.win64 = false;
-      P.smem64 = own;
-      P.ok64 = true;
+    for (int mode = 0; mode < 4 && !ok; ++mode) {
+      const bool want_win = mode < 2, u_global = (mode & 1) != 0;
+      const size_t bytes = ((u_global ? 4 : 5) * rows + slots) * elem + (want_win ? w : 0);
+      if (!fit(bytes)) continue;
+      if (!(want_win ? cfg_win(bytes, &blocks) : cfg_nowin(bytes, &blocks))) continue;
+      ok = true;
+      win = want_win;
+      ug = u_global;
+      smem = bytes;
     }
-    if (P.ok64) {
-      P.z4d.reserve(nodes4);
-      P.p4da.reserve(nodes4);
-      P.p4db.reserve(nodes4);
-      VSGB_CUDA(cudaMemsetAsync(P.z4d.ptr, 0, sizeof(double) * nodes4, s));
-      VSGB_CUDA(cudaMemsetAsync(P.p4da.ptr, 0, sizeof(double) * nodes4, s));
-      VSGB_CUDA(cudaMemsetAsync(P.p4db.ptr, 0, sizeof(double) * nodes4, s));
-    }
+  };
+  plan(sizeof(double), configure<double, true, false>, configure<double, false, false>, P.ok64,
+       P.win64, P.ug64, P.smem64);
+  if (P.ok64) {
+    P.z4d.reserve(nodes4);
+    P.p4da.reserve(nodes4);
+    P.p4db.reserve(nodes4);
+    VSGB_CUDA(cudaMemsetAsync(P.z4d.ptr, 0, sizeof(double) * nodes4, s));
+    VSGB_CUDA(cudaMemsetAsync(P.p4da.ptr, 0, sizeof(double) * nodes4, s));
+    VSGB_CUDA(cudaMemsetAsync(P.p4db.ptr, 0, sizeof(double) * nodes4, s));
   }
   if (need32 && B.has32) {
-    const size_t own = (6 * rows + slot_count(static_cast<int>(rows))) * sizeof(float);
-    const size_t w = 4 * static_cast<size_t>(max_win) * sizeof(float);
-    int blocks = 0;
-    if (fit(own + w) && configure<float, true, true>(own + w, &blocks)) {
-      P.win32 = true;
-      P.smem32 = own + w;
-      P.ok32 = true;
-    } else if (fit(own) && configure<float, false, true>(own, &blocks)) {
-      P.win32 = false;
-      P.smem32 = own;
-      P.ok32 = true;
-    }
+    plan(sizeof(float), configure<float, true, true>, configure<float, false, true>, P.ok32,
+         P.win32, P.ug32, P.smem32);
     if (P.ok32) {
       P.z4f.reserve(nodes4);
       P.p4fa.reserve(nodes4);
@@ -684,6 +708,7 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
       VSGB_CUDA(cudaMemsetAsync(P.z4f.ptr, 0, sizeof(float) * nodes4, s));
       VSGB_CUDA(cudaMemsetAsync(P.p4fa.ptr, 0, sizeof(float) * nodes4, s));
       VSGB_CUDA(cudaMemsetAsync(P.p4fb.ptr, 0, sizeof(float) * nodes4, s));
+      if (P.ug32) P.u32g.reserve(3 * static_cast<size_t>(nb));
     }
   }
   VSGB_CUDA(cudaStreamSynchronize(s));
@@ -692,23 +717,29 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
 void resident_solve32(const BsrSell& B, ResidentPlan& P, const double* r64, double* u64,
                       PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
                       cudaStream_t s, const double* dinv) {
+  float* ug = P.ug32 ? P.u32g.ptr : nullptr;
   if (P.win32)
     launch_resident<float, true, true>(B, P, B.val32.ptr, r64, u64, S, O, tol, max_iters,
-                                       P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, P.smem32, s);
+                                       P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, P.smem32, ug, s);
   else
     launch_resident<float, false, true>(B, P, B.val32.ptr, r64, u64, S, O, tol, max_iters,
-                                        P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, P.smem32, s);
+                                        P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, P.smem32, ug,
+                                        s);
 }
 
 void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double* u,
                       PcgScalars* S, double tol, int max_iters, cudaStream_t s,
                       const double* dinv) {
+  // the FP64 solve accumulates straight into its output when u is global
+  double* ug = P.ug64 ? u : nullptr;
   if (P.win64)
     launch_resident<double, true, false>(B, P, B.val64.ptr, f, u, S, nullptr, tol, max_iters,
-                                         P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, P.smem64, s);
+                                         P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, P.smem64, ug,
+                                         s);
   else
     launch_resident<double, false, false>(B, P, B.val64.ptr, f, u, S, nullptr, tol, max_iters,
-                                          P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, P.smem64, s);
+                                          P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, P.smem64,
+                                          ug, s);
 }
 
 }  // namespace vsgb

@@ -12,6 +12,7 @@ namespace vsgb {
 struct ResidentPlan {
   bool ok32 = false, ok64 = false;  // usable for FP32 inner / FP64 solves
   bool win32 = false, win64 = false;  // x window staged in shared memory
+  bool ug32 = false, ug64 = false;    // solution accumulator in global memory
   int ctas = 0, threads = 0;
   size_t smem32 = 0, smem64 = 0;
   int max_slices = 0;               // slices of the largest CTA range
@@ -20,6 +21,7 @@ struct ResidentPlan {
   DevBuf<double> partials;          // 2 barrier slots x ctas x up to 4 values
   DevBuf<unsigned> barrier;         // monotonic arrival counter
   DevBuf<int> abort_flag;           // set by a barrier that gave up waiting
+  DevBuf<float> u32g;                       // FP32 solution accumulator when ug32
   DevBuf<float> z4f, p4fa, p4fb, dinv4f;    // node-padded FP32 vectors (4 per node)
   DevBuf<double> z4d, p4da, p4db, dinv4d;   // node-padded FP64 vectors
 };
