@@ -34,9 +34,10 @@ WORKLOAD = "cantilever_84k"
 # (checked every run against a converged FP64 reference, reported as rel_err).
 FP64_TOL = 1e-4          # sqrt(r.r)/||F|| of the FP64 PCG recursion
 MIXED_TOL = 1e-4         # true FP64 residual after refinement
-MIXED_INNER_TOL = 1e-3   # FP32 inner solves (the FP32 operator limits each to ~2e-3)
+MIXED_INNER_TOL = 1e-3   # first FP32 inner solve (later ones adapt to what is left)
 MIXED_MAX_SOLVES = 4
 JITTER_MIXED_TOL = 2e-5  # jittered heterogeneous mesh: <= 1e-6 error needs a tighter residual
+JITTER_INNER_TOL = 1e-4  # and a deeper first inner solve: 932 FP32 iterations vs 1043 at 1e-3
 MULTI_MIXED_TOL = 1e-8   # 16 random face-load cases: <= 1e-6 error (see extra_multi_rhs)
 # FP64 FMA rate of a GB300 measured with an FMA-chain kernel (1.91 DFMA/clk/SM
 # at 2.07 GHz): the compute floor of the FP64 SpMV.
@@ -187,7 +188,7 @@ def extra_multi_rhs(B, C, device):
     return out
 
 
-def extra_adjoint(B, C, device, n_fd=4):
+def extra_adjoint(B, C, device, n_fd=32):
     """Gradients of compliance and of the mean -z tip displacement w.r.t. all
     250 000 element moduli (100x50x50, n = 780 300, log-uniform E): one call
     (solves of K [u, lam] = [F, c] + one element pass), checked against the
@@ -252,6 +253,7 @@ def extra_jitter(B, C, device, uniform):
     eq6, n = B.build_dof_map(m)
     F = B.apply_forces(m, eq6, n)
     be = _mixed_backend(B, device, tol=JITTER_MIXED_TOL)
+    be.set_option(B.OPT_INNER_TOL, JITTER_INNER_TOL)
     asm = B.ChexaAssembler(be)
     asm.assemble(m, eq6, n)
     asm.upload_rhs(F)
@@ -266,7 +268,7 @@ def extra_jitter(B, C, device, uniform):
     be.close()
     out = {"workload": "cantilever_84k_jitter", "dofs": n, "seed": m.seed,
            "fp64": {"iterations": st_d.iterations, "solve_s": st_d.solve_ms / 1e3},
-           "mixed": {"tolerance": JITTER_MIXED_TOL,
+           "mixed": {"tolerance": JITTER_MIXED_TOL, "inner_tolerance": JITTER_INNER_TOL,
                      "iterations_fp32": st_m.iterations, "inner_solves": st_m.inner_solves,
                      "solve_s": st_m.solve_ms / 1e3},
            "iteration_growth_vs_uniform": {
