@@ -22,6 +22,9 @@ struct vsgb_ctx {
   int device = 0;
   int num_sms = 152;
   cudaStream_t stream = nullptr;
+  cudaStream_t topo = nullptr;      // high priority: topology passes beside the element kernel
+  cudaEvent_t topo_done = nullptr;  // joins topo into stream
+  cudaEvent_t topo_start = nullptr; // orders topo after earlier work on stream
   std::string device_name;
   std::string last_error;
   double tol = 1e-8;
@@ -34,7 +37,7 @@ struct vsgb_ctx {
   // resident mesh
   int n_nodes = 0, n_elem = 0, n_dof = 0;
   bool mesh_ok = false, assembled = false, has_form = false;
-  DevBuf<double> xyz, E, nu, kbuf;
+  DevBuf<double> xyz, E, nu, kbuf, lame;
   DevBuf<int> eq3, conn, form;
   DevBuf<vsgb::ElementError> elem_err;
   vsgb::AssemblyScratch scr;
@@ -124,9 +127,9 @@ void check_assembly_error(vsgb_ctx* c) {
   }
 }
 
-void reset_assembly_error(vsgb_ctx* c) {
+void reset_assembly_error(vsgb_ctx* c, cudaStream_t s) {
   c->scr.err.reserve(1);
-  VSGB_CUDA(cudaMemsetAsync(c->scr.err.ptr, 0, sizeof(vsgb::AssemblyError), c->stream));
+  VSGB_CUDA(cudaMemsetAsync(c->scr.err.ptr, 0, sizeof(vsgb::AssemblyError), s));
   c->scr.flag.reserve(1);
 }
 
@@ -135,7 +138,7 @@ void reset_assembly_error(vsgb_ctx* c) {
 void ensure_csr(vsgb_ctx* c) {
   if (c->csr_ready) return;
   if (!c->mesh_ok) throw Error(VSGB_ERR_STATE, "no mesh uploaded");
-  reset_assembly_error(c);
+  reset_assembly_error(c, c->stream);
   vsgb::assemble_csr(c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof, c->kbuf.ptr,
                      c->scr, c->K, c->num_sms, c->stream);
   c->eng->add_launches(18);
@@ -298,7 +301,12 @@ int vsgb_create(int device, double tol, int max_iters, int precision, vsgb_ctx**
   c->precision = precision;
   c->tol = tol > 0.0 ? tol : default_tol(precision);
   c->max_iters = max_iters > 0 ? max_iters : 10000;
+  int prio_low = 0, prio_high = 0;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->topo, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->topo_done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->topo_start, cudaEventDisableTiming) != cudaSuccess ||
       cudaMallocHost(&c->h_scal, sizeof(vsgb::PcgScalars) * 2) != cudaSuccess) {
     vsgb_destroy(c);
     return VSGB_ERR_CUDA;
@@ -317,10 +325,14 @@ void vsgb_destroy(vsgb_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->topo) cudaStreamSynchronize(c->topo);
   c->eng.reset();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->h_scal) cudaFreeHost(c->h_scal);
+  if (c->topo_done) cudaEventDestroy(c->topo_done);
+  if (c->topo_start) cudaEventDestroy(c->topo_start);
+  if (c->topo) cudaStreamDestroy(c->topo);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -422,7 +434,7 @@ int vsgb_solve_csr(vsgb_ctx* c, int n, int nnz, const int* row_ptr, const int* c
     upload(c->in_rp.ptr, row_ptr, sizeof(int) * (n + 1), s);
     upload(c->in_ci.ptr, col_ind, sizeof(int) * nnz, s);
     upload(c->in_v.ptr, values, sizeof(double) * nnz, s);
-    reset_assembly_error(c);
+    reset_assembly_error(c, s);
     c->assembled = false;
     vsgb::prepare_full_csr(n, nnz, c->in_rp.ptr, c->in_ci.ptr, c->in_v.ptr, lower_only != 0,
                            c->scr, c->K, c->num_sms, s);
@@ -497,21 +509,30 @@ int vsgb_assemble_resident(vsgb_ctx* c, long long* nnz_lower_out) {
     c->elem_err.reserve(1);
     const vsgb::ElementError init{INT_MAX, 0};
     VSGB_CUDA(cudaMemcpyAsync(c->elem_err.ptr, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    c->lame.reserve(2 * static_cast<size_t>(c->n_elem));
+    // the topology passes (side stream) rewrite the block layout: they follow
+    // everything queued on the stream before the element kernel
+    VSGB_CUDA(cudaEventRecord(c->topo_start, s));
+    VSGB_CUDA(cudaStreamWaitEvent(c->topo, c->topo_start, 0));
     vsgb::launch_chexa8_stiffness(c->n_elem, c->xyz.ptr, c->conn.ptr, c->E.ptr, c->nu.ptr,
                                   c->has_form ? c->form.ptr : nullptr, c->kbuf.ptr,
-                                  c->elem_err.ptr, c->num_sms, s);
-    c->eng->add_launches(1);
-    reset_assembly_error(c);
+                                  c->elem_err.ptr, c->lame.ptr, c->num_sms, s);
+    c->eng->add_launches(2);
     c->csr_ready = false;
     c->blocks_prebuilt = false;
     // Node-aligned equations: assemble the 3x3 block operator directly; the
     // scalar CSR is built only when asked for (vsgb_copy_csr_lower, or the
-    // scalar format).
-    if (c->format != 1 &&
-        vsgb::assemble_blocks(c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof,
-                              c->kbuf.ptr, c->scr, c->K, c->eng->blocks(),
-                              c->precision == VSGB_MIXED, c->num_sms, s)) {
-      c->blocks_prebuilt = true;
+    // scalar format).  Its topology passes run on the side stream while the
+    // element kernel runs.
+    if (c->format != 1) {
+      reset_assembly_error(c, c->topo);
+      c->blocks_prebuilt = vsgb::assemble_blocks(
+          c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof, c->kbuf.ptr, c->scr, c->K,
+          c->eng->blocks(), c->precision == VSGB_MIXED, c->num_sms, s, c->topo, c->topo_done);
+    } else {
+      reset_assembly_error(c, s);
+    }
+    if (c->blocks_prebuilt) {
       c->eng->add_launches(12);
     } else {
       vsgb::assemble_csr(c->n_nodes, c->n_elem, c->conn.ptr, c->eq3.ptr, c->n_dof, c->kbuf.ptr,

@@ -851,38 +851,55 @@ void assemble_csr(int n_nodes, int n_elem, const int* conn, const int* eq3, int 
 
 bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, int n_dof,
                      const double* kbuf, AssemblyScratch& scr, AssembledCsr& out, BsrSell& B,
-                     bool need32, int num_sms, cudaStream_t s) {
+                     bool need32, int num_sms, cudaStream_t s, cudaStream_t topo,
+                     cudaEvent_t joined) {
   if (n_dof <= 0 || n_dof % 3 != 0) return false;
+  // Everything up to the fill depends on the mesh topology only: it runs on
+  // `topo` (its host round trips wait for topology work alone, not for the
+  // element kernel already queued on s), and s waits for it before the fill.
+  auto join = [&] {
+    VSGB_CUDA(cudaEventRecord(joined, topo));
+    VSGB_CUDA(cudaStreamWaitEvent(s, joined, 0));
+  };
   scr.flag.reserve(1);
-  VSGB_CUDA(cudaMemsetAsync(scr.flag.ptr, 0, sizeof(int), s));
-  k_node_aligned<<<grid_for(n_nodes, kThreads, 1 << 30), kThreads, 0, s>>>(n_nodes, eq3,
-                                                                         scr.flag.ptr);
+  VSGB_CUDA(cudaMemsetAsync(scr.flag.ptr, 0, sizeof(int), topo));
+  k_node_aligned<<<grid_for(n_nodes, kThreads, 1 << 30), kThreads, 0, topo>>>(n_nodes, eq3,
+                                                                            scr.flag.ptr);
   VSGB_LAUNCH_CHECK();
   int misaligned = 0;
-  VSGB_CUDA(cudaMemcpyAsync(&misaligned, scr.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-  VSGB_CUDA(cudaStreamSynchronize(s));
-  if (misaligned) return false;
+  VSGB_CUDA(cudaMemcpyAsync(&misaligned, scr.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, topo));
+  VSGB_CUDA(cudaStreamSynchronize(topo));
+  if (misaligned) {
+    join();
+    return false;
+  }
 
-  build_incidence(n_nodes, n_elem, conn, eq3, n_dof, scr, s);
+  build_incidence(n_nodes, n_elem, conn, eq3, n_dof, scr, topo);
   const int nb = n_dof / 3;
   B.valid = false;
   B.rowlen.reserve(static_cast<size_t>(nb));
-  VSGB_CUDA(cudaMemsetAsync(B.rowlen.ptr, 0, sizeof(int) * nb, s));
+  VSGB_CUDA(cudaMemsetAsync(B.rowlen.ptr, 0, sizeof(int) * nb, topo));
   scr.counts.reserve(2);
-  VSGB_CUDA(cudaMemsetAsync(scr.counts.ptr, 0, sizeof(unsigned long long) * 2, s));
+  VSGB_CUDA(cudaMemsetAsync(scr.counts.ptr, 0, sizeof(unsigned long long) * 2, topo));
   const int pgrid = grid_for(static_cast<long long>(n_nodes) * 32, kPatWarps * 32, num_sms * 16);
-  k_block_count<<<pgrid, kPatWarps * 32, 0, s>>>(n_nodes, conn, eq3, scr.node_ptr.ptr,
-                                                 scr.node_elem.ptr, B.rowlen.ptr, scr.err.ptr);
+  k_block_count<<<pgrid, kPatWarps * 32, 0, topo>>>(n_nodes, conn, eq3, scr.node_ptr.ptr,
+                                                    scr.node_elem.ptr, B.rowlen.ptr, scr.err.ptr);
   VSGB_LAUNCH_CHECK();
-  const long long total_steps = bsr_layout(B, nb, s);  // synchronises
+  const long long total_steps = bsr_layout(B, nb, topo);  // synchronises topo
   // stored blocks (the sum of the row lengths)
   B.h_blen.resize(static_cast<size_t>(nb));
   VSGB_CUDA(cudaMemcpyAsync(B.h_blen.data(), B.rowlen.ptr, sizeof(int) * nb,
-                            cudaMemcpyDeviceToHost, s));
-  VSGB_CUDA(cudaStreamSynchronize(s));
+                            cudaMemcpyDeviceToHost, topo));
+  int last = 0;  // first step of the last slice
+  VSGB_CUDA(cudaMemcpyAsync(&last, B.slice_ptr.ptr + B.nslices - 1, sizeof(int),
+                            cudaMemcpyDeviceToHost, topo));
+  VSGB_CUDA(cudaStreamSynchronize(topo));
   long long blocks = 0;
   for (int R = 0; R < nb; ++R) blocks += B.h_blen[R];
-  if (blocks == 0) return false;
+  if (blocks == 0) {
+    join();
+    return false;
+  }
 
   const size_t nstep = static_cast<size_t>(total_steps > 0 ? total_steps : 1);
   B.cols.reserve(nstep * 32);
@@ -891,18 +908,16 @@ bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, i
   if (nb % 8 != 0) {
     // lanes of the last slice beyond nb belong to no node: block column 0,
     // zero values (read, never stored)
-    int last = 0;
-    VSGB_CUDA(cudaMemcpyAsync(&last, B.slice_ptr.ptr + B.nslices - 1, sizeof(int),
-                              cudaMemcpyDeviceToHost, s));
-    VSGB_CUDA(cudaStreamSynchronize(s));
     const size_t tail = nstep - static_cast<size_t>(last);
-    VSGB_CUDA(cudaMemsetAsync(B.cols.ptr + static_cast<size_t>(last) * 32, 0, sizeof(int) * tail * 32, s));
+    VSGB_CUDA(cudaMemsetAsync(B.cols.ptr + static_cast<size_t>(last) * 32, 0,
+                              sizeof(int) * tail * 32, topo));
     VSGB_CUDA(cudaMemsetAsync(B.val64.ptr + static_cast<size_t>(last) * 288, 0,
-                              sizeof(double) * tail * 288, s));
+                              sizeof(double) * tail * 288, topo));
     if (need32)
       VSGB_CUDA(cudaMemsetAsync(B.val32.ptr + static_cast<size_t>(last) * 288, 0,
-                                sizeof(float) * tail * 288, s));
+                                sizeof(float) * tail * 288, topo));
   }
+  join();
   out.n = n_dof;
   out.dinv.reserve(static_cast<size_t>(n_dof));
   const int fgrid = grid_for(static_cast<long long>(n_nodes) * 32, kFillWarps * 32, num_sms * 32);

@@ -181,12 +181,11 @@ long long bsr_layout(BsrSell& B, int nb, cudaStream_t s) {
   B.slice_ptr.reserve(static_cast<size_t>(nslices) + 1);
   B.tmp.reserve(scan_tmp_size(nslices + 1));
   B.total.reserve(1);
-  DevBuf<int> steps;
-  steps.reserve(static_cast<size_t>(nslices) + 1);
-  k_slice_steps<<<grid_for(nslices, kThreads, 1 << 30), kThreads, 0, s>>>(nb, nslices,
-                                                                          B.rowlen.ptr, steps.ptr);
+  B.slice_steps.reserve(static_cast<size_t>(nslices) + 1);
+  k_slice_steps<<<grid_for(nslices, kThreads, 1 << 30), kThreads, 0, s>>>(
+      nb, nslices, B.rowlen.ptr, B.slice_steps.ptr);
   VSGB_LAUNCH_CHECK();
-  exclusive_scan_checked(steps.ptr, B.slice_ptr.ptr, nslices, B.tmp.ptr, B.total.ptr, s);
+  exclusive_scan_checked(B.slice_steps.ptr, B.slice_ptr.ptr, nslices, B.tmp.ptr, B.total.ptr, s);
   long long total_steps = 0;
   VSGB_CUDA(cudaMemcpyAsync(&total_steps, B.total.ptr, sizeof(long long), cudaMemcpyDeviceToHost, s));
   VSGB_CUDA(cudaStreamSynchronize(s));

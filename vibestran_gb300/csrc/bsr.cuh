@@ -27,6 +27,7 @@ struct BsrSell {
   // in the plain product (fewer FP32 iterations after each refinement).
   DevBuf<float> val32;     // steps * 32 * 9
   DevBuf<int> tmp;
+  DevBuf<int> slice_steps;  // scratch of bsr_layout (kept: a free would synchronise the device)
   DevBuf<long long> total;
   std::vector<int> h_blen;
 };
@@ -43,11 +44,15 @@ long long bsr_layout(BsrSell& B, int nb, cudaStream_t s);
 
 // Block operator straight from the element stiffness buffer when the
 // equations are node-aligned triples (no scalar CSR is built); returns false,
-// with nothing changed in B, when they are not or the blocks are < 90%
-// filled.  out receives n, dinv and the scalar nnz (full and lower).
+// with B left invalid, when they are not or the blocks are < 90% filled.
+// out receives n, dinv and the scalar nnz (full and lower).  The topology
+// passes (incidence, block counts, layout) run on topo, concurrently with
+// whatever s is still running (the element kernel); s waits for them (through
+// the event joined) before the fill, on every return path.
 bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, int n_dof,
                      const double* kbuf, AssemblyScratch& scr, AssembledCsr& out, BsrSell& B,
-                     bool need32, int num_sms, cudaStream_t s);
+                     bool need32, int num_sms, cudaStream_t s, cudaStream_t topo,
+                     cudaEvent_t joined);
 
 // FP32 copy of the block operator (difference form) from val64.
 void bsr_make_f32(BsrSell& B, int num_sms, cudaStream_t s);

@@ -10,15 +10,22 @@
 // over 11 virtual nodes: the 8 element nodes (g = J^-1 dN/dxi) and the three
 // EAS enhancement gradients h_p = J0^-1.row(p) * xi_p * detJ0/detJ (the
 // reference's row-of-inverse form, solid_elements.cpp:1131-1133, :1109).
-// Accumulating the 66 M_AB (594 FP64 values) replaces the 24x24 / 24x9 / 9x9
-// B^T D B products, then Ke = Kuu - Kua Kaa^-1 Kau is condensed with a 9x9
-// Cholesky (Eigen::LLT at :1201-1204), as Kuu - Y^T Y with Y = L^-1 Kau.
+// The 66 M_AB (594 FP64 values) replace the 24x24 / 24x9 / 9x9 B^T D B
+// products.  h_p is a fixed vector times a per-point scalar, so with
+// c_p = detJ0 J0^-1.row(p) the enhancement moments factor as
+//     M_{A,8+p}   = (sum_gp xi_p g_A) (x) c_p
+//     M_{8+p,8+q} = (sum_gp xi_p xi_q / detJ) c_p (x) c_q
+// (78 eight-term sums instead of 270).  Ke = Kuu - Kua Kaa^-1 Kau is then
+// condensed with a 9x9 Cholesky (Eigen::LLT at :1201-1204), as Kuu - Y^T Y
+// with Y = L^-1 Kau.
 // Ke is written exactly symmetric (entry (c,r) is a copy of (r,c)).
 //
 // Roofline: FP64-pipe bound (ncu: FP64 pipe ~90% busy; GB300 issues one FP64
 // warp instruction per ~17 cycles per SM whatever its active lanes, so the
 // work is spread over the warp wherever it can be).  Inputs 8 node
 // coordinates + E, nu (~220 B), output 576 doubles (4.6 kB) per element.
+
+#include <cstddef>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -30,21 +37,33 @@ namespace {
 constexpr int kWarpsPerBlock = 4;
 constexpr int kVN = 11;        // virtual nodes: 8 element nodes + 3 enhancement gradients
 constexpr int kPairs = 66;     // A <= B over 11 virtual nodes
-constexpr int kPairsSri = 36;  // A <= B over the 8 element nodes
 
 
-struct WarpSmem {
-  double g[9][kVN][3];    // gradients at the 8 Gauss points + centroid (index 8)
-  double wg[9][kVN][3];   // weighted gradients (w = detJ; centroid: 8*detJ0 for SRI)
-  double M[kPairs][9];    // moment matrices M_AB (row i, col j)
+// 16-byte aligned size: warp w's area starts at w * sizeof(WarpSmem), and the
+// staged Ke is copied out with 16-byte loads.
+struct alignas(16) WarpSmem {
+  // Phases A-C; Ke is staged over these in phase D (all dead by then).
+  double g[9][8][3];      // node gradients at the 8 Gauss points + centroid (index 8)
+  double wg[9][8][3];     // weighted gradients (w = detJ; centroid: 8*detJ0 for SRI)
+  double V[8][3][3];      // EAS: sum_gp xi_p(gp) g_A,i(gp)  [A][p][i]
+  double C[6];            // EAS: sum_gp xi_p xi_q / detJ  (p <= q: 00 01 02 11 12 22)
+  double idet[8];         // 1 / detJ at the Gauss points
+  double c0[9];           // detJ0 * J0^-1
   double L[9][9];         // Cholesky factor of Kaa
   double Linv[9];         // 1 / L[i][i]
   double Kua[24][9];
+  // Phase D inputs.
+  double M[kPairs][9];    // moment matrices M_AB (row i, col j)
+  double tr[kPairs];      // their traces
   double X[9][24];        // L^-1 Kau (Kaa = L L^T)
   double j0[12];          // J0^-1 (9), detJ0
 };
-// Ke staging aliases g/wg (dead after the moment accumulation): 594 >= 576.
-static_assert(sizeof(double) * 2 * 9 * kVN * 3 >= sizeof(double) * 576, "Ke alias");
+static_assert(offsetof(WarpSmem, M) >= sizeof(double) * 576, "Ke staging over g..Kua");
+static_assert(sizeof(WarpSmem) % 16 == 0, "per-warp areas and the Ke copy need 16-byte alignment");
+
+// (p, q), p <= q, of the six enhancement pairs u = 0..5.
+__device__ __forceinline__ int pp_first(int u) { return u < 3 ? 0 : (u < 5 ? 1 : 2); }
+__device__ __forceinline__ int pp_second(int u) { return u < 3 ? u : (u < 5 ? u - 2 : 2); }
 
 // 1/sqrt(d) in FP64 from an FP32 seed and two Newton-Raphson steps
 // y <- y * (1.5 - 0.5 d y^2): quadratic convergence takes the ~2^-22 seed error
@@ -62,6 +81,12 @@ __device__ __forceinline__ int pair_index(int A, int B) {  // A <= B < 11
   return A * kVN - (A * (A - 1)) / 2 + (B - A);
 }
 
+// Second virtual node B of each pair index (pairs (A, B), A <= B, A-major).
+__constant__ unsigned char kPairB[kPairs] = {
+    0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 2, 3, 4, 5, 6, 7, 8, 9,
+    10, 3, 4, 5, 6, 7, 8, 9, 10, 4, 5, 6, 7, 8, 9, 10, 5, 6, 7, 8, 9, 10, 6, 7, 8, 9, 10, 7,
+    8, 9, 10, 8, 9, 10, 9, 10, 10};
+
 // Stiffness coupling of virtual nodes (A,i) and (B,j) for the EAS element
 // (full isotropic D), from the canonical (A <= B) moment matrix.
 __device__ __forceinline__ double kval(const WarpSmem& s, double lam, double mu, int A, int i,
@@ -70,10 +95,10 @@ __device__ __forceinline__ double kval(const WarpSmem& s, double lam, double mu,
     int t = A; A = B; B = t;
     t = i; i = j; j = t;
   }
-  const double* m = s.M[pair_index(A, B)];
-  const double tr = m[0] + m[4] + m[8];
+  const int pr = pair_index(A, B);
+  const double* m = s.M[pr];
   double v = lam * m[i * 3 + j] + mu * m[j * 3 + i];
-  if (i == j) v += mu * tr;
+  if (i == j) v += mu * s.tr[pr];
   return v;
 }
 
@@ -86,31 +111,54 @@ __device__ __forceinline__ double kval_sri(const WarpSmem& s, double lam, double
     int t = a; a = b; b = t;
     t = ii; ii = jj; jj = t;
   }
-  const double* m = s.M[pair_index(a, b)];
-  const double tr = m[0] + m[4] + m[8];
+  const int pr = pair_index(a, b);
+  const double* m = s.M[pr];
   double v = mu * m[jj * 3 + ii];
-  if (ii == jj) v += mu * tr;
+  if (ii == jj) v += mu * s.tr[pr];
   // volumetric: symmetric product, use canonical order for exact symmetry
   v += lam * (s.wg[8][a][ii] * s.g[8][b][jj]);
   return v;
 }
 
+// Lame constants of isotropic_D (solid_elements.cpp:17-27), one element per
+// thread: the two FP64 divisions take one warp instruction per 32 elements
+// here instead of one per element inside the warp-per-element kernel.
+__global__ void k_lame(int n_elem, const double* __restrict__ E, const double* __restrict__ nu,
+                       double2* __restrict__ lame) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_elem; e += gridDim.x * blockDim.x) {
+    const double Ee = E[e], ne = nu[e];
+    lame[e] = make_double2(Ee * ne / ((1 + ne) * (1 - 2 * ne)), Ee / (2 * (1 + ne)));
+  }
+}
+
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __restrict__ conn,
-                   const double* __restrict__ E, const double* __restrict__ nu,
-                   const int* __restrict__ form, double* __restrict__ kbuf,
-                   ElementError* __restrict__ err) {
+                   const double2* __restrict__ lame, const int* __restrict__ form,
+                   double* __restrict__ kbuf, ElementError* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpSmem& s = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * kWarpsPerBlock;
   const double gpt = 0.57735026918962576451;  // 1/sqrt(3)
+  // Gauss point coordinates xi_p(gp) (gp = 4 i_xi + 2 i_eta + i_zeta) and the
+  // products xi_p xi_q of the six enhancement pairs.
+  __shared__ double s_par[3][8], s_pp[6][8];
+  if (threadIdx.x < 24) {
+    const int p = threadIdx.x >> 3, q = threadIdx.x & 7;
+    s_par[p][q] = ((q >> (2 - p)) & 1) ? gpt : -gpt;
+  }
+  if (threadIdx.x < 48) {
+    const int u = threadIdx.x >> 3, q = threadIdx.x & 7;
+    const double a = ((q >> (2 - pp_first(u))) & 1) ? gpt : -gpt;
+    const double b = ((q >> (2 - pp_second(u))) & 1) ? gpt : -gpt;
+    s_pp[u][q] = a * b;
+  }
+  __syncthreads();
 
   for (int e = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); e < n_elem; e += warps_total) {
     const bool sri = form != nullptr && form[e] == VSGB_SRI;
-    const double Ee = E[e], ne = nu[e];
-    const double lam = Ee * ne / ((1 + ne) * (1 - 2 * ne));
-    const double mu = Ee / (2 * (1 + ne));
+    const double2 lm = __ldg(&lame[e]);
+    const double lam = lm.x, mu = lm.y;
 
     // ── Phase A: Jacobians and gradients at the 8 Gauss points + centroid ──
     double X[8][3];
@@ -210,53 +258,83 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
         s.g[gp][n][rr] = gv;
         s.wg[gp][n][rr] = w * gv;
       }
-      if (gp < 8) {
-        // Enhancement gradients: J0^-1.row(p) * xi_p * detJ0/detJ.
-        const double scale = s.j0[9] / detJ;
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-          const double hv = s.j0[3 * p + rr] * par[p] * scale;
-          s.g[gp][8 + p][rr] = hv;
-          s.wg[gp][8 + p][rr] = w * hv;
-        }
-      }
+      if (gp < 8 && rr == 0) s.idet[gp] = id;
     }
     __syncwarp();
+    if (!sri && lane < 9) s.c0[lane] = s.j0[9] * s.j0[lane];
 
     // ── Phase B: moment matrices M_AB = sum_gp w g_A (x) g_B ──
-    const int n_entries = (sri ? kPairsSri : kPairs) * 9;
-    for (int t = lane; t < n_entries; t += 32) {
-      const int pr = t / 9, ij = t - 9 * pr;
-      const int i = ij / 3, j = ij - 3 * i;
-      // decode pair index -> (A, B) over 11 virtual nodes (SRI uses the
-      // first 36 pairs of the 8-node triangle, remapped below)
-      int A, B;
-      if (sri) {
-        // pairs of the 8x8 upper triangle in row order
-        int rem = pr;
-        A = 0;
+    // Work items with the same eight-FMA body: the 36 node pairs (x 9), and
+    // for EAS the enhancement sums V (72) and C (6).
+    const int n_items = sri ? 324 : 402;
+    for (int t = lane; t < n_items; t += 32) {
+      const double* pa;
+      const double* pb;
+      int sa, sb;
+      double* dst;
+      if (t < 324) {
+        const int pr = t / 9, ij = t - 9 * pr, i = ij / 3, j = ij - 3 * i;
+        int rem = pr, A = 0;  // pairs of the 8x8 upper triangle in row order
         while (rem >= 8 - A) {
           rem -= 8 - A;
           ++A;
         }
-        B = A + rem;
+        const int B = A + rem;
+        pa = &s.wg[0][A][i];
+        pb = &s.g[0][B][j];
+        sa = sb = 24;
+        dst = &s.M[pair_index(A, B)][ij];
+      } else if (t < 396) {
+        const int u = t - 324, A = u / 9, rem = u - 9 * A, p = rem / 3, i = rem - 3 * p;
+        pa = &s.g[0][A][i];
+        sa = 24;
+        pb = &s_par[p][0];
+        sb = 1;
+        dst = &s.V[A][p][i];
       } else {
-        int rem = pr;
-        A = 0;
-        while (rem >= kVN - A) {
-          rem -= kVN - A;
-          ++A;
-        }
-        B = A + rem;
+        const int u = t - 396;
+        pa = &s_pp[u][0];
+        pb = &s.idet[0];
+        sa = sb = 1;
+        dst = &s.C[u];
       }
       double acc = 0.0;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc = fma(s.wg[q][A][i], s.g[q][B][j], acc);
-      s.M[pair_index(A, B)][ij] = acc;
+      for (int q = 0; q < 8; ++q) acc = fma(pa[q * sa], pb[q * sb], acc);
+      *dst = acc;
     }
     __syncwarp();
+    if (!sri) {
+      // enhancement moments from V, C and c0 (the same two products per item)
+      for (int t = lane; t < 270; t += 32) {
+        double x, y, z;
+        double* dst;
+        if (t < 216) {
+          const int A = t / 27, rem = t - 27 * A, p = rem / 9, ij = rem - 9 * p;
+          const int i = ij / 3, j = ij - 3 * i;
+          x = s.V[A][p][i];
+          y = s.c0[3 * p + j];
+          z = 1.0;
+          dst = &s.M[pair_index(A, 8 + p)][ij];
+        } else {
+          const int u = (t - 216) / 9, ij = (t - 216) - 9 * u, i = ij / 3, j = ij - 3 * i;
+          const int p = pp_first(u), q = pp_second(u);
+          x = s.c0[3 * p + i];
+          y = s.c0[3 * q + j];
+          z = s.C[u];
+          dst = &s.M[pair_index(8 + p, 8 + q)][ij];
+        }
+        *dst = x * y * z;
+      }
+      __syncwarp();
+    }
+    // traces, once per pair (SRI: only the pairs of the 8 element nodes hold
+    // moments)
+    for (int t = lane; t < kPairs; t += 32)
+      if (!sri || kPairB[t] < 8) s.tr[t] = s.M[t][0] + s.M[t][4] + s.M[t][8];
+    __syncwarp();
 
-    double* ke_s = &s.g[0][0][0];  // alias (g/wg dead after this point except SRI centroid)
+    double* ke_s = &s.g[0][0][0];  // Ke staging over g..Kua (EAS only; SRI writes global)
     if (!sri) {
       // ── Phase C: Kaa Cholesky (lane 0) and Kua ──
       for (int t = lane; t < 24 * 9; t += 32) {
@@ -406,15 +484,18 @@ size_t element_smem_bytes() { return sizeof(WarpSmem) * kWarpsPerBlock; }
 
 void launch_chexa8_stiffness(int n_elem, const double* xyz, const int* conn, const double* E,
                              const double* nu, const int* form, double* kbuf, ElementError* err,
-                             int num_sms, cudaStream_t s) {
+                             double* lame, int num_sms, cudaStream_t s) {
   if (n_elem <= 0) return;
+  double2* lm = reinterpret_cast<double2*>(lame);
+  k_lame<<<grid_for(n_elem, kThreads, num_sms * 8), kThreads, 0, s>>>(n_elem, E, nu, lm);
+  VSGB_LAUNCH_CHECK();
   const size_t smem = element_smem_bytes();
   VSGB_CUDA(cudaFuncSetAttribute(k_chexa8_stiffness, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
   const int blocks_needed = (n_elem + kWarpsPerBlock - 1) / kWarpsPerBlock;
   const int grid = blocks_needed < num_sms * 8 ? blocks_needed : num_sms * 8;
-  k_chexa8_stiffness<<<grid, kWarpsPerBlock * 32, smem, s>>>(n_elem, xyz, conn, E, nu, form,
-                                                             kbuf, err);
+  k_chexa8_stiffness<<<grid, kWarpsPerBlock * 32, smem, s>>>(n_elem, xyz, conn, lm, form, kbuf,
+                                                             err);
   VSGB_LAUNCH_CHECK();
 }
 

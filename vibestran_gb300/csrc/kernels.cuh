@@ -18,9 +18,10 @@ __device__ __forceinline__ void record_element_error(ElementError* err, int e, i
 }
 
 size_t element_smem_bytes();
+// lame: scratch of 2 * n_elem doubles (per-element lambda, mu).
 void launch_chexa8_stiffness(int n_elem, const double* xyz, const int* conn, const double* E,
                              const double* nu, const int* form, double* kbuf, ElementError* err,
-                             int num_sms, cudaStream_t s);
+                             double* lame, int num_sms, cudaStream_t s);
 // out[e] = -lam_e^T (K_e / E_e) u_e; with lam2/out2 non-null the same pass
 // also gives out2[e] = -lam2_e^T (K_e / E_e) u_e (K_e u_e is formed once).
 void launch_element_sensitivity(int n_elem, const int* conn, const int* eq3, const double* E,

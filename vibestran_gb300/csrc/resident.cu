@@ -633,12 +633,12 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
   const int wgrid = (ns + 7) / 8;
   k_fix_padding<<<wgrid, 256, 0, s>>>(nb, ns, B.slice_ptr.ptr, B.rowlen.ptr, B.cols.ptr);
   VSGB_LAUNCH_CHECK();
-  DevBuf<int> mm;
-  mm.reserve(2 * static_cast<size_t>(ns));
-  k_slice_minmax<<<wgrid, 256, 0, s>>>(ns, B.slice_ptr.ptr, B.cols.ptr, mm.ptr);
+  P.slice_mm.reserve(2 * static_cast<size_t>(ns));
+  k_slice_minmax<<<wgrid, 256, 0, s>>>(ns, B.slice_ptr.ptr, B.cols.ptr, P.slice_mm.ptr);
   VSGB_LAUNCH_CHECK();
   std::vector<int> hmm(2 * static_cast<size_t>(ns));
-  VSGB_CUDA(cudaMemcpyAsync(hmm.data(), mm.ptr, sizeof(int) * 2 * ns, cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaMemcpyAsync(hmm.data(), P.slice_mm.ptr, sizeof(int) * 2 * ns,
+                            cudaMemcpyDeviceToHost, s));
   VSGB_CUDA(cudaStreamSynchronize(s));
   std::vector<int> win(2 * static_cast<size_t>(G));
   int max_win = 0;

@@ -18,6 +18,7 @@ struct ResidentPlan {
   int max_slices = 0;               // slices of the largest CTA range
   DevBuf<int> cta_slice;            // ctas + 1: slice range of each CTA
   DevBuf<int> cta_win;              // 2 * ctas: [first, last] block column per CTA
+  DevBuf<int> slice_mm;             // 2 * nslices: column range per slice (planning scratch)
   DevBuf<double> partials;          // 2 barrier slots x ctas x up to 4 values
   DevBuf<unsigned> barrier;         // monotonic arrival counter
   DevBuf<int> abort_flag;           // set by a barrier that gave up waiting
