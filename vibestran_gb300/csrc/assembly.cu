@@ -533,11 +533,18 @@ k_block_fill(int n_nodes, const int* __restrict__ conn, const int* __restrict__ 
       }
     }
     // FP32 difference form: the diagonal slot holds the sum of the row's
-    // blocks (ascending neighbour order).
-    if (v32 && lane < 9) {
+    // blocks.  Lane 3k+h (k < 9) adds blocks h, h+3, ... of entry k, then the
+    // three partial sums are added in fixed order (every FP64 warp
+    // instruction costs the same pipe time whatever its active lanes, so the
+    // sum is spread over 27 lanes).
+    if (v32) {
+      const int k = lane / 3, h = lane - 3 * k;
       double t = 0.0;
-      for (int u = 0; u < U; ++u) t += s.acc[u][lane];
-      s.rsum[lane] = t;
+      if (lane < 27)
+        for (int u = h; u < U; u += 3) t += s.acc[u][k];
+      const double t1 = __shfl_down_sync(0xffffffffu, t, 1);
+      const double t2 = __shfl_down_sync(0xffffffffu, t, 2);
+      if (lane < 27 && h == 0) s.rsum[k] = (t + t1) + t2;
     }
     __syncwarp();
     const int sl = R >> 3, ln0 = (R & 7) * 4;

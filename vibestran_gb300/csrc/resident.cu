@@ -109,14 +109,17 @@ __device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, in
 }
 
 // Grid-wide sum of NV doubles: CTA sums -> partial slot -> barrier -> fixed
-// order sum by warp 0 of every CTA (bitwise identical in all CTAs).
+// order sum by warp 0 of every CTA (bitwise identical in all CTAs), after which
+// thread 0 runs fin(totals, ok) — the scalar recurrence, which writes its
+// results to shared memory — and one CTA barrier publishes them.
 // Per-thread partials are summed over the warp in their own precision A (FP32
 // in the FP32 solve: GB300 runs FP64 at 1/58 of the FP32 rate), then the
-// kResWarps warp sums and the CTA partials are added in FP64, in fixed order.
-template <typename A, int NV>
+// kResWarps warp sums (a fixed shuffle tree in warp 0) and the CTA partials
+// are added in FP64.
+template <typename A, int NV, typename Fin>
 __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned* count,
                                unsigned& target, int* abort_flag, double* sm, int* s_ok,
-                               double (&tot)[NV]) {
+                               Fin&& fin) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
@@ -125,13 +128,17 @@ __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned*
     for (int k = 0; k < NV; ++k) sm[wid * NV + k] = static_cast<double>(v[k]);
   __syncthreads();
   double* part = partials + static_cast<size_t>(slot) * gridDim.x * NV;
-  if (threadIdx.x == 0) {
+  if (wid == 0) {
+    double w[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double s = 0.0;
-      for (int w = 0; w < kResWarps; ++w) s += sm[w * NV + k];
-      part[blockIdx.x * NV + k] = s;
-    }
+    for (int k = 0; k < NV; ++k) w[k] = lane < kResWarps ? sm[lane * NV + k] : 0.0;
+#pragma unroll
+    for (int o = kResWarps / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = w[k];
   }
   const bool ok = grid_sync(count, target, abort_flag, s_ok);
   if (threadIdx.x < 32) {
@@ -143,27 +150,22 @@ __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned*
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = 0.0;
     for (unsigned c0 = threadIdx.x; c0 < gridDim.x; c0 += 32 * kRound) {
-      double v[kRound][NV];
+      double u[kRound][NV];
 #pragma unroll
-      for (int u = 0; u < kRound; ++u) {
-        const unsigned c = c0 + 32u * u;
+      for (int r = 0; r < kRound; ++r) {
+        const unsigned c = c0 + 32u * r;
 #pragma unroll
-        for (int k = 0; k < NV; ++k) v[u][k] = c < gridDim.x ? __ldcg(&part[c * NV + k]) : 0.0;
+        for (int k = 0; k < NV; ++k) u[r][k] = c < gridDim.x ? __ldcg(&part[c * NV + k]) : 0.0;
       }
 #pragma unroll
-      for (int u = 0; u < kRound; ++u)
+      for (int r = 0; r < kRound; ++r)
 #pragma unroll
-        for (int k = 0; k < NV; ++k) acc[k] += v[u][k];
+        for (int k = 0; k < NV; ++k) acc[k] += u[r][k];
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = warp_sum(acc[k]);
-    if (threadIdx.x == 0)
-#pragma unroll
-      for (int k = 0; k < NV; ++k) sm[32 * NV + k] = acc[k];
+    if (threadIdx.x == 0) fin(acc, ok);
   }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NV; ++k) tot[k] = sm[32 * NV + k];
   __syncthreads();
   return ok;
 }
@@ -260,39 +262,43 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     acc2[0] = rfma(rv, rv, acc2[0]);
     acc2[1] = rfma(rv, zv, acc2[1]);
   }
-  double tot2[2];
-  ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok, tot2);
-  slot ^= 1;
   // The scalar recurrence runs on thread 0 only (FP64 sqrt / division are long
-  // instruction sequences on GB300's FP64 pipe) and is broadcast through
-  // shared memory: s_sc = {alpha, beta}.
+  // instruction sequences on GB300's FP64 pipe), inside the reductions, and is
+  // broadcast through shared memory: s_sc = {alpha, beta}.
   __shared__ double s_sc[2];
   __shared__ int s_flags;
-  double norm_b = 0.0, rz = 0.0, rel = 1.0, pAp = 0.0, rr = 0.0, beta = 0.0, alpha = 0.0;
+  // Recurrence scalars: thread 0 only, in shared memory so that they hold no
+  // registers of the other threads across the SpMV.
+  __shared__ double norm_b, rz, rel, pAp, rr, beta, alpha;
+  if (tid == 0) {
+    norm_b = rz = pAp = rr = beta = alpha = 0.0;
+    rel = 1.0;
+  }
   int flags = 0, it = 0;
   T* p_old = a.p4a;
   T* p_new = a.p4b;
-  if (tid == 0) {
-    norm_b = sqrt(fabs(tot2[0]));
-    rz = tot2[1];
-    rr = tot2[0];
-    if (!ok) {
-      flags = kFlagDone | kFlagAbort;
-    } else if (norm_b < 1e-300) {
-      flags = kFlagDone | kFlagZeroRhs | kFlagConverged;
-      rel = 0.0;
-    } else if (!(rz > 0.0)) {
-      flags = kFlagDone | kFlagNonPosRz;
-    }
-    s_flags = flags;
-    s_sc[1] = 0.0;
-  }
-  __syncthreads();
+  ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok,
+                            [&](const double (&t)[2], bool good) {
+                              norm_b = sqrt(fabs(t[0]));
+                              rz = t[1];
+                              rr = t[0];
+                              if (!good) {
+                                flags = kFlagDone | kFlagAbort;
+                              } else if (norm_b < 1e-300) {
+                                flags = kFlagDone | kFlagZeroRhs | kFlagConverged;
+                                rel = 0.0;
+                              } else if (!(rz > 0.0)) {
+                                flags = kFlagDone | kFlagNonPosRz;
+                              }
+                              s_flags = flags;
+                              s_sc[1] = 0.0;
+                            });
+  slot ^= 1;
   flags = s_flags;
 
   while (!(flags & kFlagDone)) {
     // ── phase 1: x = z + beta p over the window, Ap = K x, own p update ──
-    const T tb = static_cast<T>(beta);
+    const T tb = static_cast<T>(s_sc[1]);
     if (tid == 0) s_next = kResWarps;
     if (!kWindow) __syncthreads();
     if (kWindow) {
@@ -421,22 +427,20 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       s = warp_sum(s);
       if (lane == 0) accp[0] = s;
     }
-    double totp[1];
-    ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok, totp);
+    ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok,
+                              [&](const double (&t)[1], bool good) {
+                                pAp = t[0];
+                                if (!good) {
+                                  flags |= kFlagDone | kFlagAbort;
+                                } else if (!(pAp > 0.0)) {
+                                  flags |= kFlagDone | kFlagBreakdown;
+                                } else {
+                                  alpha = rz / pAp;
+                                }
+                                s_flags = flags;
+                                s_sc[0] = alpha;
+                              });
     slot ^= 1;
-    if (tid == 0) {
-      pAp = totp[0];
-      if (!ok) {
-        flags |= kFlagDone | kFlagAbort;
-      } else if (!(pAp > 0.0)) {
-        flags |= kFlagDone | kFlagBreakdown;
-      } else {
-        alpha = rz / pAp;
-      }
-      s_flags = flags;
-      s_sc[0] = alpha;
-    }
-    __syncthreads();
     flags = s_flags;
     if (flags & kFlagDone) break;
     const T ta = static_cast<T>(s_sc[0]);
@@ -453,31 +457,29 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       acc2[0] = rfma(rv, zv, acc2[0]);
       acc2[1] = rfma(rv, rv, acc2[1]);
     }
-    ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok, tot2);
-    slot ^= 1;
     ++it;
-    if (tid == 0) {
-      if (!ok) {
-        flags |= kFlagDone | kFlagAbort;
-      } else {
-        rr = tot2[1];
-        rel = sqrt(fabs(rr)) / norm_b;
-        if (rel < a.tol) {
-          flags |= kFlagDone | kFlagConverged;
-          beta = 0.0;
-        } else {
-          beta = tot2[0] / rz;
-          if (it >= a.max_iters) flags |= kFlagDone | kFlagMaxIters;
-        }
-        rz = tot2[0];
-      }
-      s_flags = flags;
-      s_sc[1] = beta;
-    }
-    __syncthreads();
+    ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok,
+                              [&](const double (&t)[2], bool good) {
+                                if (!good) {
+                                  flags |= kFlagDone | kFlagAbort;
+                                } else {
+                                  rr = t[1];
+                                  rel = sqrt(fabs(rr)) / norm_b;
+                                  if (rel < a.tol) {
+                                    flags |= kFlagDone | kFlagConverged;
+                                    beta = 0.0;
+                                  } else {
+                                    beta = t[0] / rz;
+                                    if (it >= a.max_iters) flags |= kFlagDone | kFlagMaxIters;
+                                  }
+                                  rz = t[0];
+                                }
+                                s_flags = flags;
+                                s_sc[1] = beta;
+                              });
+    slot ^= 1;
     flags = s_flags;
     if (flags & kFlagAbort) break;
-    beta = s_sc[1];
     T* t = p_old;
     p_old = p_new;
     p_new = t;
