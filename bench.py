@@ -242,6 +242,43 @@ def extra_adjoint(B, C, device, n_fd=32):
             "central_fd_max_rel_err": fd_err, "fd_elements": n_fd}
 
 
+def extra_stress(B, C, device):
+    """CHEXA8 stress recovery (centroid + 8 corners, von Mises) of the 84k
+    cantilever's mixed solution on the GPU, from the device-resident
+    displacements, against the oracle's recovery of the same displacements
+    (vectorised numpy over the elements, one host thread)."""
+    from oracle import oracle as O
+    m = C.cantilever_84k()
+    eq6, n = B.build_dof_map(m)
+    F = B.apply_forces(m, eq6, n)
+    be = _mixed_backend(B, device)
+    asm = B.ChexaAssembler(be)
+    asm.upload(m, eq6, n)
+    asm.assemble_resident()
+    asm.upload_rhs(F)
+    asm.solve_resident()
+    u = asm.download()
+    asm.solid_stress()  # warm-up
+    kern, call = [], []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        cen, nodal, ms = asm.solid_stress()
+        call.append(time.perf_counter() - t0)
+        kern.append(ms)
+    be.close()
+    t0 = time.perf_counter()
+    oc, on = O.solid_stress(m, eq6, u)
+    t_oracle = time.perf_counter() - t0
+    err = max(float(np.abs(cen - oc).max() / np.abs(oc).max()),
+              float(np.abs(nodal - on).max() / np.abs(on).max()))
+    return {"workload": "cantilever_84k", "elements": m.n_elem, "points_per_element": 9,
+            "kernel_ms": float(np.median(kern)),
+            "call_ms_with_d2h": 1e3 * float(np.median(call)),
+            "d2h_bytes": int(cen.nbytes + nodal.nbytes),
+            "oracle_s": t_oracle, "max_rel_err_vs_oracle": err,
+            "max_von_mises_pa": float(cen[:, 6].max())}
+
+
 def extra_jitter(B, C, device, uniform):
     """Jittered (U(+-0.2 h) interior nodes) heterogeneous (log-uniform E)
     84 000-element cantilever: FP64 and mixed iteration counts against the
@@ -481,6 +518,7 @@ def main():
         be_e2e.close()
         extras = {"multi_rhs_16": extra_multi_rhs(B, C, device),
                   "adjoint_250k": extra_adjoint(B, C, device),
+                  "stress_84k": extra_stress(B, C, device),
                   "jitter_84k": extra_jitter(B, C, device,
                                              {"fp64": st_fp64.iterations, "mixed": it_mixed})}
     line = {

@@ -195,6 +195,18 @@ int vsgb_adjoint_gradients(vsgb_ctx* ctx, const double* F, const double* dJdu, d
                            double* lambda_out, double* dCdE_out, double* dJdE_out,
                            vsgb_stats* stats);
 
+/* CHEXA8 stresses of the resident mesh (LinearStaticSolver::recover_results,
+ * solid branch, src/solver/linear_static.cpp:1059-1195): for every element the
+ * stress at the centroid and at its 8 corner nodes, each as (sx, sy, sz, sxy,
+ * syz, szx, von_mises), sigma = D B u_e of the plain trilinear element.  u:
+ * n_dof host displacements, or NULL for load case k of the last solve on this
+ * context.  centroid_out: n_elem*7 doubles; nodal_out: n_elem*8*7 doubles
+ * (corner j of element e at (8e+j)*7) or NULL; kernel_ms (may be NULL): device
+ * time of the recovery kernels.  No TEMP loads are on this path, so the thermal
+ * strain of solid_sigma_from_B (:186-196) is zero. */
+int vsgb_solid_stress(vsgb_ctx* ctx, const double* u, int k, double* centroid_out,
+                      double* nodal_out, double* kernel_ms);
+
 /* ── measurement helpers ────────────────────────────────────────────────── */
 
 /* Events on the context stream, synchronised on both sides. */

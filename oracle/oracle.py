@@ -374,3 +374,64 @@ def fd_gradient(model, eq6, K: Csr, u, C, elems, h=1e-4, kes=None) -> np.ndarray
             dJ.append(C.T @ du)
         out[t] = (dJ[0] - dJ[1]) / (2.0 * h * model.E[e])
     return out
+
+
+# ── CHEXA8 stress recovery ────────────────────────────────────────────────
+# LinearStaticSolver::recover_results, solid branch (src/solver/linear_static.cpp):
+# u_e from the element's global DOFs with constrained DOFs zero (:661-672);
+# sigma = D (B u_e - eps_th) at the centroid and at the 8 corner nodes
+# (eval_chexa8 at :1059-1118, points at :1164-1185), D = solid_constitutive_matrix
+# (:119-138), B rows xx, yy, zz, xy, yz, zx with engineering shears (:1088-1113),
+# von Mises as solid_von_mises (:140-150).  No TEMP loads are on this path, so
+# the point temperature equals the reference temperature and eps_th = 0
+# (solid_sigma_from_B, :186-196).
+
+# Corner coordinates in CHEXA8 node order (kHexCoords at :1165-1174).
+HEX_CORNERS = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
+                        [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], np.float64)
+
+
+def _hex_dN(xi):
+    """dN/d(xi, eta, zeta) (3, 8) of CHexa8::shape_functions
+    (src/elements/solid_elements.cpp:76-93) at one point."""
+    s = HEX_CORNERS
+    f = 1.0 + s * np.asarray(xi, np.float64)  # (8, 3)
+    return 0.125 * np.stack([s[:, 0] * f[:, 1] * f[:, 2],
+                             s[:, 1] * f[:, 0] * f[:, 2],
+                             s[:, 2] * f[:, 0] * f[:, 1]])
+
+
+def solid_stress(model, eq6, u):
+    """Centroid and corner-node stresses of every CHEXA8 element.
+
+    Returns (centroid (M, 7), nodal (M, 8, 7)), each row
+    (sx, sy, sz, sxy, syz, szx, von_mises)."""
+    idx = element_dofs(model, eq6)
+    u = np.asarray(u, np.float64)
+    ue = np.where(idx >= 0, u[np.maximum(idx, 0)], 0.0).reshape(-1, 8, 3)
+    X = np.asarray(model.xyz, np.float64)[model.conn]            # (M, 8, 3)
+    E = np.asarray(model.E, np.float64)
+    nu = np.asarray(model.nu, np.float64)
+    lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    mu = E / (2.0 * (1.0 + nu))
+
+    def at(xi):
+        dN = _hex_dN(xi)                                          # (3, 8)
+        J = np.einsum("in,enc->eic", dN, X)                       # rows d/dxi_i, cols x,y,z
+        g = np.einsum("eij,jn->ein", np.linalg.inv(J), dN)        # (M, 3, 8): dN/dx, dy, dz
+        du = np.einsum("ein,enc->eci", g, ue)                     # du_c / dx_i
+        exx, eyy, ezz = du[:, 0, 0], du[:, 1, 1], du[:, 2, 2]
+        gxy = du[:, 0, 1] + du[:, 1, 0]
+        gyz = du[:, 1, 2] + du[:, 2, 1]
+        gzx = du[:, 2, 0] + du[:, 0, 2]
+        tr = exx + eyy + ezz
+        s = np.stack([lam * tr + 2.0 * mu * exx, lam * tr + 2.0 * mu * eyy,
+                      lam * tr + 2.0 * mu * ezz, mu * gxy, mu * gyz, mu * gzx], axis=1)
+        vm = np.sqrt(0.5 * ((s[:, 0] - s[:, 1]) ** 2 + (s[:, 1] - s[:, 2]) ** 2 +
+                            (s[:, 2] - s[:, 0]) ** 2 +
+                            6.0 * (s[:, 3] ** 2 + s[:, 4] ** 2 + s[:, 5] ** 2)))
+        return np.concatenate([s, vm[:, None]], axis=1)
+
+    centroid = at(np.zeros(3))
+    nodal = np.stack([at(HEX_CORNERS[k]) for k in range(8)], axis=1)
+    return centroid, nodal

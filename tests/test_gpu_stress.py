@@ -1,0 +1,103 @@
+"""GPU CHEXA8 stress recovery (centroid + corner nodes, von Mises) against the
+oracle's restatement of linear_static.cpp:1059-1195 and the reference's
+single-hex axial expectations."""
+import numpy as np
+import pytest
+
+from conftest import model_from_spec
+
+pytestmark = pytest.mark.gpu
+
+# FP64 throughout; the GPU and the oracle differ only in summation order.
+REL = 1e-10
+
+
+def _close(a, b, rel=REL):
+    scale = max(np.abs(b).max(), 1e-300)
+    return np.abs(np.asarray(a) - np.asarray(b)).max() <= rel * scale
+
+
+@pytest.mark.parametrize("isop", [0, 1])
+def test_axial_single_hex(vsgb, oracle, known, isop):
+    spec = known["hexa_bar_axial_extension"]
+    st = spec["expect"]["stress"]
+    m = model_from_spec(spec, isop)
+    eq6, n = vsgb.build_dof_map(m)
+    F = vsgb.apply_forces(m, eq6, n)
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-12, 1000)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    u = asm.solve(F)
+    cen, nodal, _ = asm.solid_stress()  # load case 0 of the last solve
+    for s in [cen[0]] + list(nodal[0]):
+        assert abs(s[2] - st["sz"]) <= st["sz_rel_tol"] * st["sz"]
+        assert abs(s[0] - st["sx"]) <= st["sx_sy_abs_tol"]
+        assert abs(s[1] - st["sy"]) <= st["sx_sy_abs_tol"]
+        assert abs(s[6] - st["sz"]) <= st["sz_rel_tol"] * st["sz"]
+    oc, on = oracle.solid_stress(m, eq6, u)
+    assert _close(cen, oc) and _close(nodal, on)
+    be.close()
+
+
+@pytest.mark.parametrize("case", ["jitter_hetero", "mixed_forms", "cantilever_1500"])
+def test_stress_matches_oracle(vsgb, oracle, case):
+    from vibestran_gb300 import cantilever as C
+    if case == "jitter_hetero":
+        m = C.small_block(8, 4, 3, 0.05, seed=11, jitter=0.2, hetero=True)
+    elif case == "mixed_forms":
+        m = C.small_block(6, 3, 3, 0.1, seed=2, jitter=0.1)
+        m.form[::2] = C.SRI
+    else:
+        m = C.cantilever_1500()
+    eq6, n = vsgb.build_dof_map(m)
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-10, 20000)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    # host displacements (any field: recovery is linear in u)
+    u = np.random.default_rng(7).normal(0.0, 1e-4, n)
+    cen, nodal, ms = asm.solid_stress(u)
+    oc, on = oracle.solid_stress(m, eq6, u)
+    assert _close(cen, oc) and _close(nodal, on)
+    assert ms > 0.0
+    # the centroid-only call returns the same centroid values
+    cen2, none, _ = asm.solid_stress(u, nodal=False)
+    assert none is None and np.array_equal(cen, cen2)
+    be.close()
+
+
+def test_stress_needs_a_solution(vsgb):
+    from vibestran_gb300 import cantilever as C
+    m = C.small_block(3, 2, 2, 0.1)
+    eq6, n = vsgb.build_dof_map(m)
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-10, 1000)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    with pytest.raises(vsgb.SolverError):
+        asm.solid_stress()
+    be.close()
+
+
+def test_stress_full_size_84k(vsgb, oracle):
+    """84 000-element cantilever: stresses of the mixed solution recovered on
+    the GPU from the device-resident displacements, against the oracle's
+    recovery from the same displacements."""
+    from vibestran_gb300 import cantilever as C
+    m = C.cantilever_84k()
+    eq6, n = vsgb.build_dof_map(m)
+    F = vsgb.apply_forces(m, eq6, n)
+    be = vsgb.Gb300MixedPcgSolverBackend.try_create(1e-4, 20000)
+    be.set_option(vsgb.OPT_INNER_TOL, 1e-3)
+    asm = vsgb.ChexaAssembler(be)
+    asm.upload(m, eq6, n)
+    asm.assemble_resident()
+    asm.upload_rhs(F)
+    asm.solve_resident()
+    u = asm.download()
+    cen, nodal, ms = asm.solid_stress()
+    oc, on = oracle.solid_stress(m, eq6, u)
+    assert _close(cen, oc) and _close(nodal, on)
+    # bending: the clamped end carries the largest von Mises stress
+    i_max = int(np.argmax(cen[:, 6]))
+    x_el = m.xyz[m.conn[i_max]][:, 0].mean()
+    assert x_el < 0.1 * m.xyz[:, 0].max()
+    be.close()

@@ -185,3 +185,43 @@ def C_hash(K):
     h.update(np.ascontiguousarray(K.row_ptr, np.int32).tobytes())
     h.update(np.ascontiguousarray(K.col_ind, np.int32).tobytes())
     return h.hexdigest()
+
+
+@pytest.mark.parametrize("isop", [0, 1])
+def test_hexa_axial_stress(oracle, known, isop):
+    """Element stresses of the single-hex axial case against the reference's
+    e2e expectations (chexa8_axial_force.expected.json): sigma_z = F/A at the
+    centroid and at every corner (the trilinear field is exact), no lateral
+    stress, von Mises = sigma_z."""
+    spec = known["hexa_bar_axial_extension"]
+    st = spec["expect"]["stress"]
+    m = model_from_spec(spec, isop)
+    eq6, n, K, F, u = oracle.solve_model(m)
+    cen, nodal = oracle.solid_stress(m, eq6, u)
+    for s in [cen[0]] + list(nodal[0]):
+        assert abs(s[2] - st["sz"]) <= st["sz_rel_tol"] * st["sz"]
+        assert abs(s[0] - st["sx"]) <= st["sx_sy_abs_tol"]
+        assert abs(s[1] - st["sy"]) <= st["sx_sy_abs_tol"]
+        assert abs(s[6] - st["sz"]) <= st["sz_rel_tol"] * st["sz"]
+
+
+def test_rigid_motion_gives_zero_stress(oracle):
+    """A rigid translation plus a small rigid rotation of a distorted mesh
+    strains nothing (the reference's rigid-body stress checks,
+    tests/integration/test_integration.cpp:182-215)."""
+    from vibestran_gb300 import cantilever as C
+    m = C.small_block(3, 2, 2, 0.1, seed=4, jitter=0.2, hetero=True)
+    m.spc_nodes = np.zeros(0, np.int32)
+    m.spc_mask = np.zeros(0, np.int32)
+    eq6, n = oracle.dof_map(m)
+    w = np.array([1e-3, -2e-3, 1.5e-3])
+    disp = np.array([1e-2, -3e-3, 5e-3]) + np.cross(w, m.xyz)
+    u = np.zeros(n)
+    for i in range(m.xyz.shape[0]):
+        for d in range(3):
+            if eq6[i, d] >= 0:
+                u[eq6[i, d]] = disp[i, d]
+    cen, nodal = oracle.solid_stress(m, eq6, u)
+    scale = float(np.max(m.E)) * 1e-3  # stress of a strain of 1e-3
+    assert np.abs(cen).max() <= 1e-9 * scale
+    assert np.abs(nodal).max() <= 1e-9 * scale

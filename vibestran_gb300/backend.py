@@ -59,7 +59,7 @@ OPT_ADAPTIVE_INNER = 12
 
 # The symbols include/vsgb.h declares (checked by tests against the .so).
 EXPORTS = (
-    "vsgb_rhs_stats", "vsgb_adjoint_gradients",
+    "vsgb_rhs_stats", "vsgb_adjoint_gradients", "vsgb_solid_stress",
     "vsgb_create", "vsgb_destroy", "vsgb_set_option", "vsgb_last_error", "vsgb_device_name",
     "vsgb_backend_name", "vsgb_solve_csr", "vsgb_build_dof_map", "vsgb_apply_forces",
     "vsgb_assemble_chexa8", "vsgb_copy_csr_lower", "vsgb_solve_assembled", "vsgb_mesh_upload",
@@ -138,6 +138,7 @@ def load_library(build_if_missing: bool = False):
     L.vsgb_kernel_launches.argtypes = [vp]
     L.vsgb_kernel_launches.restype = c_ll
     L.vsgb_adjoint_gradients.argtypes = [vp, _f64p, vp, vp, vp, vp, vp, ctypes.POINTER(VsgbStats)]
+    L.vsgb_solid_stress.argtypes = [vp, vp, c_int, _f64p, vp, ctypes.POINTER(c_dbl)]
     L.vsgb_rhs_stats.argtypes = [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_dbl),
                                  ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.vsgb_pcg_solve_noalloc.argtypes = [c_int, c_int, vp, vp, vp, vp, vp, c_dbl, c_int, vp,
@@ -400,6 +401,21 @@ class ChexaAssembler:
         self.backend.context.check(
             load_library().vsgb_solution_download(self.backend.context.ptr, u))
         return u if nrhs == 1 else u.reshape(nrhs, self.n).T.copy()
+
+    def solid_stress(self, u=None, k=0, nodal=True):
+        """CHEXA8 stresses (linear_static.cpp:1059-1195): returns (centroid
+        (n_elem, 7), nodal (n_elem, 8, 7) or None, kernel ms), columns sx, sy,
+        sz, sxy, syz, szx, von Mises.  u: host displacements, or None for load
+        case k of the last solve."""
+        cen = np.zeros((self.n_elem, 7))
+        nod = np.zeros((self.n_elem, 8, 7)) if nodal else None
+        u_in = None if u is None else np.ascontiguousarray(u, np.float64)
+        ms = ctypes.c_double(0.0)
+        self.backend.context.check(load_library().vsgb_solid_stress(
+            self.backend.context.ptr,
+            None if u_in is None else u_in.ctypes.data_as(ctypes.c_void_p), k, cen,
+            None if nod is None else nod.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ms)))
+        return cen, nod, ms.value
 
     def adjoint_gradients(self, F, dJdu=None, with_adjoint=False):
         """Compliance and linear-response gradients w.r.t. every element's E

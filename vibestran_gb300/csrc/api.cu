@@ -46,7 +46,9 @@ struct vsgb_ctx {
 
   // right-hand sides / solutions
   int nrhs = 0;
+  int u_cases = 0;                     // load cases held in u by the last solve
   DevBuf<double> f, u;
+  DevBuf<double> u_in, stress_c, stress_n;  // stress recovery staging
   // staging of an uploaded CSR (solve_csr)
   DevBuf<int> in_rp, in_ci;
   DevBuf<double> in_v;
@@ -200,6 +202,7 @@ void run_batched(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
     st.spmv_bytes = c->eng->spmv_bytes(c->precision);
     *stats = st;
   }
+  c->u_cases = nrhs;
 }
 
 // Auto mode batches from the load-case count where one 16-wide sweep beats
@@ -270,6 +273,7 @@ void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
     st.spmv_bytes = c->eng->spmv_bytes(c->precision);
     *stats = st;
   }
+  c->u_cases = nrhs;
 }
 
 void upload(void* dst, const void* src, size_t bytes, cudaStream_t s) {
@@ -465,6 +469,7 @@ int vsgb_mesh_upload(vsgb_ctx* c, int n_nodes, const double* node_xyz, const int
         (n_elem > 0 && (!conn || !E || !nu)))
       throw Error(VSGB_ERR_INVALID, "vsgb_mesh_upload: invalid argument");
     if (n_elem > INT_MAX / 8) throw Error(VSGB_ERR_LIMIT, "too many elements");
+    c->u_cases = 0;
     // Every index a kernel will dereference is range-checked here, on the host.
     for (long long k = 0; k < 8LL * n_elem; ++k)
       if (conn[k] < 0 || conn[k] >= n_nodes)
@@ -617,6 +622,48 @@ int vsgb_solve_assembled(vsgb_ctx* c, const double* F, int nrhs, double* u_out,
   rc = vsgb_solve_resident(c, stats);
   if (rc != VSGB_OK) return rc;
   return vsgb_solution_download(c, u_out);
+}
+
+int vsgb_solid_stress(vsgb_ctx* c, const double* u, int k, double* centroid_out,
+                      double* nodal_out, double* kernel_ms) {
+  return guarded(c, [&] {
+    if (!c->mesh_ok) throw Error(VSGB_ERR_STATE, "no mesh uploaded");
+    if (!centroid_out) throw Error(VSGB_ERR_INVALID, "null output");
+    cudaStream_t s = c->stream;
+    const int n = c->n_dof;
+    const double* du = nullptr;
+    if (u) {
+      c->u_in.reserve(static_cast<size_t>(n > 0 ? n : 1));
+      upload(c->u_in.ptr, u, sizeof(double) * n, s);
+      du = c->u_in.ptr;
+    } else {
+      if (k < 0 || k >= c->u_cases || c->K.n != n)
+        throw Error(VSGB_ERR_STATE, "no solution of load case " + std::to_string(k) +
+                                        " on this context");
+      du = c->u.ptr + static_cast<size_t>(k) * n;
+    }
+    const size_t ne = static_cast<size_t>(c->n_elem);
+    c->stress_c.reserve(7 * ne + 1);
+    if (nodal_out) c->stress_n.reserve(56 * ne + 1);
+    c->lame.reserve(2 * ne + 1);
+    VSGB_CUDA(cudaEventRecord(c->ev[2], s));
+    vsgb::launch_solid_stress(c->n_elem, c->xyz.ptr, c->conn.ptr, c->eq3.ptr, c->E.ptr, c->nu.ptr,
+                              du, n, c->lame.ptr, c->stress_c.ptr,
+                              nodal_out ? c->stress_n.ptr : nullptr, c->num_sms, s);
+    VSGB_CUDA(cudaEventRecord(c->ev[3], s));
+    c->eng->add_launches(2);
+    VSGB_CUDA(cudaMemcpyAsync(centroid_out, c->stress_c.ptr, sizeof(double) * 7 * ne,
+                              cudaMemcpyDeviceToHost, s));
+    if (nodal_out)
+      VSGB_CUDA(cudaMemcpyAsync(nodal_out, c->stress_n.ptr, sizeof(double) * 56 * ne,
+                                cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+    if (kernel_ms) {
+      float ms = 0.f;
+      VSGB_CUDA(cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]));
+      *kernel_ms = ms;
+    }
+  });
 }
 
 int vsgb_element_sensitivity(vsgb_ctx* c, const double* u, const double* lambda,

@@ -482,13 +482,20 @@ __global__ void k_element_sensitivity(int n_elem, const int* __restrict__ conn,
 
 size_t element_smem_bytes() { return sizeof(WarpSmem) * kWarpsPerBlock; }
 
+void launch_lame(int n_elem, const double* E, const double* nu, double* lame, int num_sms,
+                 cudaStream_t s) {
+  if (n_elem <= 0) return;
+  k_lame<<<grid_for(n_elem, kThreads, num_sms * 8), kThreads, 0, s>>>(
+      n_elem, E, nu, reinterpret_cast<double2*>(lame));
+  VSGB_LAUNCH_CHECK();
+}
+
 void launch_chexa8_stiffness(int n_elem, const double* xyz, const int* conn, const double* E,
                              const double* nu, const int* form, double* kbuf, ElementError* err,
                              double* lame, int num_sms, cudaStream_t s) {
   if (n_elem <= 0) return;
-  double2* lm = reinterpret_cast<double2*>(lame);
-  k_lame<<<grid_for(n_elem, kThreads, num_sms * 8), kThreads, 0, s>>>(n_elem, E, nu, lm);
-  VSGB_LAUNCH_CHECK();
+  launch_lame(n_elem, E, nu, lame, num_sms, s);
+  const double2* lm = reinterpret_cast<const double2*>(lame);
   const size_t smem = element_smem_bytes();
   VSGB_CUDA(cudaFuncSetAttribute(k_chexa8_stiffness, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));

@@ -18,6 +18,15 @@ __device__ __forceinline__ void record_element_error(ElementError* err, int e, i
 }
 
 size_t element_smem_bytes();
+// Per-element Lame constants (lambda, mu) of isotropic_D into lame[2 * n_elem].
+void launch_lame(int n_elem, const double* E, const double* nu, double* lame, int num_sms,
+                 cudaStream_t s);
+// CHEXA8 centroid (n_elem x 7) and corner (n_elem x 8 x 7, may be null)
+// stresses from the displacements u[n_dof] (stress.cu); lame: 2 * n_elem scratch.
+void launch_solid_stress(int n_elem, const double* xyz, const int* conn, const int* eq3,
+                         const double* E, const double* nu, const double* u, int n_dof,
+                         double* lame, double* centroid, double* nodal, int num_sms,
+                         cudaStream_t s);
 // lame: scratch of 2 * n_elem doubles (per-element lambda, mu).
 void launch_chexa8_stiffness(int n_elem, const double* xyz, const int* conn, const double* E,
                              const double* nu, const int* form, double* kbuf, ElementError* err,
