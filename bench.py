@@ -279,6 +279,37 @@ def extra_stress(B, C, device):
             "max_von_mises_pa": float(cen[:, 6].max())}
 
 
+def extra_bdf(B, C):
+    """BDF ingestion of the 250 000-element adjoint deck (one MAT1 / PSOLID
+    pair per element, as the heterogeneous configs are written): the native
+    reader with every host thread and with one, the deck written by
+    cantilever.write_bdf into a temporary directory."""
+    import tempfile
+    m = C.block_250k_adjoint()
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "block_250k_adjoint.bdf")
+        C.write_bdf(m, path)
+        size = os.path.getsize(path)
+        out = {"workload": "block_250k_adjoint deck", "bytes": size}
+        for label, th in (("all_threads", 0), ("one_thread", 1)):
+            runs = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                d = B.read_bdf(path=path, threads=th)
+                mm = d.model()
+                runs.append((time.perf_counter() - t0, d.stats))
+            wall, st = min(runs, key=lambda r: r[0])
+            out[label] = {"threads": st["threads"], "wall_s": wall,
+                          "read_ms": st["read_ms"], "parse_ms": st["parse_ms"],
+                          "lines_ms": st["lines_ms"], "cards_ms": st["cards_ms"],
+                          "mesh_ms": st["mesh_ms"], "mb_per_s": size / 1e6 / wall}
+        out["lines"] = st["lines"]
+        out["cards"] = st["cards"]
+        out["model_equal"] = bool(np.array_equal(mm.E, m.E) and
+                                  np.array_equal(mm.node_ids[mm.conn], m.conn_ids()))
+    return out
+
+
 def extra_jitter(B, C, device, uniform):
     """Jittered (U(+-0.2 h) interior nodes) heterogeneous (log-uniform E)
     84 000-element cantilever: FP64 and mixed iteration counts against the
@@ -519,6 +550,7 @@ def main():
         extras = {"multi_rhs_16": extra_multi_rhs(B, C, device),
                   "adjoint_250k": extra_adjoint(B, C, device),
                   "stress_84k": extra_stress(B, C, device),
+                  "bdf_250k": extra_bdf(B, C),
                   "jitter_84k": extra_jitter(B, C, device,
                                              {"fp64": st_fp64.iterations, "mixed": it_mixed})}
     line = {

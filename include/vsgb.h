@@ -207,6 +207,61 @@ int vsgb_adjoint_gradients(vsgb_ctx* ctx, const double* F, const double* dJdu, d
 int vsgb_solid_stress(vsgb_ctx* ctx, const double* u, int k, double* centroid_out,
                       double* nodal_out, double* kernel_ms);
 
+/* ── BDF decks (host only, no GPU needed) ────────────────────────────────── */
+
+/* Reader of the deck subset of the SOL 101 CHEXA8 path, in place of
+ * BdfParser::parse_file / parse_string (src/io/bdf_parser.cpp:83-95) for it:
+ * GRID, CHEXA, PSOLID, MAT1, SPC1, FORCE, PARAM bulk cards (free, small and
+ * large field, continuations, Nastran number forms) and SOL / SUBCASE / LOAD /
+ * SPC case control, with the reference's card assembly rules.  Cards the
+ * reference does not know are ignored and listed (vsgb_bdf_message 1); cards
+ * it knows that change the model outside this path (other elements, rigid
+ * elements, coordinate systems in use, other loads / SPCs or temperatures of
+ * a selected set, MPC sets) make vsgb_bdf_mesh or the per-subcase calls
+ * fail with the reason.  The bulk data is parsed by `threads` host threads
+ * (<= 0: all).  Parse errors return VSGB_ERR_INVALID with the reference's
+ * "Line N: ..." text in err. */
+typedef struct vsgb_bdf vsgb_bdf;
+
+typedef struct {
+  int n_nodes;       /* distinct GRIDs */
+  int n_elem;        /* CHEXA cards */
+  int n_subcases;
+  int sol;           /* 101, 103, or 0 when the deck has no SOL line */
+  long long lines;   /* physical lines */
+  long long cards;   /* logical bulk cards */
+  int threads;       /* host threads used for the bulk data */
+  double read_ms;    /* file read (vsgb_bdf_read) */
+  double parse_ms;   /* line split, cards, mesh arrays */
+  int mesh_ok;       /* 1 when vsgb_bdf_mesh succeeds */
+  double lines_ms;   /* of parse_ms: line index, markers, case control */
+  double cards_ms;   /* of parse_ms: bulk cards (the threaded part) */
+  double mesh_ms;    /* of parse_ms: mesh arrays and checks */
+} vsgb_bdf_stats;
+
+int vsgb_bdf_read(const char* path, int threads, vsgb_bdf** out, char* err, size_t err_len);
+int vsgb_bdf_parse(const char* text, size_t len, int threads, vsgb_bdf** out, char* err,
+                   size_t err_len);
+void vsgb_bdf_free(vsgb_bdf* deck);
+int vsgb_bdf_info(vsgb_bdf* deck, vsgb_bdf_stats* info);
+/* which: 0 why the mesh cannot be formed ("" when it can), 1 ignored-card
+ * warnings, 2 the last error of a call on this deck. */
+int vsgb_bdf_message(vsgb_bdf* deck, int which, char* buf, size_t len);
+/* Subcase s (file order): its id and LOAD / SPC set ids. */
+int vsgb_bdf_subcase(vsgb_bdf* deck, int s, int* id, int* load_set, int* spc_set);
+/* Mesh arrays, each optional: node_ids[n_nodes] ascending, xyz[3 n_nodes];
+ * elem_ids[n_elem], conn[8 n_elem] (0-based indices into node_ids, CHEXA G1-G8
+ * order), E / nu[n_elem] (MAT1 of the element's PSOLID), form[n_elem]
+ * (VSGB_EAS / VSGB_SRI from PSOLID ISOP).  Elements in card order. */
+int vsgb_bdf_mesh(vsgb_bdf* deck, int* node_ids, double* xyz, int* elem_ids, int* conn,
+                  double* E, double* nu, int* form);
+/* SPC1 entries (grid id, component mask bit d = DOF d+1) and FORCE cards
+ * (grid id, scale, direction[3]) of subcase s's sets, in card order; call
+ * with null arrays for *count first. */
+int vsgb_bdf_constraints(vsgb_bdf* deck, int s, int* count, int* nodes, int* masks);
+int vsgb_bdf_forces(vsgb_bdf* deck, int s, int* count, int* nodes, double* scale,
+                    double* dir);
+
 /* ── measurement helpers ────────────────────────────────────────────────── */
 
 /* Events on the context stream, synchronised on both sides. */

@@ -60,6 +60,8 @@ OPT_ADAPTIVE_INNER = 12
 # The symbols include/vsgb.h declares (checked by tests against the .so).
 EXPORTS = (
     "vsgb_rhs_stats", "vsgb_adjoint_gradients", "vsgb_solid_stress",
+    "vsgb_bdf_read", "vsgb_bdf_parse", "vsgb_bdf_free", "vsgb_bdf_info", "vsgb_bdf_message",
+    "vsgb_bdf_subcase", "vsgb_bdf_mesh", "vsgb_bdf_constraints", "vsgb_bdf_forces",
     "vsgb_create", "vsgb_destroy", "vsgb_set_option", "vsgb_last_error", "vsgb_device_name",
     "vsgb_backend_name", "vsgb_solve_csr", "vsgb_build_dof_map", "vsgb_apply_forces",
     "vsgb_assemble_chexa8", "vsgb_copy_csr_lower", "vsgb_solve_assembled", "vsgb_mesh_upload",
@@ -76,6 +78,17 @@ class SolverError(RuntimeError):
     def __init__(self, msg: str, code: int = VSGB_ERR_INVALID):
         super().__init__(msg)
         self.code = code
+
+
+class BdfStats(ctypes.Structure):
+    """vsgb_bdf_stats."""
+    _fields_ = [("n_nodes", ctypes.c_int), ("n_elem", ctypes.c_int),
+                ("n_subcases", ctypes.c_int), ("sol", ctypes.c_int),
+                ("lines", ctypes.c_longlong), ("cards", ctypes.c_longlong),
+                ("threads", ctypes.c_int), ("read_ms", ctypes.c_double),
+                ("parse_ms", ctypes.c_double), ("mesh_ok", ctypes.c_int),
+                ("lines_ms", ctypes.c_double), ("cards_ms", ctypes.c_double),
+                ("mesh_ms", ctypes.c_double)]
 
 
 class VsgbStats(ctypes.Structure):
@@ -139,6 +152,17 @@ def load_library(build_if_missing: bool = False):
     L.vsgb_kernel_launches.restype = c_ll
     L.vsgb_adjoint_gradients.argtypes = [vp, _f64p, vp, vp, vp, vp, vp, ctypes.POINTER(VsgbStats)]
     L.vsgb_solid_stress.argtypes = [vp, vp, c_int, _f64p, vp, ctypes.POINTER(c_dbl)]
+    L.vsgb_bdf_read.argtypes = [cp, c_int, ctypes.POINTER(vp), cp, sz]
+    L.vsgb_bdf_parse.argtypes = [cp, sz, c_int, ctypes.POINTER(vp), cp, sz]
+    L.vsgb_bdf_free.argtypes = [vp]
+    L.vsgb_bdf_free.restype = None
+    L.vsgb_bdf_info.argtypes = [vp, ctypes.POINTER(BdfStats)]
+    L.vsgb_bdf_message.argtypes = [vp, c_int, cp, sz]
+    L.vsgb_bdf_subcase.argtypes = [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                   ctypes.POINTER(c_int)]
+    L.vsgb_bdf_mesh.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+    L.vsgb_bdf_constraints.argtypes = [vp, c_int, ctypes.POINTER(c_int), vp, vp]
+    L.vsgb_bdf_forces.argtypes = [vp, c_int, ctypes.POINTER(c_int), vp, vp, vp]
     L.vsgb_rhs_stats.argtypes = [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_dbl),
                                  ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.vsgb_pcg_solve_noalloc.argtypes = [c_int, c_int, vp, vp, vp, vp, vp, c_dbl, c_int, vp,
@@ -463,3 +487,119 @@ def time_spmv(backend, precision: int, reps: int = 50):
     backend.context.check(load_library().vsgb_time_spmv(backend.context.ptr, precision, reps,
                                                         ctypes.byref(ms), ctypes.byref(by)))
     return ms.value, by.value
+
+
+# ── BDF decks ──────────────────────────────────────────────────────────────
+
+class BdfDeck:
+    """A deck read by the native reader (vsgb_bdf_*): ``stats``, ``subcases``
+    [(id, load set, spc set)], ``warnings`` (ignored cards) and ``model()``,
+    the SolidModel of the CHEXA8 path.  Parse errors raise SolverError with
+    the reference's "Line N: ..." text."""
+
+    def __init__(self, path=None, text=None, threads=0):
+        L = load_library()
+        self._L = L
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(1024)
+        if path is not None:
+            rc = L.vsgb_bdf_read(os.fsencode(path), threads, ctypes.byref(h), err, 1024)
+        else:
+            data = text.encode() if isinstance(text, str) else bytes(text)
+            rc = L.vsgb_bdf_parse(data, len(data), threads, ctypes.byref(h), err, 1024)
+        if rc != VSGB_OK:
+            raise SolverError(err.value.decode(errors="replace"), rc)
+        self._h = h
+        st = BdfStats()
+        L.vsgb_bdf_info(h, ctypes.byref(st))
+        self.stats = {k: getattr(st, k) for k, _ in BdfStats._fields_}
+        self.subcases = []
+        for s_ in range(st.n_subcases):
+            a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            L.vsgb_bdf_subcase(h, s_, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+            self.subcases.append((a.value, b.value, c.value))
+        self.warnings = self._message(1)
+        self.mesh_error = self._message(0)
+
+    def _message(self, which):
+        buf = ctypes.create_string_buffer(4096)
+        self._L.vsgb_bdf_message(self._h, which, buf, 4096)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc):
+        if rc != VSGB_OK:
+            raise SolverError(self._message(2), rc)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.vsgb_bdf_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def mesh(self):
+        """(node_ids, xyz, elem_ids, conn, E, nu, form)."""
+        st = self.stats
+        N, M = st["n_nodes"], st["n_elem"]
+        ids = np.zeros(N, np.int32)
+        xyz = np.zeros((N, 3))
+        eids = np.zeros(M, np.int32)
+        conn = np.zeros((M, 8), np.int32)
+        E = np.zeros(M)
+        nu = np.zeros(M)
+        form = np.zeros(M, np.int32)
+
+        def p(a):
+            return a.ctypes.data_as(ctypes.c_void_p)
+
+        self._check(self._L.vsgb_bdf_mesh(self._h, p(ids), p(xyz), p(eids), p(conn), p(E), p(nu),
+                                          p(form)))
+        return ids, xyz, eids, conn, E, nu, form
+
+    def constraints(self, s=0):
+        n = ctypes.c_int()
+        self._check(self._L.vsgb_bdf_constraints(self._h, s, ctypes.byref(n), None, None))
+        nodes = np.zeros(n.value, np.int32)
+        masks = np.zeros(n.value, np.int32)
+        self._check(self._L.vsgb_bdf_constraints(self._h, s, ctypes.byref(n),
+                                                 nodes.ctypes.data_as(ctypes.c_void_p),
+                                                 masks.ctypes.data_as(ctypes.c_void_p)))
+        return nodes, masks
+
+    def forces(self, s=0):
+        n = ctypes.c_int()
+        self._check(self._L.vsgb_bdf_forces(self._h, s, ctypes.byref(n), None, None, None))
+        nodes = np.zeros(n.value, np.int32)
+        scale = np.zeros(n.value)
+        dirs = np.zeros((n.value, 3))
+        self._check(self._L.vsgb_bdf_forces(self._h, s, ctypes.byref(n),
+                                            nodes.ctypes.data_as(ctypes.c_void_p),
+                                            scale.ctypes.data_as(ctypes.c_void_p),
+                                            dirs.ctypes.data_as(ctypes.c_void_p)))
+        return nodes, scale, dirs
+
+    def model(self, subcases=None, name="bdf"):
+        """SolidModel with the SPC set of the first chosen subcase and one load
+        case per chosen subcase (all must share that SPC set)."""
+        from . import cantilever as C
+        chosen = list(range(len(self.subcases))) if subcases is None else list(subcases)
+        spc_sets = {self.subcases[s][2] for s in chosen}
+        if len(spc_sets) != 1:
+            raise SolverError("the chosen subcases use different SPC sets; take one at a time")
+        ids, xyz, eids, conn, E, nu, form = self.mesh()
+        spc_nodes, spc_mask = self.constraints(chosen[0])
+        loads = [self.forces(s) for s in chosen]
+        return C.SolidModel(node_ids=ids, xyz=xyz, conn=conn, elem_ids=eids, E=E, nu=nu,
+                            form=form, spc_nodes=spc_nodes, spc_mask=spc_mask, loads=loads,
+                            name=name)
+
+
+def read_bdf(path=None, text=None, threads=0) -> BdfDeck:
+    """Read a BDF deck (a file path, or the deck text) with the native reader."""
+    if (path is None) == (text is None):
+        raise ValueError("give exactly one of path / text")
+    return BdfDeck(path=path, text=text, threads=threads)
