@@ -101,3 +101,34 @@ def test_stress_full_size_84k(vsgb, oracle):
     x_el = m.xyz[m.conn[i_max]][:, 0].mean()
     assert x_el < 0.1 * m.xyz[:, 0].max()
     be.close()
+
+
+def test_deck_to_stresses_on_gpu(vsgb, oracle):
+    """The reference generator's 320-element bending deck through the whole
+    path: native BDF reader -> GPU DOF map, assembly, FP64 PCG -> GPU stress
+    recovery, against the oracle's direct solve and recovery, and the bending
+    stress against beam theory."""
+    import os
+    from conftest import GOLDEN
+    deck = vsgb.read_bdf(path=os.path.join(GOLDEN, "ref_generator_bending_320.bdf"))
+    m = deck.model()
+    eq6, n = vsgb.build_dof_map(m)
+    F = vsgb.apply_forces(m, eq6, n)
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-12, 20000)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    u = asm.solve(F)
+    eq_o, n_o, K, F_o, u_o = oracle.solve_model(m)
+    assert np.array_equal(eq6, eq_o)
+    assert np.linalg.norm(u - u_o) <= 1e-8 * np.linalg.norm(u_o)
+    cen, nodal, _ = asm.solid_stress()
+    oc, on = oracle.solid_stress(m, eq6, u_o)
+    assert _close(cen, oc, 1e-7) and _close(nodal, on, 1e-7)
+    # away from the clamp the outer-layer centroid sigma_xx is the beam
+    # stress -F (L - x)(z - H/2) / I (0.1 % on this mesh)
+    cx = m.xyz[m.conn].mean(axis=1)
+    beam = -1000.0 * (1.0 - cx[:, 0]) * (cx[:, 2] - 0.1) / (0.2 * 0.2 ** 3 / 12)
+    sel = (cx[:, 0] > 0.2) & (cx[:, 0] < 0.8) & (np.abs(cx[:, 2] - 0.1) > 0.07)
+    assert sel.sum() == 96
+    assert np.all(np.abs(cen[sel, 0] / beam[sel] - 1.0) < 5e-3)
+    be.close()

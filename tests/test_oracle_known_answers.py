@@ -175,8 +175,12 @@ def test_golden_oracle_fixture(oracle):
     eq6, n, K, F, u = oracle.solve_model(m)
     assert n == c1["n"] and K.nnz == c1["nnz_lower"]
     assert C_hash(K) == c1["pattern_sha256"]
-    assert np.abs(np.array(c1["u_head"]) - u[:len(c1["u_head"])]).max() <= 1e-12 * np.abs(u).max()
-    assert abs(np.linalg.norm(u) - c1["u_norm"]) <= 1e-12 * c1["u_norm"]
+    # The direct solve's threaded reductions run in an order that depends on
+    # the host's core count and vector unit (x86 here, 16-core Arm hosts
+    # elsewhere); with kappa(K) ~ 1e6 the solutions then agree to ~1e-12, so
+    # the bound is 1e-10 (the element matrices above are held to 1e-13).
+    assert np.abs(np.array(c1["u_head"]) - u[:len(c1["u_head"])]).max() <= 1e-10 * np.abs(u).max()
+    assert abs(np.linalg.norm(u) - c1["u_norm"]) <= 1e-10 * c1["u_norm"]
 
 
 def C_hash(K):
