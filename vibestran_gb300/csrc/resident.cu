@@ -72,6 +72,9 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 // 3: 24.1 / 72.5 and 46.8 / 146 us; 5: 23.8 / 72.9 and 46.4 / 144 us.
 constexpr int kSliceWeight = 4;
 
+// Window kernels keep p over the window in shared memory between iterations.
+constexpr bool kKeepWindowP = true;
+
 __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -262,6 +265,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     acc2[0] = rfma(rv, rv, acc2[0]);
     acc2[1] = rfma(rv, zv, acc2[1]);
   }
+  if (kWindow && kKeepWindowP)  // p_{-1} = 0 over the window
+    for (int j = tid; j <= we - wb; j += kResThreads) st3(win + 4 * j, T(0), T(0), T(0));
   // The scalar recurrence runs on thread 0 only (FP64 sqrt / division are long
   // instruction sequences on GB300's FP64 pipe), inside the reductions, and is
   // broadcast through shared memory: s_sc = {alpha, beta}.
@@ -304,6 +309,9 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     if (kWindow) {
       // kFill nodes per thread per round: all their loads are in flight
       // together (one L2 round trip per round instead of one per node).
+      // With kKeepWindowP the window already holds p_k of every window node
+      // (each CTA forms p = z + beta p for them with the operands and order of
+      // the owner, so the copies are bitwise the owner's): only z is read.
       constexpr int kFill = 4;
       for (int j0 = wb + tid; j0 <= we; j0 += kFill * kResThreads) {
         T z[kFill][3], q[kFill][3];
@@ -312,7 +320,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
           const int j = j0 + u * kResThreads;
           if (j <= we) {
             ld3(a.z4 + 4 * static_cast<size_t>(j), z[u][0], z[u][1], z[u][2]);
-            ld3(p_old + 4 * static_cast<size_t>(j), q[u][0], q[u][1], q[u][2]);
+            if (kKeepWindowP)
+              lds3(win + 4 * (j - wb), q[u][0], q[u][1], q[u][2]);
+            else
+              ld3(p_old + 4 * static_cast<size_t>(j), q[u][0], q[u][1], q[u][2]);
           }
         }
 #pragma unroll
@@ -408,7 +419,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         const T pn = rfma(tb, P[lr], RR[lr] * D[lr]);  // z = r diag^-1, as stored in z4
         P[lr] = pn;
         AP[lr] = yq;
-        p_new[4 * R + q] = pn;
+        if (!(kWindow && kKeepWindowP)) p_new[4 * R + q] = pn;
         part = pn * yq;
       }
       part = warp_sum(part);
