@@ -75,6 +75,14 @@ constexpr int kSliceWeight = 4;
 // Window kernels keep p over the window in shared memory between iterations.
 constexpr bool kKeepWindowP = true;
 
+// Direction of the SpMV slice walk alternates between iterations.  The
+// operator is read once per iteration and does not fit the L2 as a whole; in
+// a cyclic walk the lines read last are the ones the next walk reaches last,
+// when they are gone, while a reversed walk starts on them.  Measured per
+// FP32 iteration: 84k 21.7 -> 18.6 us, 504k 41.0 -> 35.0 us, 780k 69.1 ->
+// 63.1 us.
+constexpr bool kSnake = true;
+
 __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -339,7 +347,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     T accp[1] = {T(0)};
     // Slices are handed out dynamically (first one per warp statically), so
     // warps that drew short slices take more and the phase ends together.
-    for (int ls = warp; ls < ns;) {
+    for (int lq = warp; lq < ns;) {
+      // kSnake: odd iterations walk the CTA's slices backwards, so the lines
+      // touched last (most likely still in L2) are read first
+      const int ls = (kSnake && (it & 1)) ? ns - 1 - lq : lq;
       const int sl = s0 + ls;
       const int base = a.slice_ptr[sl], steps = a.slice_ptr[sl + 1] - base;
       const int* cp = a.cols + static_cast<size_t>(base) * 32 + lane;
@@ -428,7 +439,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         SL[ls] = part;
         nxt = atomicAdd(&s_next, 1);
       }
-      ls = __shfl_sync(0xffffffffu, nxt, 0);
+      lq = __shfl_sync(0xffffffffu, nxt, 0);
     }
     // p.Ap of the CTA in slice order, whichever warp computed each slice.
     __syncthreads();
