@@ -39,6 +39,7 @@ MIXED_MAX_SOLVES = 4
 JITTER_MIXED_TOL = 2e-5  # jittered heterogeneous mesh: <= 1e-6 error needs a tighter residual
 JITTER_INNER_TOL = 1e-4  # and a deeper first inner solve: 932 FP32 iterations vs 1043 at 1e-3
 MULTI_MIXED_TOL = 1e-8   # 16 random face-load cases: <= 1e-6 error (see extra_multi_rhs)
+MULTI_INNER_TOL = 1e-4   # first inner solves: 286 ms / 1.1e-7 error vs 306 ms / 3.1e-7 at 1e-3
 # FP64 FMA rate of a GB300 measured with an FMA-chain kernel (1.91 DFMA/clk/SM
 # at 2.07 GHz): the compute floor of the FP64 SpMV.
 FP64_TFLOPS = 1.20
@@ -157,6 +158,7 @@ def extra_multi_rhs(B, C, device):
     eq6, n = B.build_dof_map(m)
     F = np.stack([B.apply_forces(m, eq6, n, k) for k in range(16)], axis=1)
     be = _mixed_backend(B, device, tol=MULTI_MIXED_TOL, max_solves=12)
+    be.set_option(B.OPT_INNER_TOL, MULTI_INNER_TOL)
     asm = B.ChexaAssembler(be)
     asm.assemble(m, eq6, n)
     asm.upload_rhs(F)

@@ -313,7 +313,11 @@ k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restr
   T pap[RN];
 #pragma unroll
   for (int r = 0; r < RN; ++r) pap[r] = T(0);
-  for (int sl = blockIdx.x * wpb + (threadIdx.x >> 5); sl < B.nslices; sl += gridDim.x * wpb) {
+  // odd iterations walk the slices from the end: the operator lines read last
+  // (the ones still in L2) are read first
+  const bool rev = (S->iter & 1) != 0;
+  for (int sq = blockIdx.x * wpb + (threadIdx.x >> 5); sq < B.nslices; sq += gridDim.x * wpb) {
+    const int sl = rev ? B.nslices - 1 - sq : sq;
     T out[3][RN];
     mspmm_slice<T, G>(B, vals, p, sl, lane, g0, out);
     const int R = sl * 8 + (lane >> 2);
