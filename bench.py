@@ -16,6 +16,7 @@ data-parallel exchange); value is whole-job seconds per solve.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -335,6 +336,16 @@ def extra_jitter(B, C, device, uniform):
     asm.solve_resident()
     st_d = asm.solve_resident()
     u_d = asm.download()
+    # the same two solves with the 3x3 block Jacobi preconditioner
+    be.set_option(B.OPT_PRECOND, B.PRECOND_BLOCK_JACOBI)
+    asm.solve_resident()
+    st_bd = asm.solve_resident()
+    u_bd = asm.download()
+    be.set_option(B.OPT_PRECISION, B.MIXED)
+    be.set_option(B.OPT_TOLERANCE, JITTER_MIXED_TOL)
+    asm.solve_resident()
+    st_bm = asm.solve_resident()
+    u_bm = asm.download()
     be.close()
     out = {"workload": "cantilever_84k_jitter", "dofs": n, "seed": m.seed,
            "fp64": {"iterations": st_d.iterations, "solve_s": st_d.solve_ms / 1e3},
@@ -343,15 +354,20 @@ def extra_jitter(B, C, device, uniform):
                      "solve_s": st_m.solve_ms / 1e3},
            "iteration_growth_vs_uniform": {
                "fp64": st_d.iterations / uniform["fp64"],
-               "fp32_inner": st_m.iterations / uniform["mixed"]}}
+               "fp32_inner": st_m.iterations / uniform["mixed"]},
+           "block_jacobi": {
+               "fp64": {"iterations": st_bd.iterations, "solve_s": st_bd.solve_ms / 1e3},
+               "mixed": {"iterations_fp32": st_bm.iterations, "inner_solves": st_bm.inner_solves,
+                         "solve_s": st_bm.solve_ms / 1e3}}}
     path = os.path.join(ROOT, "tests", "golden", "cantilever_84k_jitter_direct.json")
     if os.path.exists(path):
         with open(path) as fh:
             g = json.load(fh)
         eqs = np.concatenate([g["tip_eq"], g["sample_eq"]])
         ref = np.concatenate([g["tip_uz"], g["sample_u"]])
-        for key, u in (("fp64", u_d), ("mixed", u_m)):
-            out[key]["rel_err_vs_direct"] = float(np.linalg.norm(u[eqs] - ref) / np.linalg.norm(ref))
+        for d, key, u in ((out, "fp64", u_d), (out, "mixed", u_m),
+                          (out["block_jacobi"], "fp64", u_bd), (out["block_jacobi"], "mixed", u_bm)):
+            d[key]["rel_err_vs_direct"] = float(np.linalg.norm(u[eqs] - ref) / np.linalg.norm(ref))
     return out
 
 
@@ -514,6 +530,17 @@ def main():
     st_fp64 = be.last_stats
     u_fp64 = asm.download()
     err_fp64 = float(np.linalg.norm(u_fp64 - u_ref) / np.linalg.norm(u_ref))
+    # The same mixed solve with the 3x3 block Jacobi preconditioner (option).
+    be.set_option(B.OPT_PRECISION, B.MIXED)
+    be.set_option(B.OPT_TOLERANCE, MIXED_TOL)
+    be.set_option(B.OPT_PRECOND, B.PRECOND_BLOCK_JACOBI)
+    bj_solve = [asm.solve_resident().solve_ms for _ in range(a.steps + 1)][1:]
+    st_bj = be.last_stats
+    u_bj = asm.download()
+    err_bj = float(np.linalg.norm(u_bj - u_ref) / np.linalg.norm(u_ref))
+    be.set_option(B.OPT_PRECOND, B.PRECOND_JACOBI)
+    be.set_option(B.OPT_PRECISION, B.FP64)
+    be.set_option(B.OPT_TOLERANCE, FP64_TOL)
 
     # Launch-path block SpMVs (not in the step) for comparison.
     spmv_ms, spmv_bytes = B.time_spmv(be, B.MIXED, 200)
@@ -523,23 +550,32 @@ def main():
     be.set_option(B.OPT_PRECISION, B.MIXED)
     be.set_option(B.OPT_TOLERANCE, MIXED_TOL)
 
-    # End to end through the C ABI with host buffers (mesh + F in, u out).
+    # End to end through the C ABI with host buffers (mesh + F in, u out),
+    # the host arrays in page-locked memory.
     be_e2e = B.Gb300MixedPcgSolverBackend.try_create(MIXED_TOL, 10000, device)
     be_e2e.set_option(B.OPT_INNER_TOL, MIXED_INNER_TOL)
     be_e2e.set_option(B.OPT_MAX_SOLVES, MIXED_MAX_SOLVES)
+    pin = be_e2e.pinned_copy
+    model_h = dataclasses.replace(model, xyz=pin(model.xyz), conn=pin(model.conn),
+                                  E=pin(model.E), nu=pin(model.nu),
+                                  form=pin(model.form.astype(np.int32)))
+    eq3_h = pin(np.ascontiguousarray(eq6[:, :3], np.int32))
+    F_h = pin(F)
+    u_e = be_e2e.pinned_empty(n)
     asm_e = B.ChexaAssembler(be_e2e)
     for _ in range(1):
-        asm_e.assemble(model, eq6, n)
-        asm_e.solve(F)
+        asm_e.assemble(model_h, eq3_h, n)
+        asm_e.solve(F_h, out=u_e)
     _barrier(dist)
     t0 = time.perf_counter()
     for _ in range(a.steps):
-        asm_e.assemble(model, eq6, n)
-        u_e = asm_e.solve(F)
+        asm_e.assemble(model_h, eq3_h, n)
+        asm_e.solve(F_h, out=u_e)
     t_e2e = _allmax(dist, (time.perf_counter() - t0) / a.steps)
-    h2d = (model.xyz.nbytes + 12 * model.n_nodes + model.conn.nbytes + model.E.nbytes
-           + model.nu.nbytes + 4 * model.n_elem + F.nbytes)
+    h2d = (model_h.xyz.nbytes + eq3_h.nbytes + model_h.conn.nbytes + model_h.E.nbytes
+           + model_h.nu.nbytes + model_h.form.nbytes + F_h.nbytes)
     d2h = u_e.nbytes
+    err_e2e = float(np.linalg.norm(u_e - u_ref) / np.linalg.norm(u_ref))
 
     if rank != 0:
         return
@@ -577,6 +613,8 @@ def main():
                     "reference": "FP64 PCG to 1e-12 (matches SuperLU direct to 9e-13)"},
         "phases_s": {"assembly": t_asm, "mixed_solve": statistics.median(mixed_solve) / 1e3,
                      "fp64_solve": statistics.median(fp64_solve) / 1e3},
+        "mixed_block_jacobi": {"solve_s": statistics.median(bj_solve) / 1e3,
+                               "iterations": st_bj.iterations, "rel_err": err_bj},
         "mixed": {"solve_s": statistics.median(mixed_solve) / 1e3, "iterations": it_mixed,
                   "inner_solves": st_mixed.inner_solves,
                   "pcg_iter_per_s": it_mixed / (statistics.median(mixed_solve) / 1e3)},
@@ -604,7 +642,8 @@ def main():
                          "sample": f"full workload x{a.cpu_steps}: element stiffness + build_csr "
                                    f"+ FP64 Jacobi PCG ({cpu_iters} it, tol {FP64_TOL:g})"},
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "host_buffers": "page-locked",
+                "rel_err": err_e2e},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
     }

@@ -69,6 +69,17 @@ extern "C" {
 #define VSGB_OPT_L2_PERSIST 11    /* 1: mark the operator values persisting in L2 during
                                      each persistent PCG launch (default 0: measured no
                                      gain, the solve is not bound by L2 misses) */
+#define VSGB_OPT_PRECOND 13       /* VSGB_PRECOND_JACOBI (default, the reference's Jacobi
+                                     fallback, cuda_pcg_backend_impl.hpp:1041-1252) or
+                                     VSGB_PRECOND_BLOCK_JACOBI: the inverse 3x3 diagonal
+                                     block of every node (the persistent solve on the
+                                     block operator, FP64 and mixed; one solve per load
+                                     case); a solve it cannot run returns
+                                     VSGB_ERR_INVALID, a block that is not positive
+                                     definite VSGB_ERR_SINGULAR */
+
+#define VSGB_PRECOND_JACOBI 0
+#define VSGB_PRECOND_BLOCK_JACOBI 1
 
 typedef struct vsgb_ctx vsgb_ctx;
 
@@ -173,6 +184,13 @@ int vsgb_rhs_upload(vsgb_ctx* ctx, const double* F, int nrhs);
 int vsgb_solve_resident(vsgb_ctx* ctx, vsgb_stats* stats);
 /* Download the resident solution (n*nrhs doubles). */
 int vsgb_solution_download(vsgb_ctx* ctx, double* u_out);
+
+/* Page-locked host memory on the context's device, for the host arrays the
+ * calls above copy from or into (mesh, loads, solutions): those copies then
+ * run at the host link's rate instead of through a pageable staging copy.
+ * No reference counterpart (the reference's host arrays are std::vector). */
+int vsgb_host_alloc(vsgb_ctx* ctx, size_t bytes, void** out);
+int vsgb_host_free(vsgb_ctx* ctx, void* p);
 
 /* ── adjoint sensitivities ──────────────────────────────────────────────── */
 

@@ -435,3 +435,70 @@ def solid_stress(model, eq6, u):
     centroid = at(np.zeros(3))
     nodal = np.stack([at(HEX_CORNERS[k]) for k in range(8)], axis=1)
     return centroid, nodal
+
+
+def block_jacobi_inverse(K: Csr) -> np.ndarray:
+    """Inverse 3x3 diagonal block of every node (equations 3i..3i+2), from the
+    blocks' upper triangles mirrored (the symmetric part), (n/3, 3, 3).
+
+    No reference counterpart: the reference's cuda-pcg preconditions with IC0
+    and falls back to scalar Jacobi (src/solver/cuda_pcg_backend_impl.hpp:
+    1041-1252); the 3x3 block form is the block-diagonal of the same K."""
+    if K.n % 3:
+        raise OracleError("block Jacobi needs node-aligned equation triples")
+    full = K if not K.lower else K.expanded_symmetric()
+    nb = K.n // 3
+    D = np.zeros((nb, 3, 3))
+    rows = np.repeat(np.arange(full.n), np.diff(full.row_ptr))
+    cols = np.asarray(full.col_ind)
+    sel = (rows // 3 == cols // 3) & (rows % 3 <= cols % 3)
+    r, c, v = rows[sel], cols[sel], np.asarray(full.values)[sel]
+    D[r // 3, r % 3, c % 3] = v
+    D[r // 3, c % 3, r % 3] = v
+    return np.linalg.inv(D)
+
+
+def pcg_block_jacobi(K: Csr, F, tol=1e-8, max_iters=10000):
+    """FP64 PCG with the 3x3 block Jacobi preconditioner z_I = B_I r_I: the
+    recurrence, stopping test (sqrt(r.r)/||b|| < tol) and zero-RHS / rz <= 0 /
+    pAp <= 0 handling of the oracle's scalar Jacobi PCG (run_pcg_prepared,
+    src/solver/cuda_pcg_backend_impl.hpp:1688-1999).  Returns (u, iters, rel)."""
+    import scipy.sparse as sp
+    full = K if not K.lower else K.expanded_symmetric()
+    A = sp.csr_matrix((full.values, full.col_ind, full.row_ptr), shape=(full.n, full.n))
+    B = block_jacobi_inverse(K)
+    nb = K.n // 3
+
+    def prec(r):
+        return np.einsum("ijk,ik->ij", B, r.reshape(nb, 3)).reshape(-1)
+
+    b = np.asarray(F, np.float64)
+    u = np.zeros(K.n)
+    norm_b = np.sqrt(abs(b @ b))
+    if norm_b < 1e-300:
+        return u, 0, 0.0
+    r = b.copy()
+    z = prec(r)
+    p = z.copy()
+    rz = r @ z
+    if not rz > 0.0:
+        raise OracleError("non-positive initial r*z -- preconditioner is not SPD or matrix "
+                          "is singular")
+    rel = 1.0
+    for it in range(max_iters):
+        Ap = A @ p
+        pAp = p @ Ap
+        if not pAp > 0.0:
+            break
+        alpha = rz / pAp
+        u += alpha * p
+        r -= alpha * Ap
+        z = prec(r)
+        rz_new = r @ z
+        rel = np.sqrt(abs(r @ r)) / norm_b
+        if rel < tol:
+            return u, it + 1, rel
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+    raise OracleError(f"did not converge after {max_iters} iterations (relative residual "
+                      f"{rel:g} > tolerance {tol:g})")

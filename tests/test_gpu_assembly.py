@@ -113,6 +113,32 @@ def test_element_errors(vsgb, be):
     assert np.isfinite(asm.solve(vsgb.apply_forces(m, eq6, n))).all()
 
 
+def test_mesh_index_errors(vsgb, be):
+    """Out-of-range connectivity and equation indices are rejected by the
+    upload's range check before any mesh kernel runs; the context stays
+    usable and holds no mesh after a rejected upload."""
+    from vibestran_gb300 import cantilever as C
+    asm = vsgb.ChexaAssembler(be)
+    for bad in (-1, None):
+        m = C.small_block(3, 2, 2, 0.1)
+        m.conn[3, 5] = m.n_nodes if bad is None else bad
+        eq6, n = vsgb.build_dof_map(C.small_block(3, 2, 2, 0.1))
+        with pytest.raises(vsgb.SolverError,
+                           match="element index 3 references a node index out of range"):
+            asm.assemble(m, eq6, n)
+        with pytest.raises(vsgb.SolverError, match="no mesh uploaded"):
+            asm.assemble_resident()
+    m = C.small_block(3, 2, 2, 0.1)
+    eq6, n = vsgb.build_dof_map(m)
+    for v in (n, -2):
+        e = eq6.copy()
+        e[5, 1] = v
+        with pytest.raises(vsgb.SolverError, match="equation index out of range at node index 5"):
+            asm.assemble(m, e, n)
+    asm.assemble(m, eq6, n)
+    assert np.isfinite(asm.solve(vsgb.apply_forces(m, eq6, n))).all()
+
+
 def test_unconstrained_model_is_reported(vsgb, be):
     # no SPC: K is singular, PCG must not report convergence silently
     from vibestran_gb300 import cantilever as C

@@ -152,3 +152,31 @@ def test_cpp_conformance_driver(vsgb):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "ALL PASS" in r.stdout
+
+
+def test_page_locked_host_arrays(vsgb):
+    """Mesh, equation table, loads and solution in page-locked host memory
+    (vsgb_host_alloc) give the same solution, bit for bit, as pageable
+    arrays; the blocks are freed with the context."""
+    import dataclasses
+    from vibestran_gb300 import cantilever as C
+    m = C.small_block(6, 3, 3, 0.1, seed=3, jitter=0.1)
+    eq6, n = vsgb.build_dof_map(m)
+    F = vsgb.apply_forces(m, eq6, n)
+    be = vsgb.Gb300MixedPcgSolverBackend.try_create(1e-8, 20000)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    u_ref = asm.solve(F)
+    pin = be.pinned_copy
+    mh = dataclasses.replace(m, xyz=pin(m.xyz), conn=pin(m.conn), E=pin(m.E), nu=pin(m.nu),
+                             form=pin(m.form))
+    eq3 = pin(np.ascontiguousarray(eq6[:, :3], np.int32))
+    assert eq3.shape == (m.n_nodes, 3) and np.array_equal(mh.xyz, m.xyz)
+    u = be.pinned_empty(n)
+    asm.assemble(mh, eq3, n)
+    assert asm.solve(pin(F), out=u) is u
+    assert np.array_equal(u, u_ref)
+    with pytest.raises(ValueError):
+        asm.solve(F, out=np.zeros(n + 1))
+    assert len(be.context.pinned) == 8
+    be.close()

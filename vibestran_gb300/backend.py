@@ -56,6 +56,10 @@ OPT_RESIDENT = 9
 OPT_BATCHED = 10
 OPT_L2_PERSIST = 11
 OPT_ADAPTIVE_INNER = 12
+OPT_PRECOND = 13
+
+PRECOND_JACOBI = 0
+PRECOND_BLOCK_JACOBI = 1
 
 # The symbols include/vsgb.h declares (checked by tests against the .so).
 EXPORTS = (
@@ -66,6 +70,7 @@ EXPORTS = (
     "vsgb_backend_name", "vsgb_solve_csr", "vsgb_build_dof_map", "vsgb_apply_forces",
     "vsgb_assemble_chexa8", "vsgb_copy_csr_lower", "vsgb_solve_assembled", "vsgb_mesh_upload",
     "vsgb_assemble_resident", "vsgb_rhs_upload", "vsgb_solve_resident",
+    "vsgb_host_alloc", "vsgb_host_free",
     "vsgb_solution_download", "vsgb_element_sensitivity", "vsgb_timer_start",
     "vsgb_timer_stop", "vsgb_time_spmv", "vsgb_kernel_launches", "vsgb_pcg_solve_noalloc",
 )
@@ -144,6 +149,8 @@ def load_library(build_if_missing: bool = False):
     L.vsgb_rhs_upload.argtypes = [vp, _f64p, c_int]
     L.vsgb_solve_resident.argtypes = [vp, ctypes.POINTER(VsgbStats)]
     L.vsgb_solution_download.argtypes = [vp, _f64p]
+    L.vsgb_host_alloc.argtypes = [vp, sz, ctypes.POINTER(vp)]
+    L.vsgb_host_free.argtypes = [vp, vp]
     L.vsgb_element_sensitivity.argtypes = [vp, _f64p, _f64p, _f64p]
     L.vsgb_timer_start.argtypes = [vp]
     L.vsgb_timer_stop.argtypes = [vp, ctypes.POINTER(c_dbl)]
@@ -188,6 +195,7 @@ class CsrData:
 class _Context:
     def __init__(self, ptr):
         self.ptr = ptr
+        self.pinned = []  # page-locked host blocks, freed with the context
 
     def check(self, rc: int):
         if rc != VSGB_OK:
@@ -200,7 +208,11 @@ class _Context:
 
     def close(self):
         if self.ptr:
-            load_library().vsgb_destroy(self.ptr)
+            L = load_library()
+            for p in self.pinned:
+                L.vsgb_host_free(self.ptr, p)
+            self.pinned = []
+            L.vsgb_destroy(self.ptr)
             self.ptr = None
 
     def __del__(self):
@@ -240,6 +252,26 @@ class Gb300PcgSolverBackend:
 
     def set_option(self, option: int, value: float):
         self._ctx.check(load_library().vsgb_set_option(self._ctx.ptr, option, float(value)))
+
+    def pinned_empty(self, shape, dtype=np.float64) -> np.ndarray:
+        """Uninitialised page-locked host array (vsgb_host_alloc) for the
+        host arrays handed to the library; valid until close()."""
+        dt = np.dtype(dtype)
+        shape = (int(shape),) if np.isscalar(shape) else tuple(int(x) for x in shape)
+        count = int(np.prod(shape))
+        nbytes = max(count * dt.itemsize, 1)
+        p = ctypes.c_void_p()
+        self._ctx.check(load_library().vsgb_host_alloc(self._ctx.ptr, nbytes, ctypes.byref(p)))
+        self._ctx.pinned.append(p.value)
+        buf = (ctypes.c_char * nbytes).from_address(p.value)
+        return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
+
+    def pinned_copy(self, a) -> np.ndarray:
+        """Page-locked copy of a host array (same shape and dtype)."""
+        a = np.asarray(a)
+        out = self.pinned_empty(a.shape, a.dtype)
+        out[...] = a
+        return out
 
     def solve(self, K: CsrData, F, factor_ratio_policy=None) -> np.ndarray:
         """SolverBackend::solve: K as CsrData, F (n,) or (n, nrhs) -> u."""
@@ -362,7 +394,9 @@ class ChexaAssembler:
 
     def upload(self, model, eq6, n):
         L = load_library()
-        eq3 = np.ascontiguousarray(np.asarray(eq6)[:, :3], np.int32).reshape(-1)
+        eq6 = np.asarray(eq6)
+        # an (N, 3) int32 table is passed as is (no copy); (N, 6) is sliced
+        eq3 = np.ascontiguousarray(eq6 if eq6.shape[1] == 3 else eq6[:, :3], np.int32).reshape(-1)
         form = np.ascontiguousarray(model.form, np.int32)
         rc = L.vsgb_mesh_upload(self.backend.context.ptr, model.n_nodes,
                                 np.ascontiguousarray(model.xyz, np.float64).reshape(-1), eq3,
@@ -393,11 +427,19 @@ class ChexaAssembler:
             load_library().vsgb_copy_csr_lower(self.backend.context.ptr, rp, ci, v))
         return CsrData(rp, ci, v, self.n, self.nnz_lower, True)
 
-    def solve(self, F) -> np.ndarray:
+    def solve(self, F, out=None) -> np.ndarray:
+        """u for F (n,) or (n, nrhs); out: optional (n,) float64 array that
+        receives u (single load case, e.g. a page-locked one)."""
         F = np.asarray(F, dtype=np.float64)
         nrhs = 1 if F.ndim == 1 else F.shape[1]
         Fc = np.ascontiguousarray(F.T if F.ndim == 2 else F).reshape(-1)
-        u = np.zeros(self.n * nrhs)
+        if out is not None:
+            if nrhs != 1 or out.dtype != np.float64 or out.shape != (self.n,) or \
+                    not out.flags.c_contiguous:
+                raise ValueError("out must be a contiguous (n,) float64 array, one load case")
+            u = out
+        else:
+            u = np.zeros(self.n * nrhs)
         st = VsgbStats()
         self.backend.context.check(load_library().vsgb_solve_assembled(
             self.backend.context.ptr, Fc, nrhs, u, ctypes.byref(st)))

@@ -58,6 +58,8 @@ struct vsgb_ctx {
   DevBuf<double> in_v;
 
   vsgb::PcgScalars* h_scal = nullptr;  // pinned
+  int* h_bad = nullptr;                // pinned: first bad conn / eq3 index of an upload
+  DevBuf<int> mesh_bad;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   long long launches = 0;
   int last_iters = 0;
@@ -215,6 +217,7 @@ void run_batched(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
 // both forms are bound by the FP64 pipe).
 bool use_batched(const vsgb_ctx* c, int nrhs) {
   if (nrhs < 2 || c->batched == 0 || !c->eng->multi_supported()) return false;
+  if (c->eng->precond() != 0 && c->batched == 1) return false;  // scalar Jacobi only
   if (c->batched == 2) return true;
   return nrhs >= (c->precision == VSGB_MIXED ? 4 : 10);
 }
@@ -284,6 +287,25 @@ void upload(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   if (bytes) VSGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
 }
 
+// Range check of every index the mesh kernels dereference: bad[0] = first
+// connectivity entry outside [0, n_nodes), bad[1] = first equation entry
+// outside [-1, n_dof) (INT_MAX when none).
+__global__ void k_check_mesh(long long n_conn, const int* __restrict__ conn, int n_nodes,
+                             long long n_eq, const int* __restrict__ eq3, int n_dof,
+                             int* __restrict__ bad) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+       k < n_conn + n_eq; k += stride) {
+    if (k < n_conn) {
+      const int v = conn[k];
+      if (v < 0 || v >= n_nodes) atomicMin(&bad[0], static_cast<int>(k));
+    } else {
+      const int v = eq3[k - n_conn];
+      if (v < -1 || v >= n_dof) atomicMin(&bad[1], static_cast<int>(k - n_conn));
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -315,7 +337,8 @@ int vsgb_create(int device, double tol, int max_iters, int precision, vsgb_ctx**
       cudaStreamCreateWithPriority(&c->topo, cudaStreamNonBlocking, prio_low) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->topo_done, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->topo_start, cudaEventDisableTiming) != cudaSuccess ||
-      cudaMallocHost(&c->h_scal, sizeof(vsgb::PcgScalars) * 2) != cudaSuccess) {
+      cudaMallocHost(&c->h_scal, sizeof(vsgb::PcgScalars) * 2) != cudaSuccess ||
+      cudaMallocHost(&c->h_bad, sizeof(int) * 2) != cudaSuccess) {
     vsgb_destroy(c);
     return VSGB_ERR_CUDA;
   }
@@ -338,6 +361,7 @@ void vsgb_destroy(vsgb_ctx* c) {
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->h_scal) cudaFreeHost(c->h_scal);
+  if (c->h_bad) cudaFreeHost(c->h_bad);
   if (c->topo_done) cudaEventDestroy(c->topo_done);
   if (c->topo_start) cudaEventDestroy(c->topo_start);
   if (c->topo) cudaStreamDestroy(c->topo);
@@ -389,6 +413,13 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
       case VSGB_OPT_ADAPTIVE_INNER:
         c->eng->set_adaptive_inner(value != 0.0);
         break;
+      case VSGB_OPT_PRECOND: {
+        const int p = static_cast<int>(value);
+        if (p != VSGB_PRECOND_JACOBI && p != VSGB_PRECOND_BLOCK_JACOBI)
+          throw Error(VSGB_ERR_INVALID, "preconditioner must be 0 (Jacobi) or 1 (3x3 block Jacobi)");
+        c->eng->set_precond(p);
+        break;
+      }
       case VSGB_OPT_BATCHED: {
         const int b = static_cast<int>(value);
         if (b < 0 || b > 2) throw Error(VSGB_ERR_INVALID, "batched mode must be 0, 1 or 2");
@@ -415,10 +446,12 @@ int vsgb_device_name(vsgb_ctx* c, char* buf, size_t len) {
 
 int vsgb_backend_name(vsgb_ctx* c, char* buf, size_t len) {
   if (!c || !buf || len == 0) return VSGB_ERR_INVALID;
-  std::snprintf(buf, len, "%s",
-                c->precision == VSGB_MIXED
-                    ? "CUDA GB300 mixed-precision PCG + Jacobi, FP64 refinement on GPU (GPU)"
-                    : "CUDA GB300 PCG + Jacobi float64 (GPU)");
+  const char* pre = c->eng && c->eng->precond() != 0 ? "3x3 block Jacobi" : "Jacobi";
+  if (c->precision == VSGB_MIXED)
+    std::snprintf(buf, len, "CUDA GB300 mixed-precision PCG + %s, FP64 refinement on GPU (GPU)",
+                  pre);
+  else
+    std::snprintf(buf, len, "CUDA GB300 PCG + %s float64 (GPU)", pre);
   return VSGB_OK;
 }
 
@@ -472,17 +505,11 @@ int vsgb_mesh_upload(vsgb_ctx* c, int n_nodes, const double* node_xyz, const int
     if (n_nodes < 0 || n_elem < 0 || n_dof < 0 || (n_nodes > 0 && (!node_xyz || !node_eq3)) ||
         (n_elem > 0 && (!conn || !E || !nu)))
       throw Error(VSGB_ERR_INVALID, "vsgb_mesh_upload: invalid argument");
-    if (n_elem > INT_MAX / 8) throw Error(VSGB_ERR_LIMIT, "too many elements");
+    if (n_elem > INT_MAX / 8 || n_nodes > INT_MAX / 3)
+      throw Error(VSGB_ERR_LIMIT, "too many elements or nodes");
     c->u_cases = 0;
-    // Every index a kernel will dereference is range-checked here, on the host.
-    for (long long k = 0; k < 8LL * n_elem; ++k)
-      if (conn[k] < 0 || conn[k] >= n_nodes)
-        throw Error(VSGB_ERR_INVALID, "element index " + std::to_string(k / 8) +
-                                          " references a node index out of range");
-    for (long long k = 0; k < 3LL * n_nodes; ++k)
-      if (node_eq3[k] < -1 || node_eq3[k] >= n_dof)
-        throw Error(VSGB_ERR_INVALID, "equation index out of range at node index " +
-                                          std::to_string(k / 3));
+    c->mesh_ok = false;
+    c->assembled = false;
     cudaStream_t s = c->stream;
     c->n_nodes = n_nodes;
     c->n_elem = n_elem;
@@ -502,9 +529,28 @@ int vsgb_mesh_upload(vsgb_ctx* c, int n_nodes, const double* node_xyz, const int
       c->form.reserve(static_cast<size_t>(n_elem) + 1);
       upload(c->form.ptr, formulation, sizeof(int) * n_elem, s);
     }
+    // Every index a kernel will dereference is range-checked here, on the
+    // device, before any kernel reads the mesh.
+    c->mesh_bad.reserve(2);
+    c->h_bad[0] = c->h_bad[1] = INT_MAX;
+    upload(c->mesh_bad.ptr, c->h_bad, sizeof(int) * 2, s);
+    const long long n_conn = 8LL * n_elem, n_eq = 3LL * n_nodes;
+    if (n_conn + n_eq > 0) {
+      k_check_mesh<<<4 * c->num_sms, 256, 0, s>>>(n_conn, c->conn.ptr, n_nodes, n_eq,
+                                                 c->eq3.ptr, n_dof, c->mesh_bad.ptr);
+      VSGB_LAUNCH_CHECK();
+      c->eng->add_launches(1);
+    }
+    VSGB_CUDA(cudaMemcpyAsync(c->h_bad, c->mesh_bad.ptr, sizeof(int) * 2, cudaMemcpyDeviceToHost,
+                              s));
     VSGB_CUDA(cudaStreamSynchronize(s));
+    if (c->h_bad[0] != INT_MAX)
+      throw Error(VSGB_ERR_INVALID, "element index " + std::to_string(c->h_bad[0] / 8) +
+                                        " references a node index out of range");
+    if (c->h_bad[1] != INT_MAX)
+      throw Error(VSGB_ERR_INVALID, "equation index out of range at node index " +
+                                        std::to_string(c->h_bad[1] / 3));
     c->mesh_ok = true;
-    c->assembled = false;
   });
 }
 
@@ -616,6 +662,24 @@ int vsgb_solution_download(vsgb_ctx* c, double* u_out) {
     VSGB_CUDA(cudaMemcpyAsync(u_out, c->u.ptr, sizeof(double) * c->K.n * c->nrhs,
                               cudaMemcpyDeviceToHost, c->stream));
     VSGB_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int vsgb_host_alloc(vsgb_ctx* c, size_t bytes, void** out) {
+  return guarded(c, [&] {
+    if (!out) throw Error(VSGB_ERR_INVALID, "vsgb_host_alloc: null output");
+    *out = nullptr;
+    if (cudaMallocHost(out, bytes ? bytes : 1) != cudaSuccess) {
+      cudaGetLastError();
+      *out = nullptr;
+      throw Error(VSGB_ERR_CUDA, "cudaMallocHost of " + std::to_string(bytes) + " bytes failed");
+    }
+  });
+}
+
+int vsgb_host_free(vsgb_ctx* c, void* p) {
+  return guarded(c, [&] {
+    if (p) VSGB_CUDA(cudaFreeHost(p));
   });
 }
 

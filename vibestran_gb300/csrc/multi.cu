@@ -729,6 +729,8 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
                             double inner_tol, int max_iters, int max_solves, cudaStream_t s,
                             std::vector<SolveResult>& res) {
   if (!use_bsr_) throw Error(VSGB_ERR_STATE, "batched PCG needs the 3x3 block operator");
+  if (precond_ != 0)
+    throw Error(VSGB_ERR_INVALID, "the batched PCG runs the scalar Jacobi preconditioner only");
   if (mixed && !(bsr_.has32 && has32_))
     throw Error(VSGB_ERR_STATE, "batched mixed PCG needs the FP32 operator copy");
   if (!multi_) multi_ = new MultiWork();

@@ -843,14 +843,33 @@ void PcgEngine::resident_end(cudaStream_t s) {
   }
 }
 
+bool PcgEngine::block_jacobi(bool mixed, cudaStream_t s) {
+  if (precond_ == 0) return false;
+  if (!resident_used(mixed))
+    throw Error(VSGB_ERR_INVALID,
+                "3x3 block Jacobi needs the persistent solve on the 3x3 block operator");
+  if (bj_gen_ != generation_) {
+    const int bad = resident_block_jacobi(bsr_, res_, has32_, num_sms_, s);
+    ++launches_;
+    if (bad >= 0)
+      throw Error(VSGB_ERR_SINGULAR, "GB300 PCG: the diagonal block of equations " +
+                                         std::to_string(3 * bad) + ".." +
+                                         std::to_string(3 * bad + 2) +
+                                         " is not positive definite");
+    bj_gen_ = generation_;
+  }
+  return true;
+}
+
 void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStream_t s,
                            PcgScalars* host, SolveResult& res) {
   ensure_vectors(false);
   resident_ms_ = 0.0;
   resident_iters_ = 0;
+  const bool bj = block_jacobi(false, s);
   if (resident_used(false)) {
     resident_begin(s, bsr_.val64.ptr, static_cast<size_t>(bsr_.steps) * 288 * sizeof(double));
-    resident_solve64(bsr_, res_, d_f, u_.ptr, scal_.ptr, tol, max_iters, s, op_->dinv.ptr);
+    resident_solve64(bsr_, res_, d_f, u_.ptr, scal_.ptr, tol, max_iters, s, op_->dinv.ptr, bj);
     resident_end(s);
     ++launches_;
     read_scalars(s, host, 0);
@@ -898,6 +917,7 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
   ensure_vectors(true);
   resident_ms_ = 0.0;
   resident_iters_ = 0;
+  const bool bj = block_jacobi(true, s);
   // Outer record (index 1) holds ||f||, the true residual and the RHS scale.
   k_outer_init<<<vec_grid_, kThreads, 0, s>>>(n_, d_f, r_.ptr, u_.ptr, scal_.ptr + 1,
                                               partials_.ptr, counters_.ptr + 3);
@@ -930,7 +950,7 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       // accumulation u += delta / scale.
       resident_begin(s, bsr_.val32.ptr, static_cast<size_t>(bsr_.steps) * 288 * sizeof(float));
       resident_solve32(bsr_, res_, r_.ptr, u_.ptr, scal_.ptr, scal_.ptr + 1, itol,
-                       max_iters, s, op_->dinv.ptr);
+                       max_iters, s, op_->dinv.ptr, bj);
       resident_end(s);
       ++launches_;
       read_scalars(s, host, 0);

@@ -59,6 +59,10 @@ class PcgEngine {
   // Mixed refinement: loosen later inner tolerances to what the outer
   // tolerance still needs (never tighter than the inner tolerance).
   void set_adaptive_inner(bool on) { adaptive_inner_ = on; }
+  // 0: scalar Jacobi; 1: 3x3 block Jacobi (persistent solve on the block
+  // operator only).
+  void set_precond(int p) { precond_ = p; }
+  int precond() const { return precond_; }
   bool resident_used(bool mixed) const {
     return resident_ && use_bsr_ && (mixed ? res_.ok32 : res_.ok64);
   }
@@ -89,6 +93,7 @@ class PcgEngine {
   void launch_batch64(cudaStream_t s);
   void launch_batch32(cudaStream_t s);
   void iterate(cudaStream_t s, bool fp32, PcgScalars* host);
+  bool block_jacobi(bool mixed, cudaStream_t s);  // builds the blocks on first use
 
   int num_sms_;
   const AssembledCsr* op_ = nullptr;
@@ -129,6 +134,8 @@ class PcgEngine {
   void resident_end(cudaStream_t s);    // right after it (waits for it)
   bool l2_persist_ = false;
   bool adaptive_inner_ = true;
+  int precond_ = 0;
+  unsigned bj_gen_ = ~0u;  // operator generation the block inverses belong to
   bool l2_window_set_ = false;
   size_t l2_persist_max_ = 0;   // device limit (0: not supported)
   size_t l2_window_max_ = 0;

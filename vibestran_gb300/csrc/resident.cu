@@ -41,6 +41,7 @@ struct ResArgs {
   const int* __restrict__ cta_slice;
   const int* __restrict__ cta_win;
   const double* __restrict__ dinv;
+  const T* __restrict__ bj;  // 3x3 block Jacobi: inverse diagonal blocks, 6 per node
   const double* __restrict__ rhs;
   double* __restrict__ u_out;
   T* z4;
@@ -234,7 +235,21 @@ __device__ __forceinline__ void st3(double* p, double a, double b, double c) {
   p[2] = c;
 }
 
-template <typename T, bool kWindow, bool kMixed>
+// z = B r for one node, B the symmetric inverse of its diagonal block stored
+// as its upper triangle (xx, xy, xz, yy, yz, zz).
+template <typename T>
+__device__ __forceinline__ void bj_apply(const T* __restrict__ b, const T (&r)[3], T (&z)[3]) {
+  const T b0 = __ldg(b), b1 = __ldg(b + 1), b2 = __ldg(b + 2);
+  const T b3 = __ldg(b + 3), b4 = __ldg(b + 4), b5 = __ldg(b + 5);
+  z[0] = rfma(b0, r[0], rfma(b1, r[1], b2 * r[2]));
+  z[1] = rfma(b1, r[0], rfma(b3, r[1], b4 * r[2]));
+  z[2] = rfma(b2, r[0], rfma(b4, r[1], b5 * r[2]));
+}
+
+// kBJ: 3x3 block Jacobi (z = B_I r_I per node) instead of the scalar one; the
+// fourth own-row vector then holds z itself instead of diag^-1, and the row
+// loops of the init and of phase 2 run over nodes.
+template <typename T, bool kWindow, bool kMixed, bool kBJ>
 __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[96];
@@ -247,6 +262,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   const int nrows = max(0, min(24 * s1, a.n) - g0);
   // Own-row vectors r, p, Ap, diag^-1 (and the solution accumulator u unless
   // it lives in global memory; z = r diag^-1 is recomputed where needed).
+  // With kBJ the diag^-1 slot holds z.
   T* RR = reinterpret_cast<T*>(smem);
   T* P = RR + a.rows_max;
   T* AP = P + a.rows_max;
@@ -262,7 +278,32 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
 
   // ── init: r = rhs, u = 0, z = r / diag, p = 0 ──
   T acc2[2] = {T(0), T(0)};
-  for (int lr = tid; lr < nrows; lr += kResThreads) {
+  if (kBJ) {
+    for (int ln = tid; 3 * ln < nrows; ln += kResThreads) {
+      const int lr = 3 * ln, R = 8 * s0 + ln;
+      T rv[3], zv[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const double f = a.rhs[g0 + lr + q];
+        rv[q] = kMixed ? static_cast<T>(f * scale) : static_cast<T>(f);
+      }
+      bj_apply(a.bj + 6 * static_cast<size_t>(R), rv, zv);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        RR[lr + q] = rv[q];
+        U[lr + q] = T(0);
+        P[lr + q] = T(0);
+        AP[lr + q] = T(0);
+        D[lr + q] = zv[q];
+        acc2[0] = rfma(rv[q], rv[q], acc2[0]);
+        acc2[1] = rfma(rv[q], zv[q], acc2[1]);
+      }
+      st3(a.z4 + 4 * static_cast<size_t>(R), zv[0], zv[1], zv[2]);
+      st3(a.p4a + 4 * static_cast<size_t>(R), T(0), T(0), T(0));
+      st3(a.p4b + 4 * static_cast<size_t>(R), T(0), T(0), T(0));
+    }
+  }
+  for (int lr = tid; !kBJ && lr < nrows; lr += kResThreads) {
     const int g = g0 + lr;
     const int R = g / 3, q = g - 3 * R;
     const double d = a.dinv[g];
@@ -435,7 +476,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       if (q < 3 && R < a.nb) {
         const int lr = 24 * ls + 3 * r + q;
         const T yq = q == 0 ? y0 : (q == 1 ? y1 : y2);
-        const T pn = rfma(tb, P[lr], RR[lr] * D[lr]);  // z = r diag^-1, as stored in z4
+        // z = r diag^-1 (or the stored block Jacobi z), as in z4
+        const T pn = rfma(tb, P[lr], kBJ ? D[lr] : RR[lr] * D[lr]);
         P[lr] = pn;
         AP[lr] = yq;
         if (!(kWindow && kKeepWindowP)) p_new[4 * R + q] = pn;
@@ -479,7 +521,27 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     const T ta = static_cast<T>(s_sc[0]);
     // ── phase 2: u, r, z updates on the own rows ──
     acc2[0] = acc2[1] = T(0);
-    for (int lr = tid; lr < nrows; lr += kResThreads) {
+    if (kBJ) {
+      for (int ln = tid; 3 * ln < nrows; ln += kResThreads) {
+        const int lr = 3 * ln, R = 8 * s0 + ln;
+        T rv[3], zv[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          U[lr + q] = rfma(ta, P[lr + q], U[lr + q]);
+          rv[q] = rfma(-ta, AP[lr + q], RR[lr + q]);
+        }
+        bj_apply(a.bj + 6 * static_cast<size_t>(R), rv, zv);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          RR[lr + q] = rv[q];
+          D[lr + q] = zv[q];
+          acc2[0] = rfma(rv[q], zv[q], acc2[0]);
+          acc2[1] = rfma(rv[q], rv[q], acc2[1]);
+        }
+        st3(a.z4 + 4 * static_cast<size_t>(R), zv[0], zv[1], zv[2]);
+      }
+    }
+    for (int lr = tid; !kBJ && lr < nrows; lr += kResThreads) {
       const int g = g0 + lr;
       const int R = g / 3, q = g - 3 * R;
       U[lr] = rfma(ta, P[lr], U[lr]);
@@ -587,11 +649,55 @@ __global__ void k_slice_minmax(int nslices, const int* __restrict__ slice_ptr,
   }
 }
 
+// Thread per node: finds the diagonal block among the node's stored blocks
+// (entries 4t+q < rowlen of its slice row; padding comes after them), and
+// inverts its symmetric part (upper triangle) by cofactors in FP64.  A block
+// is accepted when its leading minors are positive (SPD, Sylvester).
+__global__ void k_block_jacobi_inverse(int nb, const int* __restrict__ slice_ptr,
+                                       const int* __restrict__ rowlen,
+                                       const int* __restrict__ cols,
+                                       const double* __restrict__ v64, double* __restrict__ bj64,
+                                       float* __restrict__ bj32, int* __restrict__ bad) {
+  const int R = blockIdx.x * blockDim.x + threadIdx.x;
+  if (R >= nb) return;
+  const int sl = R >> 3, ln0 = (R & 7) * 4, len = rowlen[R];
+  const long long sp = slice_ptr[sl];
+  long long at = -1;
+  for (int j = 0; j < len && at < 0; ++j) {
+    const long long o = (sp + (j >> 2)) * 32 + ln0 + (j & 3);
+    if (cols[o] == R) at = (sp + (j >> 2)) * 288 + ln0 + (j & 3);
+  }
+  if (at < 0) {
+    atomicMin(bad, R);
+    return;
+  }
+  const double a00 = v64[at], a01 = v64[at + 32], a02 = v64[at + 64];
+  const double a11 = v64[at + 128], a12 = v64[at + 160], a22 = v64[at + 256];
+  const double c00 = a11 * a22 - a12 * a12;
+  const double c01 = a02 * a12 - a01 * a22;
+  const double c02 = a01 * a12 - a02 * a11;
+  const double c11 = a00 * a22 - a02 * a02;
+  const double c12 = a01 * a02 - a00 * a12;
+  const double c22 = a00 * a11 - a01 * a01;
+  const double det = a00 * c00 + a01 * c01 + a02 * c02;
+  if (!(a00 > 0.0) || !(c22 > 0.0) || !(det > 0.0)) {
+    atomicMin(bad, R);
+    return;
+  }
+  const double id = 1.0 / det;
+  const double b[6] = {c00 * id, c01 * id, c02 * id, c11 * id, c12 * id, c22 * id};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    bj64[6 * static_cast<size_t>(R) + k] = b[k];
+    if (bj32) bj32[6 * static_cast<size_t>(R) + k] = static_cast<float>(b[k]);
+  }
+}
+
 template <typename T, bool kWindow, bool kMixed>
 void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const double* rhs,
                      double* u, PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
-                     T* z4, T* p4a, T* p4b, const double* dinv, size_t smem, T* u_glob,
-                     cudaStream_t s) {
+                     T* z4, T* p4a, T* p4b, const double* dinv, const T* bj, size_t smem,
+                     T* u_glob, cudaStream_t s) {
   ResArgs<T> a;
   a.nb = B.nb;
   a.n = 3 * B.nb;
@@ -601,6 +707,7 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   a.cta_slice = P.cta_slice.ptr;
   a.cta_win = P.cta_win.ptr;
   a.dinv = dinv;
+  a.bj = bj;
   a.rhs = rhs;
   a.u_out = u;
   a.z4 = z4;
@@ -618,25 +725,31 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   VSGB_CUDA(cudaMemsetAsync(P.barrier.ptr, 0, sizeof(unsigned), s));
   VSGB_CUDA(cudaMemsetAsync(P.abort_flag.ptr, 0, sizeof(int), s));
   void* args[] = {&a};
-  VSGB_CUDA(cudaLaunchCooperativeKernel(
-      reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed>), dim3(P.ctas),
-      dim3(kResThreads), args, smem, s));
+  const void* fn = bj ? reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, true>)
+                      : reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false>);
+  VSGB_CUDA(cudaLaunchCooperativeKernel(fn, dim3(P.ctas), dim3(kResThreads), args, smem, s));
 }
 
+// Both preconditioner forms of a kernel take the same shared memory; the plan
+// holds when both fit one CTA per SM.
 template <typename T, bool kWindow, bool kMixed>
 bool configure(size_t smem, int* blocks) {
-  const void* fn = reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed>);
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(smem)) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
+  const void* fns[2] = {reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false>),
+                        reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, true>)};
+  for (const void* fn : fns) {
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, kResThreads, smem) !=
+            cudaSuccess ||
+        *blocks < 1) {
+      cudaGetLastError();
+      return false;
+    }
   }
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, kResThreads, smem) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return *blocks >= 1;
+  return true;
 }
 
 }  // namespace
@@ -760,31 +873,53 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
   VSGB_CUDA(cudaStreamSynchronize(s));
 }
 
+int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, int num_sms,
+                          cudaStream_t s) {
+  (void)num_sms;
+  const size_t m = 6 * static_cast<size_t>(B.nb > 0 ? B.nb : 1);
+  P.bj64.reserve(m);
+  if (need32) P.bj32.reserve(m);
+  P.bj_bad.reserve(1);
+  const int big = INT_MAX;
+  VSGB_CUDA(cudaMemcpyAsync(P.bj_bad.ptr, &big, sizeof(int), cudaMemcpyHostToDevice, s));
+  k_block_jacobi_inverse<<<(B.nb + 255) / 256, 256, 0, s>>>(
+      B.nb, B.slice_ptr.ptr, B.rowlen.ptr, B.cols.ptr, B.val64.ptr, P.bj64.ptr,
+      need32 ? P.bj32.ptr : nullptr, P.bj_bad.ptr);
+  VSGB_LAUNCH_CHECK();
+  int bad = big;
+  VSGB_CUDA(cudaMemcpyAsync(&bad, P.bj_bad.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  return bad == big ? -1 : bad;
+}
+
 void resident_solve32(const BsrSell& B, ResidentPlan& P, const double* r64, double* u64,
                       PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
-                      cudaStream_t s, const double* dinv) {
+                      cudaStream_t s, const double* dinv, bool block_jacobi) {
   float* ug = P.ug32 ? P.u32g.ptr : nullptr;
+  const float* bj = block_jacobi ? P.bj32.ptr : nullptr;
   if (P.win32)
     launch_resident<float, true, true>(B, P, B.val32.ptr, r64, u64, S, O, tol, max_iters,
-                                       P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, P.smem32, ug, s);
+                                       P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, bj, P.smem32, ug,
+                                       s);
   else
     launch_resident<float, false, true>(B, P, B.val32.ptr, r64, u64, S, O, tol, max_iters,
-                                        P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, P.smem32, ug,
-                                        s);
+                                        P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, bj, P.smem32,
+                                        ug, s);
 }
 
 void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double* u,
                       PcgScalars* S, double tol, int max_iters, cudaStream_t s,
-                      const double* dinv) {
+                      const double* dinv, bool block_jacobi) {
   // the FP64 solve accumulates straight into its output when u is global
   double* ug = P.ug64 ? u : nullptr;
+  const double* bj = block_jacobi ? P.bj64.ptr : nullptr;
   if (P.win64)
     launch_resident<double, true, false>(B, P, B.val64.ptr, f, u, S, nullptr, tol, max_iters,
-                                         P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, P.smem64, ug,
-                                         s);
+                                         P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, bj, P.smem64,
+                                         ug, s);
   else
     launch_resident<double, false, false>(B, P, B.val64.ptr, f, u, S, nullptr, tol, max_iters,
-                                          P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, P.smem64,
+                                          P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, bj, P.smem64,
                                           ug, s);
 }
 

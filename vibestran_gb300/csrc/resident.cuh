@@ -1,5 +1,6 @@
-// vibestran_gb300/csrc/resident.cuh — persistent (SM-resident) Jacobi PCG on the
-// 3x3 block operator: one cooperative launch runs every iteration of a solve.
+// vibestran_gb300/csrc/resident.cuh — persistent (SM-resident) Jacobi or 3x3
+// block Jacobi PCG on the 3x3 block operator: one cooperative launch runs
+// every iteration of a solve.
 #pragma once
 
 #include <vector>
@@ -23,8 +24,13 @@ struct ResidentPlan {
   DevBuf<unsigned> barrier;         // monotonic arrival counter
   DevBuf<int> abort_flag;           // set by a barrier that gave up waiting
   DevBuf<float> u32g;                       // FP32 solution accumulator when ug32
-  DevBuf<float> z4f, p4fa, p4fb, dinv4f;    // node-padded FP32 vectors (4 per node)
-  DevBuf<double> z4d, p4da, p4db, dinv4d;   // node-padded FP64 vectors
+  DevBuf<float> z4f, p4fa, p4fb;    // node-padded FP32 vectors (4 per node)
+  DevBuf<double> z4d, p4da, p4db;   // node-padded FP64 vectors
+  // 3x3 block Jacobi: inverse diagonal block of every node, upper triangle
+  // (xx, xy, xz, yy, yz, zz), FP64 and its FP32 copy for the inner solve
+  DevBuf<double> bj64;
+  DevBuf<float> bj32;
+  DevBuf<int> bj_bad;               // smallest node whose block is not SPD
 };
 
 // Plans CTA ranges / windows and allocates the padded vectors; leaves both
@@ -32,16 +38,23 @@ struct ResidentPlan {
 void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int device,
                       int num_sms, ResidentPlan& P, cudaStream_t s);
 
+// Inverts the 3x3 diagonal block of every node of the FP64 operator into
+// P.bj64 (and P.bj32 when need32).  Returns -1, or the smallest node whose
+// block is not symmetric positive definite (nothing is usable then).
+int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, int num_sms,
+                          cudaStream_t s);
+
 // One FP32 inner solve: rhs = (float)(r64 * O->scale); on convergence
-// u64 += delta / O->scale.  Final counts/flags land in *S.
+// u64 += delta / O->scale.  Final counts/flags land in *S.  block_jacobi
+// selects the 3x3 block preconditioner in P.bj32 instead of dinv.
 void resident_solve32(const BsrSell& B, ResidentPlan& P, const double* r64, double* u64,
                       PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
-                      cudaStream_t s, const double* dinv);
+                      cudaStream_t s, const double* dinv, bool block_jacobi = false);
 
 // One FP64 solve of K u = f; u written (zeros on a zero RHS).
 void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double* u,
                       PcgScalars* S, double tol, int max_iters, cudaStream_t s,
-                      const double* dinv);
+                      const double* dinv, bool block_jacobi = false);
 
 // Flag set in PcgScalars::flags when a grid barrier gave up waiting.
 constexpr int kFlagResidentAbort = 64;
