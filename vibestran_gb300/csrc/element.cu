@@ -49,13 +49,17 @@ struct alignas(16) WarpSmem {
   double C[6];            // EAS: sum_gp xi_p xi_q / detJ  (p <= q: 00 01 02 11 12 22)
   double idet[8];         // 1 / detJ at the Gauss points
   double c0[9];           // detJ0 * J0^-1
-  double L[9][9];         // Cholesky factor of Kaa
-  double Linv[9];         // 1 / L[i][i]
-  double Kua[24][9];
+  double L[9][9];         // unit lower factor of Kaa = L D L^T (strictly lower part)
+  double Dinv[9];         // 1 / D[i]
+  double col[9];          // unscaled pivot column of the current elimination step
+  union {
+    double Kua[24][9];
+    double X[9][24];      // L^-1 Kau, written over Kua once every lane has read its row
+  };
   // Phase D inputs.
   double M[kPairs][9];    // moment matrices M_AB (row i, col j)
   double tr[kPairs];      // their traces
-  double X[9][24];        // L^-1 Kau (Kaa = L L^T)
+  double XD[9][24];       // D^-1 L^-1 Kau
   double j0[12];          // J0^-1 (9), detJ0
 };
 static_assert(offsetof(WarpSmem, M) >= sizeof(double) * 576, "Ke staging over g..Kua");
@@ -65,15 +69,15 @@ static_assert(sizeof(WarpSmem) % 16 == 0, "per-warp areas and the Ke copy need 1
 __device__ __forceinline__ int pp_first(int u) { return u < 3 ? 0 : (u < 5 ? 1 : 2); }
 __device__ __forceinline__ int pp_second(int u) { return u < 3 ? u : (u < 5 ? u - 2 : 2); }
 
-// 1/sqrt(d) in FP64 from an FP32 seed and two Newton-Raphson steps
-// y <- y * (1.5 - 0.5 d y^2): quadratic convergence takes the ~2^-22 seed error
-// below FP64 rounding.  Outside the FP32 range the library square root is used.
-__device__ __forceinline__ double rsqrt_nr(double d) {
-  if (!(d > 1e-30 && d < 1e30)) return 1.0 / sqrt(d);
-  double y = static_cast<double>(rsqrtf(static_cast<float>(d)));
-  const double h = 0.5 * d;
-  y = y * fma(-h * y, y, 1.5);
-  y = y * fma(-h * y, y, 1.5);
+// 1/d in FP64 from an FP32 seed and two Newton-Raphson steps
+// y <- y + y (1 - d y): quadratic convergence takes the ~2^-23 seed error
+// below FP64 rounding (the result is within an ulp or so of the rounded
+// quotient).  Outside the FP32 range the FP64 division is used.
+__device__ __forceinline__ double rcp_nr(double d) {
+  if (!(d > 1e-30 && d < 1e30)) return 1.0 / d;
+  double y = static_cast<double>(__frcp_rn(static_cast<float>(d)));
+  y = fma(y, fma(-d, y, 1.0), y);
+  y = fma(y, fma(-d, y, 1.0), y);
   return y;
 }
 
@@ -143,6 +147,16 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
   // Gauss point coordinates xi_p(gp) (gp = 4 i_xi + 2 i_eta + i_zeta) and the
   // products xi_p xi_q of the six enhancement pairs.
   __shared__ double s_par[3][8], s_pp[6][8];
+  // |dN_n/dxi_r| at a Gauss point is 0.125 (1 +- g)(1 +- g), g = 1/sqrt(3):
+  // s_mag[k] with k factors (1 + g), each formed as (0.125 fa) fb with the
+  // factors fa = fma(+-1, g, 1) of the direct evaluation (so bit for bit the
+  // same value); s_mag[3] = 0.125 at the centroid.
+  __shared__ double s_mag[4];
+  if (threadIdx.x < 4) {
+    const double fm = fma(-1.0, gpt, 1.0), fp = fma(1.0, gpt, 1.0);
+    const int k = threadIdx.x;
+    s_mag[k] = k == 3 ? 0.125 : (0.125 * (k == 2 ? fp : fm)) * (k == 0 ? fm : fp);
+  }
   if (threadIdx.x < 24) {
     const int p = threadIdx.x >> 3, q = threadIdx.x & 7;
     s_par[p][q] = ((q >> (2 - p)) & 1) ? gpt : -gpt;
@@ -177,31 +191,28 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
     const bool act = lane < 27;
     const int gp = act ? lane / 3 : 8, rr = act ? lane - 3 * (lane / 3) : lane - 27 < 3 ? lane - 27 : 0;
     const int l0 = 3 * gp;  // lane holding row 0 of this point
-    double par[3] = {0.0, 0.0, 0.0};
-    if (gp < 8) {
-      // Gauss point order of the reference loops: xi slowest, zeta fastest.
-      par[0] = (gp & 4) ? gpt : -gpt;
-      par[1] = (gp & 2) ? gpt : -gpt;
-      par[2] = (gp & 1) ? gpt : -gpt;
-    }
     // dN_n/dxi_r = (0.125 s_r(n)) (1 + s_a(n) xi_a) (1 + s_b(n) xi_b), (a, b)
-    // the other two axes in increasing order.  Node signs s_k(n) of the CHEXA8
-    // node order (src/elements/solid_elements.cpp:76-93) as bit masks, bit n
-    // set for +1: xi {-,+,+,-,-,+,+,-}, eta {-,-,+,+,-,-,+,+}, zeta {-,-,-,-,+,+,+,+}.
+    // the other two axes in increasing order, xi_k = +-g at the Gauss points
+    // (gp bit 2 - k set for +g: xi slowest, zeta fastest, the reference's loop
+    // order) and 0 at the centroid.  Node signs s_k(n) of the CHEXA8 node
+    // order (src/elements/solid_elements.cpp:76-93) as bit masks, bit n set
+    // for +1: xi {-,+,+,-,-,+,+,-}, eta {-,-,+,+,-,-,+,+}, zeta {-,-,-,-,+,+,+,+}.
+    // A factor is 1 + g where the node sign and the point coordinate agree, so
+    // the value is a signed entry of s_mag: selects and a sign bit, no FP64
+    // arithmetic.
     constexpr unsigned kPos[3] = {0x66u, 0xCCu, 0xF0u};
     const int ax1 = rr == 0 ? 1 : 0, ax2 = rr == 2 ? 1 : 2;
     const unsigned m0 = kPos[0], m1 = kPos[1], m2 = kPos[2];
     const unsigned ms = rr == 0 ? m0 : (rr == 1 ? m1 : m2);
     const unsigned ma = ax1 == 0 ? m0 : m1;
     const unsigned mb = ax2 == 1 ? m1 : m2;
-    const double pa = ax1 == 0 ? par[0] : par[1];
-    const double pb = ax2 == 1 ? par[1] : par[2];
+    const unsigned ga = (gp >> (2 - ax1)) & 1u, gb = (gp >> (2 - ax2)) & 1u;
     double dNr[8];
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
-      const double fa = fma(((ma >> n) & 1u) ? 1.0 : -1.0, pa, 1.0);
-      const double fb = fma(((mb >> n) & 1u) ? 1.0 : -1.0, pb, 1.0);
-      dNr[n] = (((ms >> n) & 1u) ? 0.125 : -0.125) * fa * fb;
+      const int k = gp == 8 ? 3 : static_cast<int>((((ma >> n) & 1u) == ga) + (((mb >> n) & 1u) == gb));
+      const unsigned long long neg = ((ms >> n) & 1u) ? 0ull : 0x8000000000000000ull;
+      dNr[n] = __longlong_as_double(__double_as_longlong(s_mag[k]) ^ neg);
     }
     double Jr[3];
 #pragma unroll
@@ -336,16 +347,18 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
 
     double* ke_s = &s.g[0][0][0];  // Ke staging over g..Kua (EAS only; SRI writes global)
     if (!sri) {
-      // ── Phase C: Kaa Cholesky (lane 0) and Kua ──
+      // ── Phase C: Kaa = L D L^T and Kua ──
       for (int t = lane; t < 24 * 9; t += 32) {
         const int r = t / 9, k = t - 9 * r;
         s.Kua[r][k] = kval(s, lam, mu, r / 3, r % 3, 8 + k / 3, k % 3);
       }
-      // Right-looking Cholesky of Kaa spread over the warp: per column one lane
-      // forms the pivot, the lanes below scale the column and the trailing
-      // triangle (<= 36 entries) is updated by all lanes.  Every FP64 warp
-      // instruction occupies GB300's FP64 pipe regardless of active lanes, so
-      // the serial (one-lane) form costs ~5x more.
+      // Right-looking L D L^T factorisation of Kaa spread over the warp (the
+      // condensation needs Kua Kaa^-1 Kau only, which Eigen's LLT at
+      // :1201-1204 gives as well): per column one lane forms the pivot
+      // reciprocal, the lanes below scale the column and the trailing triangle
+      // (<= 36 entries) is updated by all lanes.  Every FP64 warp instruction
+      // occupies GB300's FP64 pipe regardless of active lanes, so the serial
+      // (one-lane) form costs ~5x more, and the pivot needs no square root.
       for (int t = lane; t < 45; t += 32) {
         const int i = static_cast<int>((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f + 1e-4f);
         const int k = t - i * (i + 1) / 2;
@@ -360,39 +373,46 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
             fail = 1;
             d = 1.0;
           }
-          const double inv = rsqrt_nr(d);
-          s.L[jc][jc] = d * inv;
-          s.Linv[jc] = inv;
+          s.Dinv[jc] = rcp_nr(d);
         }
         __syncwarp();
-        const double inv = s.Linv[jc];
-        if (lane > jc && lane < 9) s.L[lane][jc] *= inv;
+        const double inv = s.Dinv[jc];
+        if (lane > jc && lane < 9) {
+          const double a = s.L[lane][jc];
+          s.col[lane] = a;
+          s.L[lane][jc] = a * inv;
+        }
         __syncwarp();
         const int m = 8 - jc;  // trailing size
         for (int t = lane; t < m * (m + 1) / 2; t += 32) {
           const int ii = static_cast<int>((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f + 1e-4f);
           const int kk = t - ii * (ii + 1) / 2;
           const int i = jc + 1 + ii, k = jc + 1 + kk;
-          s.L[i][k] -= s.L[i][jc] * s.L[k][jc];
+          s.L[i][k] -= s.col[i] * s.L[k][jc];
         }
         __syncwarp();
       }
       if (lane == 0 && fail) record_element_error(err, e, 2);
       __syncwarp();
-      // Kua Kaa^-1 Kau = (L^-1 Kau)^T (L^-1 Kau) with Kaa = L L^T, so only the
-      // forward substitution is needed: X[:, c] = L^-1 Kau[:, c] for the 24
-      // columns (one lane each).
+      // Kua Kaa^-1 Kau = (L^-1 Kau)^T D^-1 (L^-1 Kau) with Kaa = L D L^T, so
+      // only the forward substitution is needed: X[:, c] = L^-1 Kau[:, c] for
+      // the 24 columns (one lane each, unit diagonal), and XD = D^-1 X.
+      double y[9];
       if (lane < 24) {
-        double y[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) y[i] = s.Kua[lane][i];
+#pragma unroll
+        for (int i = 1; i < 9; ++i)
+#pragma unroll
+          for (int k = 0; k < i; ++k) y[i] -= s.L[i][k] * y[k];
+      }
+      __syncwarp();  // every row of Kua read before X overwrites it
+      if (lane < 24) {
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
-          double v = s.Kua[lane][i];
-#pragma unroll
-          for (int k = 0; k < i; ++k) v -= s.L[i][k] * y[k];
-          y[i] = v * s.Linv[i];
+          s.X[i][lane] = y[i];
+          s.XD[i][lane] = y[i] * s.Dinv[i];
         }
-#pragma unroll
-        for (int i = 0; i < 9; ++i) s.X[i][lane] = y[i];
       }
       __syncwarp();
       // ── Phase D: Ke = Kuu - X^T X (lower triangle, mirrored) ──
@@ -405,7 +425,7 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
         double v = kval(s, lam, mu, r / 3, r % 3, c / 3, c % 3);
         double corr = 0.0;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) corr = fma(s.X[k][r], s.X[k][c], corr);
+        for (int k = 0; k < 9; ++k) corr = fma(s.XD[k][r], s.X[k][c], corr);
         v -= corr;
         ke_s[r * 24 + c] = v;
         ke_s[c * 24 + r] = v;
