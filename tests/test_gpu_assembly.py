@@ -32,11 +32,20 @@ def _models(known):
     mixed = C.small_block(6, 3, 3, 0.1, seed=2, jitter=0.1)
     mixed.form[::2] = C.SRI
     out["mixed_forms"] = mixed
+    # an element entered twice: its nodes carry up to 9 elements, beyond the
+    # compact (structured-mesh) fill, so the general block fill runs
+    dup = C.small_block(4, 3, 3, 0.1, seed=5, jitter=0.1)
+    k = dup.n_elem // 2
+    dup.conn = np.concatenate([dup.conn, dup.conn[k:k + 1]])
+    dup.elem_ids = np.concatenate([dup.elem_ids, [dup.elem_ids.max() + 1]]).astype(np.int32)
+    for f in ("E", "nu", "form"):
+        setattr(dup, f, np.concatenate([getattr(dup, f), getattr(dup, f)[k:k + 1]]))
+    out["duplicate_element"] = dup
     return out
 
 
 MODEL_NAMES = ["hex1_eas", "hex1_sri", "cantilever_1500", "jitter_hetero", "sri_block",
-               "incompressible", "mixed_forms"]
+               "incompressible", "mixed_forms", "duplicate_element"]
 
 
 @pytest.mark.parametrize("name", MODEL_NAMES)

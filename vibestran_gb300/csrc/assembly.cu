@@ -25,7 +25,6 @@ namespace vsgb {
 namespace {
 
 constexpr int kMaxValence = 32;                 // elements per node in the pattern kernel
-constexpr int kMaxCand = kMaxValence * 8;       // candidate neighbour slots
 constexpr int kMaxNbr = 128;                    // unique neighbour nodes per node
 constexpr int kPatWarps = 4;
 
@@ -182,13 +181,20 @@ __global__ void k_node_sort(int n_nodes, const int* __restrict__ ptr, int* __res
 
 // ── pattern + values ───────────────────────────────────────────────────────
 
-struct PatSmem {
-  int cand[kMaxCand];
-  int key[kMaxCand];
-  int first[kMaxCand];
-  int nbr[kMaxNbr];
-  int nkey[kMaxNbr];  // first free equation of nbr[r] (ascending)
+// Neighbour gathering scratch for nodes of up to kVal incident elements and
+// kNbr distinct neighbours.
+template <int kVal, int kNbr>
+struct PatSmemT {
+  static constexpr int kValence = kVal, kCand = 8 * kVal, kNeighbours = kNbr;
+  int cand[kCand];
+  int key[kCand];
+  int first[kCand];
+  int nbr[kNbr];
+  int nkey[kNbr];  // first free equation of nbr[r] (ascending)
 };
+using PatSmem = PatSmemT<kMaxValence, kMaxNbr>;
+// Structured hexahedral meshes: 8 elements, 27 neighbours per node.
+using PatSmemSmall = PatSmemT<8, 32>;
 
 __device__ __forceinline__ int first_free_eq(const int* eq3, int b) {
   int k = INT_MAX;
@@ -215,11 +221,12 @@ __device__ __forceinline__ int warp_incl_scan(int v) {
 // elements, those with a free DOF only, ordered by their first free equation
 // into s.nbr.  Returns their number, or -1 (error 3 recorded) when node a
 // exceeds the valence / neighbour limits.  Warp-collective.
+template <typename Pat>
 __device__ int gather_neighbors(int a, int pb, int L, const int* __restrict__ conn,
                                 const int* __restrict__ eq3, const int* __restrict__ node_elem,
-                                PatSmem& s, AssemblyError* err) {
+                                Pat& s, AssemblyError* err) {
   const int lane = threadIdx.x & 31;
-  if (L > kMaxValence) {
+  if (L > Pat::kValence) {
     if (lane == 0) set_error(err, 3, a);
     return -1;
   }
@@ -245,7 +252,7 @@ __device__ int gather_neighbors(int a, int pb, int L, const int* __restrict__ co
       const int k = s.key[c];
       int r = 0;
       for (int m = 0; m < C; ++m) r += (s.first[m] && s.key[m] < k);
-      if (r < kMaxNbr) {
+      if (r < Pat::kNeighbours) {
         s.nbr[r] = s.cand[c];
         s.nkey[r] = k;
       }
@@ -254,7 +261,7 @@ __device__ int gather_neighbors(int a, int pb, int L, const int* __restrict__ co
   for (int c = lane; c < C; c += 32) U += s.first[c];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) U += __shfl_xor_sync(0xffffffffu, U, o);
-  if (U > kMaxNbr) {
+  if (U > Pat::kNeighbours) {
     if (lane == 0) set_error(err, 3, a);
     return -1;
   }
@@ -428,7 +435,7 @@ __global__ void k_node_aligned(int n_nodes, const int* __restrict__ eq3, int* __
 __global__ void __launch_bounds__(kPatWarps * 32)
 k_block_count(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3,
               const int* __restrict__ node_ptr, const int* __restrict__ node_elem,
-              int* __restrict__ blen, AssemblyError* err) {
+              int* __restrict__ blen, int* __restrict__ max_valence, AssemblyError* err) {
   __shared__ PatSmem smem_all[kPatWarps];
   PatSmem& s = smem_all[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
@@ -438,20 +445,26 @@ k_block_count(int n_nodes, const int* __restrict__ conn, const int* __restrict__
     if (r0 < 0) continue;  // aligned: all three constrained
     const int pb = node_ptr[a], L = node_ptr[a + 1] - pb;
     const int U = gather_neighbors(a, pb, L, conn, eq3, node_elem, s, err);
-    if (U >= 0 && lane == 0) blen[r0 / 3] = U;
+    if (U >= 0 && lane == 0) {
+      blen[r0 / 3] = U;
+      atomicMax(max_valence, L);
+    }
     __syncwarp();
   }
 }
 
-constexpr int kFillWarps = 2;
-
-struct FillSmem {
-  PatSmem p;
-  double acc[kMaxNbr][9];            // block sums per neighbour slot
-  unsigned char nz[kMaxNbr][9];      // entry received a value != 0.0
-  short slot[kMaxCand];              // neighbour slot of candidate c (-1: constrained)
-  double rsum[9];                    // FP64 sum of the row's blocks (FP32 diagonal slot)
+template <typename Pat>
+struct FillSmemT {
+  Pat p;
+  double acc[Pat::kNeighbours][9];         // block sums per neighbour slot
+  unsigned char nz[Pat::kNeighbours][9];   // entry received a value != 0.0
+  short slot[Pat::kCand];                  // neighbour slot of candidate c (-1: constrained)
+  double rsum[9];                          // FP64 sum of the row's blocks (FP32 diagonal slot)
 };
+// Warps per CTA of the general fill (15 KB of shared memory per warp) and of
+// the structured-mesh fill (4 KB per warp).
+template <typename Pat>
+__host__ __device__ constexpr int fill_warps() { return Pat::kNeighbours > 32 ? 2 : 4; }
 
 // Block row of node a: for each incident element (ascending, the reference's
 // summation order), its three rows of K_e (576 contiguous bytes, one
@@ -459,15 +472,17 @@ struct FillSmem {
 // the row is written to the sliced-ELL operator (FP64, and FP32 in difference
 // form) with its padding, the inverse diagonal and the scalar nonzero counts
 // (full and lower triangle).
-__global__ void __launch_bounds__(kFillWarps * 32)
+template <typename Pat>
+__global__ void __launch_bounds__(fill_warps<Pat>() * 32)
 k_block_fill(int n_nodes, const int* __restrict__ conn, const int* __restrict__ eq3,
              const int* __restrict__ node_ptr, const int* __restrict__ node_elem,
              const double* __restrict__ kbuf, unsigned long long* __restrict__ counts,
              const int* __restrict__ slice_ptr, int* __restrict__ cols,
              double* __restrict__ v64, float* __restrict__ v32, double* __restrict__ dinv,
              AssemblyError* err) {
-  __shared__ FillSmem smem_all[kFillWarps];
-  FillSmem& s = smem_all[threadIdx.x >> 5];
+  constexpr int kFillWarps = fill_warps<Pat>();
+  __shared__ FillSmemT<Pat> smem_all[kFillWarps];
+  FillSmemT<Pat>& s = smem_all[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * kFillWarps;
   for (int a = blockIdx.x * kFillWarps + (threadIdx.x >> 5); a < n_nodes; a += warps_total) {
@@ -888,9 +903,12 @@ bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, i
   VSGB_CUDA(cudaMemsetAsync(B.rowlen.ptr, 0, sizeof(int) * nb, topo));
   scr.counts.reserve(2);
   VSGB_CUDA(cudaMemsetAsync(scr.counts.ptr, 0, sizeof(unsigned long long) * 2, topo));
+  scr.max_valence.reserve(1);
+  VSGB_CUDA(cudaMemsetAsync(scr.max_valence.ptr, 0, sizeof(int), topo));
   const int pgrid = grid_for(static_cast<long long>(n_nodes) * 32, kPatWarps * 32, num_sms * 16);
   k_block_count<<<pgrid, kPatWarps * 32, 0, topo>>>(n_nodes, conn, eq3, scr.node_ptr.ptr,
-                                                    scr.node_elem.ptr, B.rowlen.ptr, scr.err.ptr);
+                                                    scr.node_elem.ptr, B.rowlen.ptr,
+                                                    scr.max_valence.ptr, scr.err.ptr);
   VSGB_LAUNCH_CHECK();
   const long long total_steps = bsr_layout(B, nb, topo);  // synchronises topo
   // stored blocks (the sum of the row lengths)
@@ -900,9 +918,16 @@ bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, i
   int last = 0;  // first step of the last slice
   VSGB_CUDA(cudaMemcpyAsync(&last, B.slice_ptr.ptr + B.nslices - 1, sizeof(int),
                             cudaMemcpyDeviceToHost, topo));
+  int max_valence = 0;
+  VSGB_CUDA(cudaMemcpyAsync(&max_valence, scr.max_valence.ptr, sizeof(int),
+                            cudaMemcpyDeviceToHost, topo));
   VSGB_CUDA(cudaStreamSynchronize(topo));
   long long blocks = 0;
-  for (int R = 0; R < nb; ++R) blocks += B.h_blen[R];
+  int max_blen = 0;
+  for (int R = 0; R < nb; ++R) {
+    blocks += B.h_blen[R];
+    max_blen = B.h_blen[R] > max_blen ? B.h_blen[R] : max_blen;
+  }
   if (blocks == 0) {
     join();
     return false;
@@ -927,12 +952,23 @@ bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, i
   join();
   out.n = n_dof;
   out.dinv.reserve(static_cast<size_t>(n_dof));
-  const int fgrid = grid_for(static_cast<long long>(n_nodes) * 32, kFillWarps * 32, num_sms * 32);
-  k_block_fill<<<fgrid, kFillWarps * 32, 0, s>>>(
-      n_nodes, conn, eq3, scr.node_ptr.ptr, scr.node_elem.ptr, kbuf, scr.counts.ptr,
-      B.slice_ptr.ptr, B.cols.ptr, B.val64.ptr, need32 ? B.val32.ptr : nullptr, out.dinv.ptr,
-      scr.err.ptr);
-  VSGB_LAUNCH_CHECK();
+  // The compact fill serves meshes whose nodes have at most 8 elements and 32
+  // neighbours (every structured hexahedral mesh): 4 KB of shared memory per
+  // warp instead of 15 KB, so more warps hide the element-matrix loads.
+  auto fill = [&](auto pat) {
+    using Pat = decltype(pat);
+    constexpr int warps = fill_warps<Pat>();
+    const int fgrid = grid_for(static_cast<long long>(n_nodes) * 32, warps * 32, num_sms * 32);
+    k_block_fill<Pat><<<fgrid, warps * 32, 0, s>>>(
+        n_nodes, conn, eq3, scr.node_ptr.ptr, scr.node_elem.ptr, kbuf, scr.counts.ptr,
+        B.slice_ptr.ptr, B.cols.ptr, B.val64.ptr, need32 ? B.val32.ptr : nullptr, out.dinv.ptr,
+        scr.err.ptr);
+    VSGB_LAUNCH_CHECK();
+  };
+  if (max_valence <= PatSmemSmall::kValence && max_blen <= PatSmemSmall::kNeighbours)
+    fill(PatSmemSmall{});
+  else
+    fill(PatSmem{});
   unsigned long long cnt[2] = {0, 0};
   VSGB_CUDA(cudaMemcpyAsync(cnt, scr.counts.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
   VSGB_CUDA(cudaStreamSynchronize(s));

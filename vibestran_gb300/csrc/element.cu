@@ -232,7 +232,7 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
     const double c02 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
     const double detJ = J[0][0] * c00 + J[1][0] * c01 + J[2][0] * c02;
     const int bad = act && !(detJ > 0.0);
-    const double id = 1.0 / detJ;
+    const double id = rcp_nr(detJ);
     // row rr of J^-1: (J[c+1][rr+1] J[c+2][rr+2] - J[c+1][rr+2] J[c+2][rr+1]) / det
     const int q1 = rr == 2 ? 0 : rr + 1, q2 = rr == 0 ? 2 : rr - 1;
     double Jir[3];
@@ -275,35 +275,44 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
     if (!sri && lane < 9) s.c0[lane] = s.j0[9] * s.j0[lane];
 
     // ── Phase B: moment matrices M_AB = sum_gp w g_A (x) g_B ──
-    // Work items with the same eight-FMA body: the 36 node pairs (x 9), and
-    // for EAS the enhancement sums V (72) and C (6).
-    const int n_items = sri ? 324 : 402;
+    // Work items with the same eight-FMA body: the 8 symmetric M_AA (x 6),
+    // the 28 node pairs A < B (x 9), and for EAS the enhancement sums V (72)
+    // and C (6).
+    const int n_items = sri ? 300 : 378;
     for (int t = lane; t < n_items; t += 32) {
       const double* pa;
       const double* pb;
       int sa, sb;
       double* dst;
-      if (t < 324) {
-        const int pr = t / 9, ij = t - 9 * pr, i = ij / 3, j = ij - 3 * i;
-        int rem = pr, A = 0;  // pairs of the 8x8 upper triangle in row order
-        while (rem >= 8 - A) {
-          rem -= 8 - A;
+      double* dst2 = nullptr;  // mirrored entry of a symmetric M_AA
+      if (t < 48) {
+        const int A = t / 6, u = t - 6 * A, i = pp_first(u), j = pp_second(u);
+        pa = &s.wg[0][A][i];
+        pb = &s.g[0][A][j];
+        sa = sb = 24;
+        dst = &s.M[pair_index(A, A)][3 * i + j];
+        if (i != j) dst2 = &s.M[pair_index(A, A)][3 * j + i];
+      } else if (t < 300) {
+        const int pr = (t - 48) / 9, ij = (t - 48) - 9 * pr, i = ij / 3, j = ij - 3 * i;
+        int rem = pr, A = 0;  // pairs of the strict 8x8 upper triangle in row order
+        while (rem >= 7 - A) {
+          rem -= 7 - A;
           ++A;
         }
-        const int B = A + rem;
+        const int B = A + 1 + rem;
         pa = &s.wg[0][A][i];
         pb = &s.g[0][B][j];
         sa = sb = 24;
         dst = &s.M[pair_index(A, B)][ij];
-      } else if (t < 396) {
-        const int u = t - 324, A = u / 9, rem = u - 9 * A, p = rem / 3, i = rem - 3 * p;
+      } else if (t < 372) {
+        const int u = t - 300, A = u / 9, rem = u - 9 * A, p = rem / 3, i = rem - 3 * p;
         pa = &s.g[0][A][i];
         sa = 24;
         pb = &s_par[p][0];
         sb = 1;
         dst = &s.V[A][p][i];
       } else {
-        const int u = t - 396;
+        const int u = t - 372;
         pa = &s_pp[u][0];
         pb = &s.idet[0];
         sa = sb = 1;
@@ -313,6 +322,7 @@ k_chexa8_stiffness(int n_elem, const double* __restrict__ xyz, const int* __rest
 #pragma unroll
       for (int q = 0; q < 8; ++q) acc = fma(pa[q * sa], pb[q * sb], acc);
       *dst = acc;
+      if (dst2) *dst2 = acc;
     }
     __syncwarp();
     if (!sri) {

@@ -51,6 +51,7 @@ struct AssemblyScratch {
   DevBuf<int> node_cnt, node_ptr, node_elem, dof_node, row_cnt, lower_rp, scan_tmp, flag;
   DevBuf<long long> total;
   DevBuf<unsigned long long> counts;  // block assembly: scalar nnz full / lower, blocks
+  DevBuf<int> max_valence;            // block assembly: most elements at one node
   DevBuf<AssemblyError> err;
 };
 
