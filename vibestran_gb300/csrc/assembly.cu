@@ -217,10 +217,44 @@ __device__ __forceinline__ int warp_incl_scan(int v) {
   return v;
 }
 
+// Ascending warp-wide bitonic sort of 64 keys, element i held by lane i & 31
+// in v[i >> 5]: the compare-exchange network over i (partner i ^ j, direction
+// from bit k of i); j = 32 pairs the two registers of a lane, smaller j pair
+// lanes through shuffles.
+__device__ __forceinline__ void warp_sort64(unsigned long long (&v)[2]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j == 32) {
+        // i = lane (register 0) against i ^ 32 = lane + 32; k = 64: ascending
+        const unsigned long long lo = v[0] < v[1] ? v[0] : v[1];
+        const unsigned long long hi = v[0] < v[1] ? v[1] : v[0];
+        v[0] = lo;
+        v[1] = hi;
+      } else {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const int i = lane + 32 * r;
+          const unsigned long long o = __shfl_xor_sync(0xffffffffu, v[r], j);
+          const bool up = (i & k) == 0;          // this block sorts ascending
+          const bool low = (i & j) == 0;         // this element is the pair's lower index
+          const bool take_min = up == low;
+          v[r] = take_min ? (o < v[r] ? o : v[r]) : (o < v[r] ? v[r] : o);
+        }
+      }
+    }
+  }
+}
+
 // Distinct neighbour nodes of node a (itself included) over its incident
 // elements, those with a free DOF only, ordered by their first free equation
 // into s.nbr.  Returns their number, or -1 (error 3 recorded) when node a
-// exceeds the valence / neighbour limits.  Warp-collective.
+// exceeds the valence / neighbour limits.  Warp-collective.  Nodes of up to 8
+// elements (64 candidates) sort (first free equation, node) pairs in
+// registers and keep the first of each run; larger ones compare every
+// candidate with the earlier ones in shared memory.
 template <typename Pat>
 __device__ int gather_neighbors(int a, int pb, int L, const int* __restrict__ conn,
                                 const int* __restrict__ eq3, const int* __restrict__ node_elem,
@@ -231,6 +265,51 @@ __device__ int gather_neighbors(int a, int pb, int L, const int* __restrict__ co
     return -1;
   }
   const int C = 8 * L;
+  if (C <= 64) {
+    unsigned long long v[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int c = lane + 32 * r;
+      v[r] = ~0ull;
+      if (c < C) {
+        const int slot = node_elem[pb + (c >> 3)];
+        const int b = conn[(slot & ~7) + (c & 7)];
+        const int k = first_free_eq(eq3, b);
+        s.cand[c] = b;
+        s.key[c] = k;
+        // constrained nodes (k = INT_MAX) sort after every free one
+        v[r] = (static_cast<unsigned long long>(static_cast<unsigned>(k)) << 32) |
+               static_cast<unsigned>(b);
+      }
+    }
+    warp_sort64(v);
+    // first of each run of equal (key, node) among the free nodes
+    const unsigned long long prev0 = __shfl_up_sync(0xffffffffu, v[0], 1);
+    const unsigned long long last0 = __shfl_sync(0xffffffffu, v[0], 31);
+    const unsigned long long prev1 = __shfl_up_sync(0xffffffffu, v[1], 1);
+    bool f[2];
+    f[0] = (lane == 0 || prev0 != v[0]) && (v[0] >> 32) < static_cast<unsigned>(INT_MAX);
+    f[1] = (lane == 0 ? last0 != v[1] : prev1 != v[1]) &&
+           (v[1] >> 32) < static_cast<unsigned>(INT_MAX);
+    const unsigned m0 = __ballot_sync(0xffffffffu, f[0]);
+    const unsigned m1 = __ballot_sync(0xffffffffu, f[1]);
+    const unsigned below = (1u << lane) - 1u;
+    const int U = __popc(m0) + __popc(m1);
+    if (U > Pat::kNeighbours) {
+      if (lane == 0) set_error(err, 3, a);
+      return -1;
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      if (f[r]) {
+        const int rank = (r ? __popc(m0) : 0) + __popc((r ? m1 : m0) & below);
+        s.nbr[rank] = static_cast<int>(static_cast<unsigned>(v[r]));
+        s.nkey[rank] = static_cast<int>(v[r] >> 32);
+      }
+    }
+    __syncwarp();
+    return U;
+  }
   for (int c = lane; c < C; c += 32) {
     const int slot = node_elem[pb + (c >> 3)];
     const int b = conn[(slot & ~7) + (c & 7)];
@@ -883,18 +962,17 @@ bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, i
     VSGB_CUDA(cudaEventRecord(joined, topo));
     VSGB_CUDA(cudaStreamWaitEvent(s, joined, 0));
   };
+  // The topology passes are enqueued back to back and read back after one
+  // synchronisation (they run in the element kernel's tail, where every
+  // host round trip shows): whether the equations are node-aligned, the
+  // layout's total steps, the block-row lengths and the largest valence.
+  // On misaligned equations the passes below are harmless (every index they
+  // form stays below n_dof) and their results are discarded.
   scr.flag.reserve(1);
   VSGB_CUDA(cudaMemsetAsync(scr.flag.ptr, 0, sizeof(int), topo));
   k_node_aligned<<<grid_for(n_nodes, kThreads, 1 << 30), kThreads, 0, topo>>>(n_nodes, eq3,
                                                                             scr.flag.ptr);
   VSGB_LAUNCH_CHECK();
-  int misaligned = 0;
-  VSGB_CUDA(cudaMemcpyAsync(&misaligned, scr.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, topo));
-  VSGB_CUDA(cudaStreamSynchronize(topo));
-  if (misaligned) {
-    join();
-    return false;
-  }
 
   build_incidence(n_nodes, n_elem, conn, eq3, n_dof, scr, topo);
   const int nb = n_dof / 3;
@@ -910,18 +988,28 @@ bool assemble_blocks(int n_nodes, int n_elem, const int* conn, const int* eq3, i
                                                     scr.node_elem.ptr, B.rowlen.ptr,
                                                     scr.max_valence.ptr, scr.err.ptr);
   VSGB_LAUNCH_CHECK();
-  const long long total_steps = bsr_layout(B, nb, topo);  // synchronises topo
+  bsr_layout(B, nb, topo);
   // stored blocks (the sum of the row lengths)
   B.h_blen.resize(static_cast<size_t>(nb));
   VSGB_CUDA(cudaMemcpyAsync(B.h_blen.data(), B.rowlen.ptr, sizeof(int) * nb,
                             cudaMemcpyDeviceToHost, topo));
+  long long total_steps = 0;
+  VSGB_CUDA(cudaMemcpyAsync(&total_steps, B.total.ptr, sizeof(long long), cudaMemcpyDeviceToHost,
+                            topo));
   int last = 0;  // first step of the last slice
   VSGB_CUDA(cudaMemcpyAsync(&last, B.slice_ptr.ptr + B.nslices - 1, sizeof(int),
                             cudaMemcpyDeviceToHost, topo));
   int max_valence = 0;
   VSGB_CUDA(cudaMemcpyAsync(&max_valence, scr.max_valence.ptr, sizeof(int),
                             cudaMemcpyDeviceToHost, topo));
+  int misaligned = 0;
+  VSGB_CUDA(cudaMemcpyAsync(&misaligned, scr.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, topo));
   VSGB_CUDA(cudaStreamSynchronize(topo));
+  if (misaligned) {
+    join();
+    return false;
+  }
+  B.steps = total_steps;
   long long blocks = 0;
   int max_blen = 0;
   for (int R = 0; R < nb; ++R) {

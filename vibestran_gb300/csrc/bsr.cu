@@ -174,7 +174,7 @@ void bsr_make_f32(BsrSell& B, int num_sms, cudaStream_t s) {
   B.has32 = true;
 }
 
-long long bsr_layout(BsrSell& B, int nb, cudaStream_t s) {
+void bsr_layout(BsrSell& B, int nb, cudaStream_t s) {
   const int nslices = (nb + 7) / 8;
   B.nb = nb;
   B.nslices = nslices;
@@ -186,11 +186,6 @@ long long bsr_layout(BsrSell& B, int nb, cudaStream_t s) {
       nb, nslices, B.rowlen.ptr, B.slice_steps.ptr);
   VSGB_LAUNCH_CHECK();
   exclusive_scan_checked(B.slice_steps.ptr, B.slice_ptr.ptr, nslices, B.tmp.ptr, B.total.ptr, s);
-  long long total_steps = 0;
-  VSGB_CUDA(cudaMemcpyAsync(&total_steps, B.total.ptr, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  VSGB_CUDA(cudaStreamSynchronize(s));
-  B.steps = total_steps;
-  return total_steps;
 }
 
 bool build_bsr(const AssembledCsr& K, BsrSell& B, bool need64, bool need32, int num_sms,

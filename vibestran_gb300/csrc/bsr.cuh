@@ -39,8 +39,9 @@ bool build_bsr(const AssembledCsr& K, BsrSell& B, bool need64, bool need32, int 
                cudaStream_t s);
 
 // Slice steps from the block-row lengths in B.rowlen (nb rows), scanned into
-// B.slice_ptr; sets nb, nslices and steps and returns the total steps.
-long long bsr_layout(BsrSell& B, int nb, cudaStream_t s);
+// B.slice_ptr, the total into B.total (device); sets nb and nslices.  Only
+// enqueues work on s: the caller reads the total back.
+void bsr_layout(BsrSell& B, int nb, cudaStream_t s);
 
 // Block operator straight from the element stiffness buffer when the
 // equations are node-aligned triples (no scalar CSR is built); returns false,
