@@ -69,9 +69,12 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 // first blocks) and ending it a reduction, so CTAs at the mesh ends, whose
 // rows have fewer blocks and whose slices are therefore more numerous, ran
 // slower with a weight of 1.  Measured per iteration on GB300 (FP32 / FP64,
-// 265k and 504k equations): weight 1: 25.5 / 75.5 and 50.3 / 156 us;
-// 3: 24.1 / 72.5 and 46.8 / 146 us; 5: 23.8 / 72.9 and 46.4 / 144 us.
-constexpr int kSliceWeight = 4;
+// 265k and 504k equations), cyclic slice order: weight 1: 25.5 / 75.5 and
+// 50.3 / 156 us; 3: 24.1 / 72.5 and 46.8 / 146 us; 5: 23.8 / 72.9 and 46.4 /
+// 144 us.  Snake order (kSnake): 4: 17.31 / 66.75 and 33.64 / 144.1 us; 8:
+// 17.09 / 65.94 and 33.64 / 143.8 us; 12: 17.09 / 65.75 and 33.57 / 144.0 us;
+// 16: 17.06 / 66.15 us (265k).
+constexpr int kSliceWeight = 12;
 
 // Window kernels keep p over the window in shared memory between iterations.
 constexpr bool kKeepWindowP = true;
