@@ -84,6 +84,14 @@ class Gb300PcgSolverBackend : public SolverBackend {
   [[nodiscard]] const vsgb_stats& last_stats() const noexcept { return stats_; }
   [[nodiscard]] vsgb_ctx* context() const noexcept { return ctx_; }
 
+  /// vsgb_set_option (VSGB_OPT_*); the display name follows the
+  /// preconditioner (VSGB_OPT_PRECOND).
+  void set_option(int option, double value) {
+    if (vsgb_set_option(ctx_, option, value) != VSGB_OK) throw SolverError(last_error());
+    char buf[256];
+    if (vsgb_backend_name(ctx_, buf, sizeof buf) == VSGB_OK) name_ = buf;
+  }
+
  protected:
   static std::optional<Gb300PcgSolverBackend> create(double tol, int max_iters, int device,
                                                      int precision) noexcept {

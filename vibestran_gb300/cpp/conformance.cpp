@@ -199,6 +199,19 @@ void run_mixed(Gb300MixedPcgSolverBackend& be) {
   auto ud = direct(K, F);
   for (int i = 0; i < 200; i += 20) CHECK(std::abs(u[i] - ud[i]) < 5e-3);
   CHECK(be.last_estimated_error() < 1e-4);
+  // options through the backend: the name follows the preconditioner, and a
+  // bad value is reported as a SolverError
+  be.set_option(VSGB_OPT_PRECOND, VSGB_PRECOND_BLOCK_JACOBI);
+  CHECK(be.name().find("3x3 block Jacobi") != std::string_view::npos);
+  be.set_option(VSGB_OPT_PRECOND, VSGB_PRECOND_JACOBI);
+  CHECK(be.name().find("block") == std::string_view::npos);
+  bool threw = false;
+  try {
+    be.set_option(VSGB_OPT_PRECOND, 7);
+  } catch (const SolverError& e) {
+    threw = std::string(e.what()).find("preconditioner must be") != std::string::npos;
+  }
+  CHECK(threw);
 }
 
 }  // namespace
