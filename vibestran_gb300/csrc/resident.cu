@@ -49,6 +49,7 @@ struct ResArgs {
   T* p4b;
   double* partials;
   unsigned* count;
+  unsigned long long* fx;  // FP32: fused reduction words (kFxSlots x 2), null: counter barrier
   int* abort_flag;
   PcgScalars* S;
   const PcgScalars* O;
@@ -195,6 +196,162 @@ __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned*
   return ok;
 }
 
+// ── Fused fixed-point reductions (FP32 solve) ──
+// One 64-bit word per summed value carries the arrivals (bits 0-7), overflow
+// reports (bits 8-15) and the sum of the CTA partials as 48-bit signed fixed
+// point (bits 16-63) at a scale 2^s chosen from the previous total of the same
+// quantity (|previous| 2^s ~ 2^36).  A CTA arrives with one release add of
+// (q << 16) + 1, q = rint(partial 2^s), so a waiter that sees every arrival
+// holds the total in the same load: one L2 round trip fewer than reading the
+// partials after a counter barrier.  Integer addition is exact and
+// associative, so the total is the same bits in every CTA and every run.  The
+// FP64 partials are stored as before; the reduction falls back to them when
+// there is no previous total, when a partial would leave the 48-bit range
+// (|q| >= 2^39, reported in bits 8-15) or when the total came out below 2^30
+// (a drop of more than 64x, where the fixed point has too few digits).
+constexpr bool kFusedReductions = true;
+constexpr int kFxSlots = 4;          // reductions in flight before a word is reused
+constexpr int kFxWords = 2;          // words per slot (the most values one reduction sums)
+constexpr int kFxScaleBits = 36;
+constexpr double kFxPartMax = 549755813888.0;   // 2^39
+constexpr long long kFxTotalMin = 1LL << 30;
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() {
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+// 2^e for e in [-1022, 1023], from the exponent bits
+__device__ __forceinline__ double pow2i(int e) {
+  return __longlong_as_double(static_cast<long long>(e + 1023) << 52);
+}
+// Scale exponent for a total near `prev` (0: none usable)
+__device__ __forceinline__ int fx_scale(double prev, bool& usable) {
+  const long long bits = __double_as_longlong(prev);
+  const int ex = static_cast<int>((bits >> 52) & 0x7FF);
+  usable = prev > 0.0 && ex > 64 && ex < 2046 - 64;
+  return usable ? kFxScaleBits - (ex - 1023) : 0;
+}
+
+// grid_allreduce for the FP32 solve over the fused words of reduction `red`
+// (ring slot red % kFxSlots of kFxWords words, NV of them used): prev[k] > 0 is the previous total
+// of value k (<= 0: none, fall back).  CTA 0 clears the slot two reductions
+// ahead (its last readers all arrived at the reduction before this one).
+template <int NV, typename Fin>
+__device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], double* partials,
+                                  int slot, unsigned long long* fx, int red, int* abort_flag,
+                                  double* sm, int* s_ok, int* s_fb, double* s_tot, Fin&& fin) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sm[wid * NV + k] = static_cast<double>(v[k]);
+  __syncthreads();
+  double* part = partials + static_cast<size_t>(slot) * gridDim.x * NV;
+  static_assert(NV <= kFxWords, "a fused reduction sums at most kFxWords values");
+  unsigned long long* words = fx + static_cast<size_t>(red % kFxSlots) * kFxWords;
+  if (wid == 0) {
+    double w[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) w[k] = lane < kResWarps ? sm[lane * NV + k] : 0.0;
+#pragma unroll
+    for (int o = kResWarps / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = w[k];
+      if (blockIdx.x == 0) {
+        unsigned long long* ahead = fx + static_cast<size_t>((red + 2) % kFxSlots) * kFxWords;
+#pragma unroll
+        for (int k = 0; k < kFxWords; ++k) ahead[k] = 0ull;
+      }
+      int sc[NV];
+      bool fx_ok = true;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        bool u;
+        sc[k] = fx_scale(prev[k], u);
+        fx_ok = fx_ok && u;
+      }
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        unsigned long long add = 1ull;
+        if (fx_ok) {
+          const double y = w[k] * pow2i(sc[k]);
+          if (fabs(y) < kFxPartMax)
+            add += static_cast<unsigned long long>(__double2ll_rn(y)) << 16;
+          else
+            add += 1ull << 8;
+        }
+        red_release_add_u64(words + k, add);
+      }
+      // wait for every arrival on every word
+      int ok = 1;
+      long long spins = 0;
+      unsigned long long got[NV];
+      for (;;) {
+        bool all = true;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          got[k] = ld_relaxed_u64(words + k);
+          all = all && (got[k] & 0xFFull) >= gridDim.x;
+        }
+        if (all) break;
+        ++spins;
+        if ((spins & 63) == 0 && *reinterpret_cast<volatile int*>(abort_flag)) {
+          ok = 0;
+          break;
+        }
+        if (spins > kSpinLimit) {
+          atomicExch(abort_flag, 1);
+          ok = 0;
+          break;
+        }
+        if (spins > 4096) __nanosleep(64);
+      }
+      fence_acq_rel_gpu();
+      int fb = fx_ok ? 0 : 1;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        const long long q = static_cast<long long>(got[k]) >> 16;
+        if (((got[k] >> 8) & 0xFFull) != 0ull || (q < kFxTotalMin && q > -kFxTotalMin)) fb = 1;
+        s_tot[k] = static_cast<double>(q) * pow2i(-sc[k]);
+      }
+      *s_ok = ok;
+      *s_fb = fb;
+    }
+  }
+  __syncthreads();
+  const bool ok = *s_ok != 0;
+  if (threadIdx.x < 32) {
+    double acc[NV];
+    if (*s_fb) {
+      // fixed-order sum of the FP64 partials, as grid_allreduce
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+      for (unsigned c = threadIdx.x; c < gridDim.x; c += 32)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += __ldcg(&part[c * NV + k]);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] = warp_sum(acc[k]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] = s_tot[k];
+    }
+    if (threadIdx.x == 0) fin(acc, ok);
+  }
+  __syncthreads();
+  return ok;
+}
+
 // Per-slice sum slots between the own-row vectors and the window: one per
 // slice of the largest CTA range (rows_max = 24 * max_slices), padded so the
 // window stays 16/32-byte aligned.
@@ -260,6 +417,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[96];
   __shared__ int s_ok;
+  __shared__ int s_fb;         // fused reduction fell back to the partials
+  __shared__ double s_tot[2];  // totals of a fused reduction
   __shared__ int s_next;  // next slice handed to a warp in phase 1
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int c = blockIdx.x;
@@ -342,6 +501,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     rel = 1.0;
   }
   int flags = 0, it = 0;
+  int fx_red = 0;  // fused reductions done (FP32)
   T* p_old = a.p4a;
   T* p_new = a.p4b;
   ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok,
@@ -505,22 +665,33 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       s = warp_sum(s);
       if (lane == 0) accp[0] = s;
     }
-    ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok,
-                              [&](const double (&t)[1], bool good) {
-                                pAp = t[0];
-                                if (!good) {
-                                  flags |= kFlagDone | kFlagAbort;
-                                } else if (!(pAp > 0.0)) {
-                                  flags |= kFlagDone | kFlagBreakdown;
-                                } else {
-                                  alpha = kFastScalars32 && sizeof(T) == 4
-                                              ? static_cast<double>(static_cast<float>(rz) /
-                                                                    static_cast<float>(pAp))
-                                              : rz / pAp;
-                                }
-                                s_flags = flags;
-                                s_sc[0] = alpha;
-                              });
+    auto fin1 = [&](const double (&t)[1], bool good) {
+      pAp = t[0];
+      if (!good) {
+        flags |= kFlagDone | kFlagAbort;
+      } else if (!(pAp > 0.0)) {
+        flags |= kFlagDone | kFlagBreakdown;
+      } else {
+        alpha = kFastScalars32 && sizeof(T) == 4
+                    ? static_cast<double>(static_cast<float>(rz) / static_cast<float>(pAp))
+                    : rz / pAp;
+      }
+      s_flags = flags;
+      s_sc[0] = alpha;
+    };
+    if constexpr (sizeof(T) == 4) {
+      if (a.fx) {
+        const double prev[1] = {pAp};
+        ok = grid_allreduce_fx<1>(accp, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
+                                  red, &s_ok, &s_fb, s_tot, fin1);
+      } else {
+        ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
+                                  &s_ok, fin1);
+      }
+    } else {
+      ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
+                                &s_ok, fin1);
+    }
     slot ^= 1;
     flags = s_flags;
     if (flags & kFlagDone) break;
@@ -559,35 +730,46 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       acc2[1] = rfma(rv, rv, acc2[1]);
     }
     ++it;
-    ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok,
-                              [&](const double (&t)[2], bool good) {
-                                if (!good) {
-                                  flags |= kFlagDone | kFlagAbort;
-                                } else {
-                                  rr = t[1];
-                                  bool conv;
-                                  if (kFastScalars32 && sizeof(T) == 4) {
-                                    // rel < tol as rr < (tol |b|)^2; rel itself at the exit
-                                    conv = fabs(rr) < rr_stop;
-                                  } else {
-                                    rel = sqrt(fabs(rr)) / norm_b;
-                                    conv = rel < a.tol;
-                                  }
-                                  if (conv) {
-                                    flags |= kFlagDone | kFlagConverged;
-                                    beta = 0.0;
-                                  } else {
-                                    beta = kFastScalars32 && sizeof(T) == 4
-                                               ? static_cast<double>(static_cast<float>(t[0]) /
-                                                                     static_cast<float>(rz))
-                                               : t[0] / rz;
-                                    if (it >= a.max_iters) flags |= kFlagDone | kFlagMaxIters;
-                                  }
-                                  rz = t[0];
-                                }
-                                s_flags = flags;
-                                s_sc[1] = beta;
-                              });
+    auto fin2 = [&](const double (&t)[2], bool good) {
+      if (!good) {
+        flags |= kFlagDone | kFlagAbort;
+      } else {
+        rr = t[1];
+        bool conv;
+        if (kFastScalars32 && sizeof(T) == 4) {
+          // rel < tol as rr < (tol |b|)^2; rel itself at the exit
+          conv = fabs(rr) < rr_stop;
+        } else {
+          rel = sqrt(fabs(rr)) / norm_b;
+          conv = rel < a.tol;
+        }
+        if (conv) {
+          flags |= kFlagDone | kFlagConverged;
+          beta = 0.0;
+        } else {
+          beta = kFastScalars32 && sizeof(T) == 4
+                     ? static_cast<double>(static_cast<float>(t[0]) / static_cast<float>(rz))
+                     : t[0] / rz;
+          if (it >= a.max_iters) flags |= kFlagDone | kFlagMaxIters;
+        }
+        rz = t[0];
+      }
+      s_flags = flags;
+      s_sc[1] = beta;
+    };
+    if constexpr (sizeof(T) == 4) {
+      if (a.fx) {
+        const double prev[2] = {rz, rr};
+        ok = grid_allreduce_fx<2>(acc2, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
+                                  red, &s_ok, &s_fb, s_tot, fin2);
+      } else {
+        ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
+                                  &s_ok, fin2);
+      }
+    } else {
+      ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
+                                &s_ok, fin2);
+    }
     slot ^= 1;
     flags = s_flags;
     if (flags & kFlagAbort) break;
@@ -721,6 +903,10 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   a.p4b = p4b;
   a.partials = P.partials.ptr;
   a.count = P.barrier.ptr;
+  // fused reductions: FP32 solve, arrivals counted in 8 bits
+  a.fx = (sizeof(T) == 4 && kFusedReductions && P.ctas <= 255) ? P.fx.ptr : nullptr;
+  if (a.fx)
+    VSGB_CUDA(cudaMemsetAsync(P.fx.ptr, 0, sizeof(unsigned long long) * kFxSlots * kFxWords, s));
   a.abort_flag = P.abort_flag.ptr;
   a.S = S;
   a.O = O;
@@ -828,6 +1014,7 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
   VSGB_CUDA(cudaMemcpyAsync(P.cta_win.ptr, win.data(), sizeof(int) * 2 * G,
                             cudaMemcpyHostToDevice, s));
   P.partials.reserve(2 * static_cast<size_t>(G) * 2);
+  P.fx.reserve(kFxSlots * kFxWords);
   P.barrier.reserve(1);
   P.abort_flag.reserve(1);
   const size_t rows = 24 * static_cast<size_t>(max_slices);

@@ -22,6 +22,7 @@ struct ResidentPlan {
   DevBuf<int> slice_mm;             // 2 * nslices: column range per slice (planning scratch)
   DevBuf<double> partials;          // 2 barrier slots x ctas x up to 4 values
   DevBuf<unsigned> barrier;         // monotonic arrival counter
+  DevBuf<unsigned long long> fx;    // FP32 solve: fused reduction words
   DevBuf<int> abort_flag;           // set by a barrier that gave up waiting
   DevBuf<float> u32g;                       // FP32 solution accumulator when ug32
   DevBuf<float> z4f, p4fa, p4fb;    // node-padded FP32 vectors (4 per node)
