@@ -606,7 +606,7 @@ void PcgEngine::prepare(const AssembledCsr& op, bool need32, cudaStream_t s, boo
   if (use_bsr_ && resident_) {
     int dev = 0;
     VSGB_CUDA(cudaGetDevice(&dev));
-    resident_prepare(bsr_, op.dinv.ptr, need32, dev, num_sms_, res_, s);
+    resident_prepare(bsr_, need32, dev, num_sms_, res_, s);
     launches_ += 2;
   }
   int pmax = (vec_grid_ > spmv_grid_ ? vec_grid_ : spmv_grid_);
@@ -849,7 +849,7 @@ bool PcgEngine::block_jacobi(bool mixed, cudaStream_t s) {
     throw Error(VSGB_ERR_INVALID,
                 "3x3 block Jacobi needs the persistent solve on the 3x3 block operator");
   if (bj_gen_ != generation_) {
-    const int bad = resident_block_jacobi(bsr_, res_, has32_, num_sms_, s);
+    const int bad = resident_block_jacobi(bsr_, res_, has32_, s);
     ++launches_;
     if (bad >= 0)
       throw Error(VSGB_ERR_SINGULAR, "GB300 PCG: the diagonal block of equations " +

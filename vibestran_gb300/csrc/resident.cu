@@ -946,9 +946,8 @@ bool configure(size_t smem, int* blocks) {
 
 }  // namespace
 
-void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int device, int num_sms,
-                      ResidentPlan& P, cudaStream_t s) {
-  (void)dinv;
+void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, ResidentPlan& P,
+                      cudaStream_t s) {
   P.ok32 = P.ok64 = false;
   if (!B.valid || B.nslices < num_sms) return;
   int coop = 0;
@@ -1066,9 +1065,7 @@ void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int dev
   VSGB_CUDA(cudaStreamSynchronize(s));
 }
 
-int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, int num_sms,
-                          cudaStream_t s) {
-  (void)num_sms;
+int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, cudaStream_t s) {
   const size_t m = 6 * static_cast<size_t>(B.nb > 0 ? B.nb : 1);
   P.bj64.reserve(m);
   if (need32) P.bj32.reserve(m);

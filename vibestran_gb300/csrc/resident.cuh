@@ -36,14 +36,13 @@ struct ResidentPlan {
 
 // Plans CTA ranges / windows and allocates the padded vectors; leaves both
 // ok flags false when the device or the operator does not allow it.
-void resident_prepare(const BsrSell& B, const double* dinv, bool need32, int device,
-                      int num_sms, ResidentPlan& P, cudaStream_t s);
+void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, ResidentPlan& P,
+                      cudaStream_t s);
 
 // Inverts the 3x3 diagonal block of every node of the FP64 operator into
 // P.bj64 (and P.bj32 when need32).  Returns -1, or the smallest node whose
 // block is not symmetric positive definite (nothing is usable then).
-int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, int num_sms,
-                          cudaStream_t s);
+int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, cudaStream_t s);
 
 // One FP32 inner solve: rhs = (float)(r64 * O->scale); on convergence
 // u64 += delta / O->scale.  Final counts/flags land in *S.  block_jacobi
