@@ -539,6 +539,7 @@ struct FillSmemT {
   unsigned char nz[Pat::kNeighbours][9];   // entry received a value != 0.0
   short slot[Pat::kCand];                  // neighbour slot of candidate c (-1: constrained)
   double rsum[9];                          // FP64 sum of the row's blocks (FP32 diagonal slot)
+  int diag;                                // neighbour slot of the node itself
 };
 // Warps per CTA of the general fill (15 KB of shared memory per warp) and of
 // the structured-mesh fill (4 KB per warp).
@@ -644,8 +645,11 @@ k_block_fill(int n_nodes, const int* __restrict__ conn, const int* __restrict__ 
     const int sl = R >> 3, ln0 = (R & 7) * 4;
     const long long sp = slice_ptr[sl];
     unsigned long long full = 0, lower = 0;
+    if (lane == 0) s.diag = -1;
+    __syncwarp();
     for (int u = lane; u < U; u += 32) {
       const int b = s.p.nbr[u], Cb = s.p.nkey[u] / 3;
+      if (b == a) s.diag = u;
       const long long st = sp + (u >> 2);
       const int ln = ln0 + (u & 3);
       cols[st * 32 + ln] = Cb;
@@ -661,17 +665,22 @@ k_block_fill(int n_nodes, const int* __restrict__ conn, const int* __restrict__ 
           full += z;
           lower += z && (3 * Cb + q <= 3 * R + d);
         }
-      if (b == a) {
-#pragma unroll
+    }
+    // Inverse diagonal: one equation per lane (an FP64 division is a long
+    // instruction sequence on the FP64 pipe, whatever its active lanes);
+    // missing or zero pivots are reported in equation order by lane 0.
+    __syncwarp();
+    {
+      const int ud = s.diag;
+      if (lane < 3 && ud >= 0 && s.nz[ud][4 * lane] && s.acc[ud][4 * lane] != 0.0)
+        dinv[3 * R + lane] = 1.0 / s.acc[ud][4 * lane];
+      if (lane == 0)
         for (int d = 0; d < 3; ++d) {
-          if (!s.nz[u][4 * d])
+          if (ud < 0 || !s.nz[ud][4 * d])
             set_error(err, 5, 3 * R + d);
-          else if (s.acc[u][4 * d] == 0.0)
+          else if (s.acc[ud][4 * d] == 0.0)
             set_error(err, 4, 3 * R + d);
-          else
-            dinv[3 * R + d] = 1.0 / s.acc[u][4 * d];
         }
-      }
     }
     // padding slots: a valid block column (the slice's first row), zeros
     const int slots = 4 * (slice_ptr[sl + 1] - slice_ptr[sl]);
