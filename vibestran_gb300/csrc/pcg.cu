@@ -830,6 +830,10 @@ void PcgEngine::resident_begin(cudaStream_t s, const void* hot, size_t hot_bytes
 void PcgEngine::resident_end(cudaStream_t s) {
   VSGB_CUDA(cudaEventRecord(rev_[1], s));
   VSGB_CUDA(cudaEventSynchronize(rev_[1]));
+  resident_finish(s);
+}
+
+void PcgEngine::resident_finish(cudaStream_t s) {
   float ms = 0.f;
   VSGB_CUDA(cudaEventElapsedTime(&ms, rev_[0], rev_[1]));
   resident_ms_ += ms;
@@ -948,12 +952,22 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
     if (resident_used(true)) {
       // One launch: FP32 inner solve of the scaled correction and the FP64
       // accumulation u += delta / scale.
+      // The true residual is launched right behind it, and both records come
+      // back after one synchronisation (the residual is not used when the
+      // inner solve failed).
       resident_begin(s, bsr_.val32.ptr, static_cast<size_t>(bsr_.steps) * 288 * sizeof(float));
       resident_solve32(bsr_, res_, r_.ptr, u_.ptr, scal_.ptr, scal_.ptr + 1, itol,
                        max_iters, s, op_->dinv.ptr, bj);
-      resident_end(s);
+      VSGB_CUDA(cudaEventRecord(rev_[1], s));
       ++launches_;
-      read_scalars(s, host, 0);
+      launch_residual64(s, d_f);
+      VSGB_LAUNCH_CHECK();
+      ++launches_;
+      VSGB_CUDA(cudaMemcpyAsync(host, scal_.ptr, 2 * sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                s));
+      VSGB_CUDA(cudaStreamSynchronize(s));
+      resident_finish(s);
+      outer = host[1];
       resident_iters_ += host->iter;
       if (host->flags & kFlagResidentAbort)
         throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
@@ -969,10 +983,6 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
         res.inner_failed = true;
         return;
       }
-      launch_residual64(s, d_f);
-      VSGB_LAUNCH_CHECK();
-      ++launches_;
-      read_scalars(s, &outer, 1);
       res.rel = outer.rel;
       if (outer.rel <= tol) {
         res.converged = true;

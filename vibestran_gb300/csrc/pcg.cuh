@@ -39,6 +39,7 @@ class PcgEngine {
   void solve_fp64(const double* d_f, double tol, int max_iters, cudaStream_t s,
                   PcgScalars* host_pinned, SolveResult& res);
   // FP32 inner PCG + FP64 refinement on the GPU; solution in solution().
+  // host_pinned holds two records (inner solve, outer residual).
   void solve_mixed(const double* d_f, double tol, double inner_tol, int max_iters,
                    int max_solves, cudaStream_t s, PcgScalars* host_pinned, SolveResult& res);
 
@@ -132,6 +133,7 @@ class PcgEngine {
   long long resident_iters_ = 0;
   void resident_begin(cudaStream_t s, const void* hot, size_t hot_bytes);  // before the launch
   void resident_end(cudaStream_t s);    // right after it (waits for it)
+  void resident_finish(cudaStream_t s); // once rev_[1] (the launch's end) has completed
   bool l2_persist_ = false;
   bool adaptive_inner_ = true;
   int precond_ = 0;
