@@ -69,16 +69,15 @@ static_assert(sizeof(WarpSmem) % 16 == 0, "per-warp areas and the Ke copy need 1
 __device__ __forceinline__ int pp_first(int u) { return u < 3 ? 0 : (u < 5 ? 1 : 2); }
 __device__ __forceinline__ int pp_second(int u) { return u < 3 ? u : (u < 5 ? u - 2 : 2); }
 
-// 1/d in FP64 from an FP32 seed and two Newton-Raphson steps
-// y <- y + y (1 - d y): quadratic convergence takes the ~2^-23 seed error
-// below FP64 rounding (the result is within an ulp or so of the rounded
-// quotient).  Outside the FP32 range the FP64 division is used.
+// 1/d in FP64 from the correctly rounded FP32 reciprocal and one
+// Newton-Raphson step y <- y + y (1 - d y): quadratic convergence takes the
+// <= 2^-24 relative error of the seed (plus the 2^-24 of rounding d to FP32)
+// to ~2^-46, far inside the 1e-12 agreement the element matrices are held
+// to.  Outside the FP32 range the FP64 division is used.
 __device__ __forceinline__ double rcp_nr(double d) {
   if (!(d > 1e-30 && d < 1e30)) return 1.0 / d;
-  double y = static_cast<double>(__frcp_rn(static_cast<float>(d)));
-  y = fma(y, fma(-d, y, 1.0), y);
-  y = fma(y, fma(-d, y, 1.0), y);
-  return y;
+  const double y = static_cast<double>(__frcp_rn(static_cast<float>(d)));
+  return fma(y, fma(-d, y, 1.0), y);
 }
 
 __device__ __forceinline__ int pair_index(int A, int B) {  // A <= B < 11
