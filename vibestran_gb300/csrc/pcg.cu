@@ -928,16 +928,23 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
   VSGB_LAUNCH_CHECK();
   ++launches_;
   PcgScalars outer{};
-  read_scalars(s, &outer, 1);
   res.iterations = 0;
   res.inner_solves = 0;
   res.converged = false;
-  res.rel = outer.rel;
-  if (outer.flags & kFlagZeroRhs) {
-    res.converged = true;
-    res.rel = 0.0;
-    return;
+  const bool resident = resident_used(true);
+  if (resident) {
+    // u starts at 0, so the true residual starts at 1 (0 for a zero right-hand
+    // side, which the first inner solve reports): no read-back needed here.
+    outer.rel = 1.0;
+  } else {
+    read_scalars(s, &outer, 1);
+    if (outer.flags & kFlagZeroRhs) {
+      res.converged = true;
+      res.rel = 0.0;
+      return;
+    }
   }
+  res.rel = outer.rel;
   double prev = 0.0;
   bool have_prev = false;
   for (int step = 0; step < max_solves; ++step) {
@@ -969,6 +976,11 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       resident_finish(s);
       outer = host[1];
       resident_iters_ += host->iter;
+      if (step == 0 && (host->flags & kFlagZeroRhs)) {  // f = 0: u stays 0
+        res.converged = true;
+        res.rel = 0.0;
+        return;
+      }
       if (host->flags & kFlagResidentAbort)
         throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
       if (host->flags & kFlagNonPosRz)
