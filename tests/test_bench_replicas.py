@@ -55,3 +55,26 @@ def test_single_process_needs_no_process_group():
     dist, r, w = bench._dist()
     assert dist is None and r == 0 and w == 1
     assert bench._allmax(dist, 0.02) == 0.02
+
+
+def test_reference_arm_json_line():
+    """`bench.py --impl reference` (the CPU port of the reference path, no GPU)
+    prints one JSON line with the fields the harness reads: the headline metric
+    and unit, impl, a cpu_baseline describing the run and an e2e object with no
+    host-device traffic."""
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "1"], cwd=ROOT, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "s" and d["higher_is_better"] is False
+    assert d["steps"] == 1 and d["warmup"] == 1 and d["value"] > 0.0
+    assert d["config"]["workload"] == "cantilever_84k"
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert d["e2e"]["value"] == d["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
