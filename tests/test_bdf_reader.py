@@ -1,8 +1,8 @@
 """Native BDF reader (vsgb_bdf_*, host only): card assembly and number rules
 of the reference's BdfParser (src/io/bdf_parser.cpp) on the SOL 101 CHEXA8
 deck subset, checked against decks written in every field format, the
-reference generator's deck, the reference's own CHEXA8 e2e decks (when the
-reference is checked out next to this repository) and the oracle."""
+reference generator's deck, the reference's own CHEXA8 e2e decks (copied into
+tests/golden/ref_e2e by tests/golden/make_ref_decks.py) and the oracle."""
 import os
 
 import numpy as np
@@ -10,7 +10,7 @@ import pytest
 
 from conftest import GOLDEN, model_from_spec
 
-REF_CASES = "/root/reference/tests/e2e/cases"
+REF_CASES = os.path.join(GOLDEN, "ref_e2e")
 
 
 @pytest.fixture(scope="module")
@@ -174,9 +174,8 @@ def test_reference_generator_deck(B, oracle):
     assert 1.0 < np.mean(u[tip]) / 1.25e-5 < 1.15
 
 
-# ── the reference's own CHEXA8 decks, when checked out beside this repo ─────
+# ── the reference's own CHEXA8 e2e decks (fixtures copied from its tests) ─────
 
-@pytest.mark.skipif(not os.path.isdir(REF_CASES), reason="reference checkout not present")
 def test_reference_axial_deck(B, known):
     d = B.read_bdf(path=os.path.join(REF_CASES, "chexa8_axial_force.bdf"))
     m = d.model()
@@ -184,13 +183,9 @@ def test_reference_axial_deck(B, known):
     assert "PARAM" not in d.warnings
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_CASES), reason="reference checkout not present")
 @pytest.mark.parametrize("name", ["chexa8_constrained_thermal", "chexa8_free_thermal"])
 def test_reference_thermal_decks_are_refused(B, name):
-    path = os.path.join(REF_CASES, name + ".bdf")
-    if not os.path.exists(path):
-        pytest.skip("deck not present")
-    d = B.read_bdf(path=path)
+    d = B.read_bdf(path=os.path.join(REF_CASES, name + ".bdf"))
     with pytest.raises(B.SolverError, match="temperature"):
         d.model()
 

@@ -185,3 +185,34 @@ def test_adjoint_sensitivity_small(vsgb, oracle, be):
     assert np.abs(g - ref).max() <= 1e-10 * np.abs(ref).max()
     # compliance identity: sum_e E_e dC/dE_e = -F^T u
     assert abs(np.sum(m.E * g) + F @ u) <= 1e-9 * abs(F @ u)
+
+
+def test_distorted_eas_hexes_match_numpy_restatement(vsgb, be):
+    """The GPU element kernel on the two distorted hexes of
+    tests/golden/eas_distorted_hex.json (independent numpy restatement of the
+    reference's EAS element with its row-of-J0^-1 enhancement mapping)."""
+    import json
+    import os
+
+    from conftest import GOLDEN
+    from vibestran_gb300 import cantilever as C
+    with open(os.path.join(GOLDEN, "eas_distorted_hex.json")) as fh:
+        cases = json.load(fh)["cases"]
+    for c in cases:
+        m = C.SolidModel(node_ids=np.arange(1, 9, dtype=np.int32), xyz=np.array(c["xyz"]),
+                         conn=np.arange(8, dtype=np.int32).reshape(1, 8),
+                         elem_ids=np.array([1], np.int32), E=np.array([c["E"]]),
+                         nu=np.array([c["nu"]]), form=np.array([0], np.int32),
+                         spc_nodes=np.zeros(0, np.int32), spc_mask=np.zeros(0, np.int32),
+                         loads=[], name=c["name"], shape=(1, 1, 1))
+        eq6, n = vsgb.build_dof_map(m)
+        assert n == 24 and np.array_equal(eq6[:, :3].reshape(-1), np.arange(24))
+        asm = vsgb.ChexaAssembler(be)
+        asm.assemble(m, eq6, n)
+        K = asm.csr_lower()
+        dense = np.zeros((24, 24))
+        for r in range(24):
+            for k in range(K.row_ptr[r], K.row_ptr[r + 1]):
+                dense[r, K.col_ind[k]] = K.values[k]
+        ref = np.tril(np.array(c["ke"]))
+        assert np.abs(dense - ref).max() <= 1e-12 * np.abs(ref).max(), c["name"]
