@@ -1004,6 +1004,154 @@ int orc_pcg_mixed(void* h, const double* F, double tol, int max_iters, double* u
   }
 }
 
+// IC(0)-preconditioned CG: the CPU baseline beside the reference's cpu-pcg
+// backend (src/solver/solver_backend.cpp:349-462, Eigen ConjugateGradient with
+// IncompleteCholesky).  NOT Eigen's IncompleteCholesky (a threshold
+// factorisation with fill, AMD ordering and its own scaling, whose iteration
+// counts cannot be pinned without restating Eigen): this is the zero-fill
+// incomplete Cholesky on K's own lower pattern, after the symmetric scaling
+// D^-1/2 K D^-1/2 (unit diagonal), with a diagonal shift that starts at 0 and
+// becomes 1e-3, 2e-3, ... while a pivot is not positive (the Manteuffel
+// shift).  CG stops, as Eigen's does, on the unpreconditioned residual:
+// ||b - K u|| < tol ||b|| (recurrence residual).  Triangular solves are
+// serial; the matvec uses all threads.
+struct Ic0 {
+  int n = 0;
+  std::vector<int> rp, ci;   // lower pattern, columns ascending, diagonal last
+  std::vector<double> l;     // factor values
+  std::vector<double> s;     // scaling D^-1/2
+  double shift = 0.0;
+};
+
+static bool ic0_factor(const Csr& L, double shift, Ic0& f) {
+  const int n = L.n;
+  f.l.assign(L.values.size(), 0.0);
+  for (int i = 0; i < n; ++i) {
+    const int b = f.rp[i], e = f.rp[i + 1];
+    for (int p = b; p < e; ++p) {
+      const int k = f.ci[p];
+      double v = L.values[p] * f.s[i] * f.s[k];
+      if (k == i) {
+        v += shift;
+        for (int q = b; q < p; ++q) v -= f.l[q] * f.l[q];
+        if (!(v > 0.0)) return false;
+        f.l[p] = std::sqrt(v);
+      } else {
+        // sum over j < k in both row i and row k
+        int q = b, r = f.rp[k];
+        const int re = f.rp[k + 1] - 1;  // row k without its diagonal
+        while (q < p && r < re) {
+          const int cq = f.ci[q], cr = f.ci[r];
+          if (cq == cr) {
+            v -= f.l[q] * f.l[r];
+            ++q;
+            ++r;
+          } else if (cq < cr) {
+            ++q;
+          } else {
+            ++r;
+          }
+        }
+        f.l[p] = v / f.l[f.rp[k + 1] - 1];
+      }
+    }
+  }
+  return true;
+}
+
+// z = (S L L^T S)^-1 r in the original variables: z = S L^-T L^-1 S r
+static void ic0_apply(const Ic0& f, const std::vector<double>& r, std::vector<double>& z) {
+  const int n = f.n;
+  for (int i = 0; i < n; ++i) {
+    double v = r[i] * f.s[i];
+    const int e = f.rp[i + 1] - 1;
+    for (int p = f.rp[i]; p < e; ++p) v -= f.l[p] * z[f.ci[p]];
+    z[i] = v / f.l[e];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    const int e = f.rp[i + 1] - 1;
+    const double xi = z[i] / f.l[e];
+    z[i] = xi;
+    for (int p = f.rp[i]; p < e; ++p) z[f.ci[p]] -= f.l[p] * xi;
+  }
+  for (int i = 0; i < n; ++i) z[i] *= f.s[i];
+}
+
+int orc_pcg_ic0(void* h, const double* F, double tol, int max_iters, double* u_out, int* iters,
+                double* rel, double* shift_out, char* err, int errlen) {
+  const Csr& K = *static_cast<Csr*>(h);
+  *iters = 0;
+  *rel = 0.0;
+  try {
+    validate(K, static_cast<size_t>(K.n));
+    const int n = K.n;
+    const Csr L = K.lower ? K : lower_triangle(K);
+    const Csr full = expanded_symmetric(L);
+    Ic0 f;
+    f.n = n;
+    f.rp = L.row_ptr;
+    f.ci = L.col_ind;
+    f.s.resize(n);
+    for (int i = 0; i < n; ++i) {
+      const int e = L.row_ptr[i + 1] - 1;
+      if (e < L.row_ptr[i] || L.col_ind[e] != i || !(L.values[e] > 0.0))
+        throw Error("IC(0): missing or non-positive diagonal at row " + std::to_string(i));
+      f.s[i] = 1.0 / std::sqrt(L.values[e]);
+    }
+    double shift = 0.0;
+    while (!ic0_factor(L, shift, f)) {
+      shift = shift == 0.0 ? 1e-3 : 2.0 * shift;
+      if (shift > 1e3) throw Error("IC(0): no positive shift found");
+    }
+    *shift_out = shift;
+    std::vector<double> u(n, 0.0), r(F, F + n), z(n), p(n), Ap(n);
+    const double norm_b = std::sqrt(dot(r, r));
+    if (norm_b < 1e-300) {
+      std::fill(u_out, u_out + n, 0.0);
+      return 0;
+    }
+    ic0_apply(f, r, z);
+    p = z;
+    double rz = dot(r, z);
+    int it = 0;
+    double rr_rel = 1.0;
+    bool conv = false;
+    for (; it < max_iters; ++it) {
+      spmv_full(full, full.values, p, Ap);
+      const double pAp = dot(p, Ap);
+      if (!(pAp > 0.0)) break;
+      const double alpha = rz / pAp;
+#pragma omp parallel for schedule(static)
+      for (int i = 0; i < n; ++i) {
+        u[i] += alpha * p[i];
+        r[i] -= alpha * Ap[i];
+      }
+      rr_rel = std::sqrt(dot(r, r)) / norm_b;
+      if (rr_rel < tol) {
+        ++it;
+        conv = true;
+        break;
+      }
+      ic0_apply(f, r, z);
+      const double rz_new = dot(r, z);
+      const double beta = rz_new / rz;
+      rz = rz_new;
+#pragma omp parallel for schedule(static)
+      for (int i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    }
+    *iters = it;
+    *rel = rr_rel;
+    std::copy(u.begin(), u.end(), u_out);
+    if (!conv)
+      throw Error("IC(0) PCG did not converge after " + std::to_string(max_iters) +
+                  " iterations (relative residual " + std::to_string(rr_rel) + ")");
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, errlen, e.what());
+    return -1;
+  }
+}
+
 // Dense LLT solve of the symmetric system (lower or full storage) — the
 // direct-solve stand-in for --backend=cpu at sizes a dense factor affords.
 int orc_dense_cholesky_solve(void* h, const double* F, double* u_out, char* err, int errlen) {

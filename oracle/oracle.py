@@ -80,6 +80,9 @@ def lib():
         L.orc_pcg_mixed.argtypes = [_vp, _f64p, ctypes.c_double, ci, _f64p, ctypes.POINTER(ci),
                                     ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_double), cp, ci]
         L.orc_dense_cholesky_solve.argtypes = [_vp, _f64p, _f64p, cp, ci]
+        L.orc_pcg_ic0.argtypes = [_vp, _f64p, ctypes.c_double, ci, _f64p, ctypes.POINTER(ci),
+                                  ctypes.POINTER(ctypes.c_double),
+                                  ctypes.POINTER(ctypes.c_double), cp, ci]
         _lib = L
     return _lib
 
@@ -276,6 +279,25 @@ def pcg_mixed(K: Csr, F, tol=1e-6, max_iters=10000):
     if rc != 0:
         raise OracleError(err.value.decode())
     return u, it.value, ns.value, rel.value
+
+
+def pcg_ic0(K: Csr, F, tol=1e-8, max_iters=10000):
+    """IC(0)-preconditioned CG (zero-fill incomplete Cholesky of the unit-diagonal
+    scaled K, Manteuffel shift), the CPU baseline beside the reference's cpu-pcg
+    (Eigen CG + IncompleteCholesky, src/solver/solver_backend.cpp:349-462) — not
+    Eigen's factorisation.  Returns (u, iterations, relative residual, shift)."""
+    u = np.zeros(K.n)
+    it = ctypes.c_int()
+    rel = ctypes.c_double()
+    shift = ctypes.c_double()
+    err = _err()
+    with K.handle() as h:
+        rc = lib().orc_pcg_ic0(h.ptr, np.ascontiguousarray(F, np.float64), float(tol),
+                               int(max_iters), u, ctypes.byref(it), ctypes.byref(rel),
+                               ctypes.byref(shift), err, 512)
+    if rc != 0:
+        raise OracleError(err.value.decode())
+    return u, it.value, rel.value, shift.value
 
 
 def direct_solve(K: Csr, F):

@@ -64,9 +64,13 @@ def test_reference_arm_json_line():
     host-device traffic."""
     import json
     import subprocess
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                        "--steps", "1", "--warmup", "1"], cwd=ROOT, capture_output=True,
-                       text=True, timeout=600)
+    # run bench.py's main in a child that reports, afterwards, whether the
+    # product library was ever mapped into it (the arm must be oracle-only)
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', "
+            "'--warmup', '1']; runpy.run_path('bench.py', run_name='__main__'); "
+            "print('PRODUCT_LIB_MAPPED', 'libvsgb' in open('/proc/self/maps').read())")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=900)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
     assert len(lines) == 1
@@ -78,3 +82,10 @@ def test_reference_arm_json_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert "PRODUCT_LIB_MAPPED False" in r.stdout
+    # the reference's other CPU solver families, restated and timed beside it
+    ic0 = cb["other_solvers"]["ic0_pcg"]
+    assert ic0["iterations"] > 0 and ic0["value"] > 0.0 and "IC(0)" in ic0["label"]
+    sd = cb["other_solvers"]["sparse_direct"]
+    assert [x["dofs"] for x in sd["samples"]] == [1500, 35910]
+    assert cb["rel_err_vs_direct"] < 1e-6
