@@ -47,10 +47,13 @@ extern "C" {
 #define VSGB_SRI 1 /* CHexa8 selective reduced integration (ISOP = SRI) */
 
 /* ── options for vsgb_set_option ────────────────────────────────────────── */
-#define VSGB_OPT_TOLERANCE 1      /* relative residual target (default 1e-8 FP64, 1e-6 mixed) */
+#define VSGB_OPT_TOLERANCE 1      /* relative residual target (default 1e-8 FP64, 1e-6 mixed);
+                                     the stopping test of a solve that is not
+                                     error-controlled (VSGB_OPT_ERROR_TARGET) */
 #define VSGB_OPT_MAX_ITERS 2      /* max PCG iterations per solve (default 10000) */
 #define VSGB_OPT_PRECISION 3      /* VSGB_FP64 or VSGB_MIXED */
-#define VSGB_OPT_INNER_TOL 4      /* mixed: inner FP32 tolerance (<=0: clamp(100*tol,1e-4,1e-2)) */
+#define VSGB_OPT_INNER_TOL 4      /* mixed: inner FP32 tolerance (<=0: 1e-3 when error-controlled,
+                                     otherwise clamp(100*tol,1e-4,1e-2) as cuda-pcg-mixed) */
 #define VSGB_OPT_MAX_SOLVES 5     /* mixed: max inner solves (default 3 = 1 + 2 corrections) */
 #define VSGB_OPT_CHECK_EVERY 6    /* iterations launched between host convergence checks */
 #define VSGB_OPT_USE_GRAPH 7      /* 1: replay iteration batches as CUDA graphs (default 1) */
@@ -78,6 +81,29 @@ extern "C" {
                                      VSGB_ERR_INVALID, a block that is not positive
                                      definite VSGB_ERR_SINGULAR */
 
+#define VSGB_OPT_ERROR_TARGET 14  /* relative displacement error target of an
+                                     error-controlled solve; < 0 (default): 1e-6 for
+                                     mixed precision unless a residual tolerance was
+                                     chosen (vsgb_create tol > 0 or VSGB_OPT_TOLERANCE
+                                     > 0), off for FP64; 0: off (the reference's
+                                     residual test, VSGB_OPT_TOLERANCE).
+                                     The solve estimates its error in the
+                                     preconditioner's norm from its own recurrence
+                                     (Hestenes-Stiefel identity over blocks of 16
+                                     iterations: a geometric tail of the current error
+                                     and a 32-iteration delayed bound, both within
+                                     target/3 in two blocks in a row) and ignores the
+                                     residual tolerance.  Mixed: the first inner solve stops on
+                                     VSGB_OPT_INNER_TOL, every later one on the error
+                                     estimate; FP64: one estimate-stopped solve.
+                                     Persistent solves and the batched solve only (the
+                                     launch-per-kernel path keeps the residual test).
+                                     No reference counterpart. */
+#define VSGB_OPT_SPIN_LIMIT 15    /* polls of a grid wait of the persistent solve before
+                                     it gives up and the solve returns VSGB_ERR_CUDA
+                                     ("a grid barrier ... timed out"); <= 0: the default
+                                     (2^22, about a second).  For tests of that path. */
+
 #define VSGB_PRECOND_JACOBI 0
 #define VSGB_PRECOND_BLOCK_JACOBI 1
 
@@ -98,6 +124,8 @@ typedef struct vsgb_stats {
                             kernels of this solve, CUDA events around each launch;
                             0 when the launch-per-kernel path ran */
   double kernel_iterations; /* PCG iterations those launches ran */
+  double est_rel_error;  /* error-controlled solve: estimated relative displacement
+                            error (max over load cases); -1 when not estimated */
 } vsgb_stats;
 
 /* Create a context on `device` (cuda-pcg uses device 0,
@@ -318,10 +346,17 @@ int vsgb_rhs_stats(vsgb_ctx* ctx, int k, int* iterations, double* rel_residual, 
  * about 2.7 MB) is one static __device__ array that every GPU loading the
  * library holds until exit, so n is limited to VSGB_NOALLOC_MAX_N (larger n
  * returns VSGB_ERR_LIMIT).  The first call on a device resolves the array's
- * device address — make it before any stream capture on that device.  All
- * calls share the array: calls that overlap on the GPU (other streams or
- * host threads) race and must be serialised by the caller.  err receives the
- * message of a failure (may be NULL). */
+ * device address — make it before any stream capture on that device.  That
+ * address is kept for the device's primary context of that moment: after a
+ * cudaDeviceReset the library must be loaded again (a new process) before
+ * this entry point is used on that device.  All calls share the array: calls
+ * that overlap on the GPU (other streams or host threads) race and must be
+ * serialised by the caller.  The row pointer is checked on the device before
+ * anything is read through it (VSGB_ERR_INVALID); column indices outside
+ * [0, n) are VSGB_ERR_INVALID, a zero or missing diagonal VSGB_ERR_SINGULAR.
+ * A non-positive p*Ap stops the solve as in cuda-pcg: iterations_out is then
+ * max_iters and VSGB_ERR_NOT_CONVERGED is returned.  err receives the message
+ * of a failure (may be NULL). */
 int vsgb_pcg_solve_noalloc(int n, int nnz, const int* d_row_ptr, const int* d_col_ind,
                            const double* d_values, const double* d_F, double* d_u, double tol,
                            int max_iters, void* stream, int* iterations_out,

@@ -116,3 +116,35 @@ def test_batched_not_converged_raises(vsgb, multi_model):
     with pytest.raises(vsgb.SolverError, match="did not converge after 5 iterations"):
         asm.solve(F[:, :4])
     be.close()
+
+
+def test_batched_error_controlled_defaults(vsgb, multi_model):
+    """Default mixed options (no tolerance chosen): every load case of the
+    batch error-controlled to 1e-6 (errest.cuh) against the sparse-direct
+    solutions, a zero case included; FP64 with the same target.  This small
+    jittered block (n = 2 352) converges in ~250 iterations with block sums
+    that jump by 100x between blocks, the hardest case measured for the
+    estimate (its worst case sits at about half the target); the full-size
+    workloads are held to half the target in test_gpu_error_control.py."""
+    m, eq6, n, F, U = multi_model
+    G = F.copy()
+    G[:, 5] = 0.0
+    be = vsgb.Gb300MixedPcgSolverBackend.try_create()
+    be.set_option(vsgb.OPT_BATCHED, 2)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    Ub = asm.solve(G)
+    for k in range(N_CASES):
+        s = be.rhs_stats(k)
+        assert s["batched"] and s["converged"], (k, s)
+        if k == 5:
+            assert np.abs(Ub[:, k]).max() == 0.0 and s["iterations"] == 0
+        else:
+            assert _rel(Ub[:, k], U[:, k]) <= 1e-6, k
+    assert 0.0 <= be.last_stats.est_rel_error <= 3.4e-7
+    be.set_option(vsgb.OPT_PRECISION, vsgb.FP64)
+    be.set_option(vsgb.OPT_ERROR_TARGET, 1e-6)
+    U64 = asm.solve(F)
+    for k in range(N_CASES):
+        assert _rel(U64[:, k], U[:, k]) <= 1e-6, k
+    be.close()

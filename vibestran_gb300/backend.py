@@ -57,6 +57,8 @@ OPT_BATCHED = 10
 OPT_L2_PERSIST = 11
 OPT_ADAPTIVE_INNER = 12
 OPT_PRECOND = 13
+OPT_ERROR_TARGET = 14
+OPT_SPIN_LIMIT = 15
 
 PRECOND_JACOBI = 0
 PRECOND_BLOCK_JACOBI = 1
@@ -101,7 +103,8 @@ class VsgbStats(ctypes.Structure):
                 ("converged", ctypes.c_int), ("format", ctypes.c_int),
                 ("rel_residual", ctypes.c_double), ("solve_ms", ctypes.c_double),
                 ("setup_ms", ctypes.c_double), ("spmv_bytes", ctypes.c_double),
-                ("kernel_ms", ctypes.c_double), ("kernel_iterations", ctypes.c_double)]
+                ("kernel_ms", ctypes.c_double), ("kernel_iterations", ctypes.c_double),
+                ("est_rel_error", ctypes.c_double)]
 
 
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

@@ -36,6 +36,8 @@ struct vsgb_ctx {
   int precision = VSGB_FP64;
   double inner_tol = 0.0;
   int max_solves = 3;
+  double err_target = -1.0;  // < 0: automatic (mixed 1e-6 unless tol was set, FP64 off)
+  bool tol_explicit = false; // the caller chose the residual tolerance
   int format = 0;
 
   // resident mesh
@@ -98,8 +100,23 @@ int guarded(vsgb_ctx* c, F&& fn) {
 
 double default_tol(int precision) { return precision == VSGB_MIXED ? 1e-6 : 1e-8; }
 
-double inner_tolerance(const vsgb_ctx* c) {
+// Relative displacement error target of the next solve (0: the reference's
+// residual test).  Mixed precision controls the error by default (1e-6, the
+// accuracy the mixed form is quoted at) unless the caller chose a residual
+// tolerance; FP64 keeps cuda-pcg's residual test unless a target is set.
+double error_target(const vsgb_ctx* c) {
+  if (c->err_target >= 0.0) return c->err_target;
+  return (c->precision == VSGB_MIXED && !c->tol_explicit) ? 1e-6 : 0.0;
+}
+
+double inner_tolerance(const vsgb_ctx* c, bool batched) {
   if (c->inner_tol > 0.0) return c->inner_tol;
+  // error-controlled refinement (batched, or persistent single solves): the
+  // first inner solve only has to bring the error to where the next,
+  // error-controlled step takes over
+  if (c->precision == VSGB_MIXED && error_target(c) > 0.0 &&
+      (batched || c->eng->resident_used(true)))
+    return 1e-3;
   // cuda_pcg_backend_impl.hpp:2166-2171: clamp(100 * tol, 1e-4, 1e-2)
   double t = c->tol * 100.0;
   if (t < 1e-4) t = 1e-4;
@@ -178,8 +195,9 @@ void run_batched(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
   const int n = c->K.n;
   c->u.reserve(static_cast<size_t>(n) * nrhs);
   const bool mixed = c->precision == VSGB_MIXED;
+  c->eng->set_error_target(error_target(c));
   VSGB_CUDA(cudaEventRecord(c->ev[0], c->stream));
-  c->eng->solve_multi(c->f.ptr, nrhs, c->u.ptr, mixed, c->tol, inner_tolerance(c), c->max_iters,
+  c->eng->solve_multi(c->f.ptr, nrhs, c->u.ptr, mixed, c->tol, inner_tolerance(c, true), c->max_iters,
                       c->max_solves, c->stream, c->rhs);
   VSGB_CUDA(cudaEventRecord(c->ev[1], c->stream));
   VSGB_CUDA(cudaEventSynchronize(c->ev[1]));
@@ -189,10 +207,12 @@ void run_batched(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
   vsgb_stats st{};
   st.format = c->eng->format_used();
   st.converged = 1;
+  st.est_rel_error = -1.0;
   for (const vsgb::SolveResult& r : c->rhs) {
     st.iterations = r.iterations > st.iterations ? r.iterations : st.iterations;
     st.inner_solves += r.inner_solves;
     st.rel_residual = r.rel > st.rel_residual ? r.rel : st.rel_residual;
+    if (r.err_est > st.est_rel_error) st.est_rel_error = r.err_est;
     if (!r.converged) st.converged = 0;
   }
   c->last_iters = st.iterations;
@@ -235,13 +255,16 @@ void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
   st.format = c->eng->format_used();
   st.inner_solves = 0;
   st.converged = 1;
+  st.est_rel_error = -1.0;
+  c->eng->set_error_target(error_target(c));
   float ms_total = 0.f;
   for (int k = 0; k < nrhs; ++k) {
     const double* fk = c->f.ptr + static_cast<size_t>(k) * n;
     vsgb::SolveResult res;
     VSGB_CUDA(cudaEventRecord(c->ev[0], c->stream));
     if (c->precision == VSGB_MIXED) {
-      c->eng->solve_mixed(fk, c->tol, inner_tolerance(c), c->max_iters, c->max_solves, c->stream,
+      c->eng->solve_mixed(fk, c->tol, inner_tolerance(c, false), c->max_iters, c->max_solves,
+                          c->stream,
                           c->h_scal, res);
     } else {
       c->eng->solve_fp64(fk, c->tol, c->max_iters, c->stream, c->h_scal, res);
@@ -258,6 +281,7 @@ void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
     st.kernel_ms += c->eng->resident_ms();
     st.kernel_iterations += static_cast<double>(c->eng->resident_iterations());
     st.rel_residual = res.rel > st.rel_residual ? res.rel : st.rel_residual;
+    if (res.err_est > st.est_rel_error) st.est_rel_error = res.err_est;
     c->last_iters = res.iterations;
     c->last_rel = res.rel;
     c->rhs[static_cast<size_t>(k)] = res;
@@ -330,6 +354,7 @@ int vsgb_create(int device, double tol, int max_iters, int precision, vsgb_ctx**
   c->device_name = prop.name;
   c->precision = precision;
   c->tol = tol > 0.0 ? tol : default_tol(precision);
+  c->tol_explicit = tol > 0.0;
   c->max_iters = max_iters > 0 ? max_iters : 10000;
   int prio_low = 0, prio_high = 0;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -374,6 +399,7 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
     switch (option) {
       case VSGB_OPT_TOLERANCE:
         c->tol = value > 0.0 ? value : default_tol(c->precision);
+        c->tol_explicit = value > 0.0;
         break;
       case VSGB_OPT_MAX_ITERS:
         c->max_iters = value > 0 ? static_cast<int>(value) : 10000;
@@ -426,6 +452,12 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
         c->batched = b;
         break;
       }
+      case VSGB_OPT_ERROR_TARGET:
+        c->err_target = value;
+        break;
+      case VSGB_OPT_SPIN_LIMIT:
+        c->eng->set_spin_limit(static_cast<long long>(value));
+        break;
       default:
         throw Error(VSGB_ERR_INVALID, "unknown option " + std::to_string(option));
     }

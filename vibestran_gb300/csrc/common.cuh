@@ -86,10 +86,13 @@ struct PcgScalars {
   double norm_b;
   double tol;
   double scale;   // mixed: scale applied to the correction RHS
+  double uD2;     // mixed outer record: ||u||_D^2 of the outer iterate (D = Jacobi diagonal)
+  double err2;    // error-controlled solve: last estimate of ||e||_M^2 (< 0: none)
+  double total2;  // error-controlled solve: ||x||_M^2 of the iterate
   int iter;
   int max_iters;
   int flags;
-  int pad;
+  int abort;      // persistent solve: set by any CTA whose grid wait gave up
 };
 
 // ── Reductions ────────────────────────────────────────────────────────────

@@ -21,10 +21,13 @@
 // All reductions are fixed-order (per-lane -> warp -> block -> block-ordered
 // grid sum), so a batched solve is bitwise reproducible.
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
+#include "errest.cuh"
 #include "pcg.cuh"
 
 namespace vsgb {
@@ -47,10 +50,18 @@ struct MultiState {
   double tolk[kP];  // per-column stopping tolerance of this solve
   int flags[kP];
   int iters[kP];  // iteration count at which the column finished
+  // error-controlled stop (errest.cuh): mode, per-column absolute target^2,
+  // relative target^2 (or floor), and the scale^2 ||u||_D^2 the absolute
+  // target refers to (for reporting the estimate relative to ||u||)
+  int err_mode;
+  double err_t2[kP];
+  double err_rel2;
+  double err_norm2[kP];
 };
 
 struct MultiOuter {
   double norm_f[kP], rel[kP], prev[kP], scale[kP];
+  double uD2[kP];  // ||u||_D^2 of each column's outer iterate
   int flags[kP];
   int active[kP];  // column takes part in the current inner solve
   int done;
@@ -302,17 +313,23 @@ __device__ __forceinline__ void mspmm_slice(const MView& B, const T* __restrict_
 template <typename T, int G>
 __global__ void __launch_bounds__(kMT)
 k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restrict__ Ap,
-        MultiState* S, double* partials, unsigned* counter) {
+        const float* __restrict__ diag32, MultiState* S, ErrEst* est, double* partials,
+        unsigned* counter) {
   if (S->done) return;
   __shared__ double s_red[kMT];
-  __shared__ double s_tot[kP];
+  __shared__ double s_tot[2 * kP];
   constexpr int RN = G / 4;
   const int lane = threadIdx.x & 31;
   const int g0 = blockIdx.y * G, cb = g0 + (lane & 3) * RN;
   constexpr int wpb = kMT / 32;
+  const bool err_on = S->err_mode != kErrOff;
   T pap[RN];
+  float pmp[RN];
 #pragma unroll
-  for (int r = 0; r < RN; ++r) pap[r] = T(0);
+  for (int r = 0; r < RN; ++r) {
+    pap[r] = T(0);
+    pmp[r] = 0.f;
+  }
   // odd iterations walk the slices from the end: the operator lines read last
   // (the ones still in L2) are read first
   const bool rev = (S->iter & 1) != 0;
@@ -330,13 +347,25 @@ k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restr
         stn<RN>(Ap + o, out[i]);
 #pragma unroll
         for (int r = 0; r < RN; ++r) pap[r] = fmaT(pv[r], out[i][r], pap[r]);
+        if (err_on) {
+          // p.Dp per column for the error estimate (FP32 suffices)
+          const float d = __ldg(diag32 + 3 * R + i);
+#pragma unroll
+          for (int r = 0; r < RN; ++r) {
+            const float pf = static_cast<float>(pv[r]);
+            pmp[r] = fmaf(pf * pf, d, pmp[r]);
+          }
+        }
       }
     }
   }
-  double a[1][RN];
+  double a[2][RN];
 #pragma unroll
-  for (int r = 0; r < RN; ++r) a[0][r] = static_cast<double>(pap[r]);
-  if (mcol_sum_last<1, RN, kMT>(a, cb, partials, counter, s_red, s_tot)) {
+  for (int r = 0; r < RN; ++r) {
+    a[0][r] = static_cast<double>(pap[r]);
+    a[1][r] = static_cast<double>(pmp[r]);
+  }
+  if (mcol_sum_last<2, RN, kMT>(a, cb, partials, counter, s_red, s_tot)) {
     if (threadIdx.x < kP) {
       const int k = threadIdx.x;
       int f = S->flags[k];
@@ -349,6 +378,7 @@ k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restr
           S->iters[k] = S->iter;
         } else {
           S->alpha[k] = S->rz[k] / pAp;
+          if (err_on) err_record(est[k], S->rz[k], pAp, s_tot[kP + k]);
         }
         S->flags[k] = f;
       } else {
@@ -363,20 +393,23 @@ k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restr
 // r = f - K u (FP64) and ||r|| per column; updates the refinement record:
 // convergence (rel <= tol), stagnation (rel >= 0.9 * previous) and the scale
 // 1/||r|| of the next inner right-hand side.
+// With err_stop the residual test is replaced by the inner solve's outcome: a
+// column is done when its (refinement) inner solve met the error target.
 template <int G>
 __global__ void __launch_bounds__(kMT)
 k_mresidual(MView B, const double* __restrict__ vals, const double* __restrict__ u,
-            const double* __restrict__ f, double* __restrict__ r, MultiOuter* O, double tol,
-            double* partials, unsigned* counter) {
+            const double* __restrict__ f, const double* __restrict__ dinv,
+            double* __restrict__ r, MultiOuter* O, const MultiState* S, int err_stop,
+            double tol, double* partials, unsigned* counter) {
   __shared__ double s_red[kMT];
-  __shared__ double s_tot[kP];
+  __shared__ double s_tot[2 * kP];
   constexpr int RN = G / 4;
   const int lane = threadIdx.x & 31;
   const int g0 = blockIdx.y * G, cb = g0 + (lane & 3) * RN;
   constexpr int wpb = kMT / 32;
-  double a[1][RN];
+  double a[2][RN];
 #pragma unroll
-  for (int q = 0; q < RN; ++q) a[0][q] = 0.0;
+  for (int q = 0; q < RN; ++q) a[0][q] = a[1][q] = 0.0;
   for (int sl = blockIdx.x * wpb + (threadIdx.x >> 5); sl < B.nslices; sl += gridDim.x * wpb) {
     double out[3][RN];
     mspmm_slice<double, G>(B, vals, u, sl, lane, g0, out);
@@ -385,18 +418,21 @@ k_mresidual(MView B, const double* __restrict__ vals, const double* __restrict__
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         const size_t o = static_cast<size_t>(3 * R + i) * kP + cb;
-        double fv[RN], rv[RN];
+        double fv[RN], rv[RN], uv[RN];
         ldn<RN>(f + o, fv);
+        ldn<RN>(u + o, uv);
+        const double dg = 1.0 / dinv[3 * R + i];
 #pragma unroll
         for (int q = 0; q < RN; ++q) {
           rv[q] = fv[q] - out[i][q];
           a[0][q] = fma(rv[q], rv[q], a[0][q]);
+          a[1][q] = fma(uv[q] * uv[q], dg, a[1][q]);
         }
         stn<RN>(r + o, rv);
       }
     }
   }
-  if (mcol_sum_last<1, RN, kMT>(a, cb, partials, counter, s_red, s_tot)) {
+  if (mcol_sum_last<2, RN, kMT>(a, cb, partials, counter, s_red, s_tot)) {
     if (threadIdx.x < kP) {
       const int k = threadIdx.x;
       if (O->active[k]) {
@@ -405,10 +441,14 @@ k_mresidual(MView B, const double* __restrict__ vals, const double* __restrict__
         int fl = O->flags[k];
         O->rel[k] = rel;
         O->scale[k] = rn > 0.0 ? 1.0 / rn : 1.0;
-        if (rel <= tol)
+        O->uD2[k] = s_tot[kP + k];
+        if (err_stop) {
+          if (S->flags[k] & kFlagErrTarget) fl |= kFlagDone | kFlagConverged;
+        } else if (rel <= tol) {
           fl |= kFlagDone | kFlagConverged;
-        else if (O->prev[k] > 0.0 && rel >= O->prev[k] * 0.9)
+        } else if (O->prev[k] > 0.0 && rel >= O->prev[k] * 0.9) {
           fl |= kFlagDone | kFlagStalled;
+        }
         O->prev[k] = rel;
         O->flags[k] = fl;
         O->active[k] = (fl & kFlagDone) ? 0 : 1;
@@ -458,6 +498,7 @@ k_mouter_init(int n, int ncols, const double* __restrict__ f, double* __restrict
       O->rel[k] = (fl & kFlagDone) ? 0.0 : 1.0;
       O->prev[k] = 0.0;
       O->scale[k] = nb > 1e-300 ? 1.0 / nb : 1.0;
+      O->uD2[k] = 0.0;
       O->flags[k] = fl;
       O->active[k] = (fl & kFlagDone) ? 0 : 1;
     }
@@ -472,12 +513,16 @@ k_mouter_init(int n, int ncols, const double* __restrict__ f, double* __restrict
 
 // PCG start: r = src * scale (src = f, or the FP64 residual of the
 // refinement), u = 0, z = D^-1 r, p = z; r.z and r.r per column.
+// err_mode != kErrOff makes the columns error-controlled (errest.cuh):
+// kErrRelative with err_rel the relative target (FP64 solve), kErrAbsolute
+// with the target err_target * scale * ||u||_D of the column's outer record
+// and err_rel the relative floor (refinement steps of the mixed solve).
 template <typename T>
 __global__ void __launch_bounds__(kVT, 1)
 k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
         const T* __restrict__ dinv, T* __restrict__ r, T* __restrict__ u, T* __restrict__ p,
-        MultiState* S, double tol, double outer_tol, int max_iters, double* partials,
-        unsigned* counter) {
+        MultiState* S, ErrEst* est, int err_mode, double err_target, double err_rel,
+        double tol, double outer_tol, int max_iters, double* partials, unsigned* counter) {
   __shared__ double s_red[kVT];
   __shared__ double s_tot[2 * kP];
   const int cb = 4 * (threadIdx.x & 3);
@@ -537,6 +582,11 @@ k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
         tk = fmax(tol, fmin(0.5, want));
       }
       S->tolk[k] = tk;
+      err_reset(est[k]);
+      const double sk = O ? O->scale[k] : 1.0;
+      const double un2 = (O && err_mode == kErrAbsolute) ? sk * sk * O->uD2[k] : 0.0;
+      S->err_t2[k] = err_target * err_target * un2;
+      S->err_norm2[k] = un2;
       S->rz[k] = rzk;
       S->rr[k] = rrk;
       S->norm_b[k] = nb;
@@ -551,6 +601,8 @@ k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
       S->tol = tol;
       S->max_iters = max_iters;
       S->ncols = ncols;
+      S->err_mode = err_mode;
+      S->err_rel2 = err_rel * err_rel;
       all_done(S);
     }
   }
@@ -562,8 +614,8 @@ k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
 template <typename T>
 __global__ void __launch_bounds__(kVT, 1)
 k_mupdate(int n, T* __restrict__ u, T* __restrict__ r, const T* __restrict__ p,
-          const T* __restrict__ Ap, const T* __restrict__ dinv, MultiState* S, double* partials,
-          unsigned* counter) {
+          const T* __restrict__ Ap, const T* __restrict__ dinv, MultiState* S, ErrEst* est,
+          double* partials, unsigned* counter) {
   if (S->done) return;
   __shared__ double s_red[kVT];
   __shared__ double s_tot[2 * kP];
@@ -610,7 +662,20 @@ k_mupdate(int n, T* __restrict__ u, T* __restrict__ r, const T* __restrict__ p,
         const int it = S->iter + 1;
         S->rr[k] = rrk;
         S->rel[k] = rel;
-        if (rel < S->tolk[k]) {
+        bool conv;
+        if (S->err_mode != kErrOff) {
+          conv = err_block_end(est[k], S->err_t2[k], S->err_rel2);
+          bool met = conv && (S->err_mode == kErrRelative ||
+                              (est[k].est2 <= S->err_t2[k] && est[k].lag2 <= S->err_t2[k]));
+          if (!(fabs(rrk) > (sizeof(T) == 4 ? 1e-20 : 1e-28) * S->norm_b[k] * S->norm_b[k])) {
+            conv = true;
+            met = met || sizeof(T) == 8;
+          }
+          if (met) fl |= kFlagErrTarget;
+        } else {
+          conv = rel < S->tolk[k];
+        }
+        if (conv) {
           fl |= kFlagDone | kFlagConverged;
           S->beta[k] = 0.0;
           S->iters[k] = it;
@@ -685,6 +750,7 @@ struct MultiWork {
   DevBuf<float> r32, u32, p32, Ap32;      // FP32 panels (mixed inner solves)
   DevBuf<MultiState> S;
   DevBuf<MultiOuter> O;
+  DevBuf<ErrEst> est;  // per-column error estimate (kP)
   DevBuf<double> partials;
   DevBuf<unsigned> counters;
   MultiState* hS = nullptr;  // pinned
@@ -715,10 +781,12 @@ int occupancy_grid(const void* fn, int num_sms) {
 
 // One iteration for T: SpMM (+alpha), update (+beta, stopping test), direction.
 template <typename T, int G>
-void launch_multi_iter(const MView& B, const T* vals, const T* dinv, T* r, T* u, T* p, T* Ap,
-                       MultiWork& W, int n, dim3 sgrid, int vgrid, cudaStream_t s) {
-  k_mspmm<T, G><<<sgrid, kMT, 0, s>>>(B, vals, p, Ap, W.S.ptr, W.partials.ptr, W.counters.ptr + 1);
-  k_mupdate<T><<<vgrid, kVT, 0, s>>>(n, u, r, p, Ap, dinv, W.S.ptr, W.partials.ptr,
+void launch_multi_iter(const MView& B, const T* vals, const T* dinv, const float* diag32, T* r,
+                       T* u, T* p, T* Ap, MultiWork& W, int n, dim3 sgrid, int vgrid,
+                       cudaStream_t s) {
+  k_mspmm<T, G><<<sgrid, kMT, 0, s>>>(B, vals, p, Ap, diag32, W.S.ptr, W.est.ptr,
+                                      W.partials.ptr, W.counters.ptr + 1);
+  k_mupdate<T><<<vgrid, kVT, 0, s>>>(n, u, r, p, Ap, dinv, W.S.ptr, W.est.ptr, W.partials.ptr,
                                      W.counters.ptr + 2);
   k_mdirection<T><<<vgrid, kVT, 0, s>>>(n, r, dinv, p, W.S.ptr);
 }
@@ -761,7 +829,15 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
   }
   grow(W.S, 1);
   grow(W.O, 1);
+  grow(W.est, kP);
   grow(W.counters, 8);
+  // Error control (errest.cuh): FP64 columns stop on their own estimate
+  // relative to ||u||; mixed columns refine until a refinement step met the
+  // absolute target err_target * ||u||_D (first inner solve: inner_tol).
+  const bool err_control = err_target_ > 0.0;
+  const double err_goal = err_target_ / kErrSafety;
+  if (err_control) ensure_diag32(s);
+  const float* diag32 = res_.diag32.ptr;
   if (!W.hS) VSGB_CUDA(cudaMallocHost(&W.hS, sizeof(MultiState)));
   if (!W.hO) VSGB_CUDA(cudaMallocHost(&W.hO, sizeof(MultiOuter)));
 
@@ -789,11 +865,11 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
   auto batch = [&](bool fp32) {
     for (int k = 0; k < check_every_; ++k) {
       if (fp32)
-        launch_multi_iter<float, 16>(B, bsr_.val32.ptr, dinv32_.ptr, W.r32.ptr, W.u32.ptr,
-                                     W.p32.ptr, W.Ap32.ptr, W, n_, g32, vgrid, s);
+        launch_multi_iter<float, 16>(B, bsr_.val32.ptr, dinv32_.ptr, diag32, W.r32.ptr,
+                                     W.u32.ptr, W.p32.ptr, W.Ap32.ptr, W, n_, g32, vgrid, s);
       else
-        launch_multi_iter<double, 8>(B, bsr_.val64.ptr, op_->dinv.ptr, W.r64.ptr, W.u64.ptr,
-                                     W.p64.ptr, W.Ap64.ptr, W, n_, g64, vgrid, s);
+        launch_multi_iter<double, 8>(B, bsr_.val64.ptr, op_->dinv.ptr, diag32, W.r64.ptr,
+                                     W.u64.ptr, W.p64.ptr, W.Ap64.ptr, W, n_, g64, vgrid, s);
     }
     VSGB_LAUNCH_CHECK();
     VSGB_CUDA(cudaMemcpyAsync(W.hS, W.S.ptr, sizeof(MultiState), cudaMemcpyDeviceToHost, s));
@@ -845,6 +921,12 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
                         " -- preconditioner is not SPD or matrix is singular");
   };
 
+  std::vector<ErrEst> hest(kP);
+  auto read_est = [&]() {
+    VSGB_CUDA(cudaMemcpyAsync(hest.data(), W.est.ptr, sizeof(ErrEst) * kP, cudaMemcpyDeviceToHost,
+                              s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  };
   res.assign(static_cast<size_t>(nrhs), SolveResult{});
   const int pack_grid = static_cast<int>((n + 31) / 32);
   for (int k0 = 0; k0 < nrhs; k0 += kP) {
@@ -853,15 +935,17 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
     VSGB_LAUNCH_CHECK();
     ++launches_;
     if (!mixed) {
-      k_minit<double><<<vgrid, kVT, 0, s>>>(n_, nc, W.f.ptr, nullptr, op_->dinv.ptr, W.r64.ptr,
-                                            W.u64.ptr, W.p64.ptr, W.S.ptr, tol, 0.0, max_iters,
-                                            W.partials.ptr, W.counters.ptr);
+      k_minit<double><<<vgrid, kVT, 0, s>>>(
+          n_, nc, W.f.ptr, nullptr, op_->dinv.ptr, W.r64.ptr, W.u64.ptr, W.p64.ptr, W.S.ptr,
+          W.est.ptr, err_control ? kErrRelative : kErrOff, 0.0, err_goal, tol, 0.0, max_iters,
+          W.partials.ptr, W.counters.ptr);
       VSGB_LAUNCH_CHECK();
       ++launches_;
       read_state();
       check_start();
       if (!W.hS->done) iterate_all(false);
       read_state();
+      if (err_control) read_est();
       for (int k = 0; k < nc; ++k) {
         SolveResult& R = res[static_cast<size_t>(k0 + k)];
         const int fl = W.hS->flags[k];
@@ -869,6 +953,14 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
         R.rel = W.hS->rel[k];
         R.converged = (fl & kFlagConverged) != 0;
         R.breakdown = (fl & kFlagBreakdown) != 0;
+        if (err_control) {
+          R.err_met = (fl & kFlagErrTarget) != 0;
+          const ErrEst& e = hest[static_cast<size_t>(k)];
+          const double e2 = std::max(e.est2, e.lag2);
+          R.err_est = (e.est2 >= 0.0 && e.lag2 >= 0.0 && e.total2 > 0.0)
+                          ? std::sqrt(e2 / e.total2)
+                          : ((fl & kFlagZeroRhs) ? 0.0 : -1.0);
+        }
       }
     } else {
       k_mouter_init<<<vgrid, kVT, 0, s>>>(n_, nc, W.f.ptr, W.r64.ptr, W.u64.ptr, W.O.ptr,
@@ -878,22 +970,31 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
       read_outer();
       for (int k = 0; k < nc; ++k) res[static_cast<size_t>(k0 + k)].inner_solves = 0;
       for (int step = 0; step < max_solves && !W.hO->done; ++step) {
-        k_minit<float><<<vgrid, kVT, 0, s>>>(n_, nc, W.r64.ptr, W.O.ptr, dinv32_.ptr, W.r32.ptr,
-                                             W.u32.ptr, W.p32.ptr, W.S.ptr, inner_tol,
-                                             adaptive_inner_ ? tol : 0.0, max_iters,
-                                             W.partials.ptr, W.counters.ptr);
+        const bool err_step = err_control && step > 0;
+        k_minit<float><<<vgrid, kVT, 0, s>>>(
+            n_, nc, W.r64.ptr, W.O.ptr, dinv32_.ptr, W.r32.ptr, W.u32.ptr, W.p32.ptr, W.S.ptr,
+            W.est.ptr, err_step ? kErrAbsolute : kErrOff, err_goal, kErrRelFloor, inner_tol,
+            (adaptive_inner_ && !err_control) ? tol : 0.0, max_iters, W.partials.ptr,
+            W.counters.ptr);
         VSGB_LAUNCH_CHECK();
         ++launches_;
         read_state();
         check_start();
         if (!W.hS->done) iterate_all(true);
         read_state();
+        if (err_step) read_est();
         bool failed = false;
         for (int k = 0; k < nc; ++k) {
           if (!W.hO->active[k]) continue;
           SolveResult& R = res[static_cast<size_t>(k0 + k)];
           ++R.inner_solves;
           R.iterations += W.hS->iters[k];
+          if (err_step) {
+            const ErrEst& e = hest[static_cast<size_t>(k)];
+            if (e.est2 >= 0.0 && e.lag2 >= 0.0 && W.hS->err_norm2[k] > 0.0)
+              R.err_est = std::sqrt(std::max(e.est2, e.lag2) / W.hS->err_norm2[k]);
+            R.err_met = (W.hS->flags[k] & kFlagErrTarget) != 0;
+          }
           if (!(W.hS->flags[k] & kFlagConverged)) {
             R.inner_failed = true;
             R.breakdown = (W.hS->flags[k] & kFlagBreakdown) != 0;
@@ -903,8 +1004,10 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
         }
         if (failed) return;
         k_maccumulate<<<num_sms_, kVT, 0, s>>>(n_, W.u64.ptr, W.u32.ptr, W.O.ptr);
-        k_mresidual<8><<<gres, kMT, 0, s>>>(B, bsr_.val64.ptr, W.u64.ptr, W.f.ptr, W.r64.ptr,
-                                            W.O.ptr, tol, W.partials.ptr, W.counters.ptr + 4);
+        k_mresidual<8><<<gres, kMT, 0, s>>>(B, bsr_.val64.ptr, W.u64.ptr, W.f.ptr,
+                                            op_->dinv.ptr, W.r64.ptr, W.O.ptr, W.S.ptr,
+                                            err_step ? 1 : 0, err_control ? 0.0 : tol,
+                                            W.partials.ptr, W.counters.ptr + 4);
         VSGB_LAUNCH_CHECK();
         launches_ += 2;
         read_outer();

@@ -348,6 +348,7 @@ k_outer_init(int n, const double* __restrict__ f, double* __restrict__ r,
     O->rr = tot[0];
     O->rel = nb > 1e-300 ? 1.0 : 0.0;
     O->scale = nb > 1e-300 ? 1.0 / nb : 1.0;
+    O->uD2 = 0.0;
     O->flags = nb < 1e-300 ? (kFlagDone | kFlagZeroRhs | kFlagConverged) : 0;
     O->iter = 0;
   }
@@ -539,14 +540,16 @@ k_bsr_spmv32_fused(BsrView B, const float* __restrict__ vals, const float* __res
   }
 }
 
+// r = f - K u (FP64), ||r||^2 and ||u||_D^2 (D = 1 / dinv, the Jacobi
+// diagonal: the scale of an error-controlled refinement step's target).
 __global__ void __launch_bounds__(kSpmvThreads)
 k_bsr_residual64(BsrView B, const double* __restrict__ vals, const double* __restrict__ u,
-                 const double* __restrict__ f, double* __restrict__ r, PcgScalars* O,
-                 double* partials, unsigned* counter) {
-  __shared__ double sm[32];
+                 const double* __restrict__ f, const double* __restrict__ dinv,
+                 double* __restrict__ r, PcgScalars* O, double* partials, unsigned* counter) {
+  __shared__ double sm[64];
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
-  double acc[1] = {0.0};
+  double acc[2] = {0.0, 0.0};
   for (int sl = blockIdx.x * wpb + (threadIdx.x >> 5); sl < B.nslices; sl += gridDim.x * wpb) {
     double y0, y1, y2;
     bsr_row_block<double>(B, vals, sl, lane,
@@ -562,14 +565,17 @@ k_bsr_residual64(BsrView B, const double* __restrict__ vals, const double* __res
       const double ri = f[i] - (q == 0 ? y0 : (q == 1 ? y1 : y2));
       r[i] = ri;
       acc[0] = fma(ri, ri, acc[0]);
+      const double ui = u[i];
+      acc[1] += ui * ui / dinv[i];
     }
   }
-  double tot[1];
-  if (grid_sum_last<1>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
+  double tot[2];
+  if (grid_sum_last<2>(acc, partials, counter, sm, tot) && threadIdx.x == 0) {
     const double rn = sqrt(fabs(tot[0]));
     O->rr = tot[0];
     O->rel = O->norm_b > 1e-300 ? rn / O->norm_b : rn;
     O->scale = rn > 0.0 ? 1.0 / rn : 1.0;
+    O->uD2 = tot[1];
   }
 }
 
@@ -704,7 +710,7 @@ void PcgEngine::launch_residual64(cudaStream_t s, const double* d_f) {
   const AssembledCsr& op = *op_;
   if (use_bsr_)
     k_bsr_residual64<<<bsr_grid_, kSpmvThreads, 0, s>>>(view_of(bsr_), bsr_.val64.ptr, u_.ptr,
-                                                        d_f, r_.ptr, scal_.ptr + 1,
+                                                        d_f, op.dinv.ptr, r_.ptr, scal_.ptr + 1,
                                                         partials_.ptr, counters_.ptr + 3);
   else
     k_residual64<<<spmv_grid_, kSpmvThreads, 0, s>>>(n_, op.row_ptr.ptr, op.col_ind.ptr,
@@ -865,6 +871,13 @@ bool PcgEngine::block_jacobi(bool mixed, cudaStream_t s) {
   return true;
 }
 
+void PcgEngine::ensure_diag32(cudaStream_t s) {
+  if (diag_gen_ == generation_) return;
+  resident_diag(res_, op_->dinv.ptr, n_, num_sms_, s);
+  ++launches_;
+  diag_gen_ = generation_;
+}
+
 void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStream_t s,
                            PcgScalars* host, SolveResult& res) {
   ensure_vectors(false);
@@ -872,13 +885,24 @@ void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStr
   resident_iters_ = 0;
   const bool bj = block_jacobi(false, s);
   if (resident_used(false)) {
+    ResidentCtl ctl;
+    ctl.tol = tol;
+    ctl.max_iters = max_iters;
+    ctl.block_jacobi = bj;
+    ctl.spin_limit = spin_limit_;
+    if (err_target_ > 0.0) {
+      // error-controlled: ||e||_M <= (target / safety) ||u||_M
+      ensure_diag32(s);
+      ctl.err_mode = kErrRelative;
+      ctl.err_rel = err_target_ / kErrSafety;
+    }
     resident_begin(s, bsr_.val64.ptr, static_cast<size_t>(bsr_.steps) * 288 * sizeof(double));
-    resident_solve64(bsr_, res_, d_f, u_.ptr, scal_.ptr, tol, max_iters, s, op_->dinv.ptr, bj);
+    resident_solve64(bsr_, res_, d_f, u_.ptr, scal_.ptr, ctl, s, op_->dinv.ptr);
     resident_end(s);
     ++launches_;
     read_scalars(s, host, 0);
     resident_iters_ += host->iter;
-    if (host->flags & kFlagResidentAbort)
+    if ((host->flags & kFlagResidentAbort) || host->abort)
       throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
     if (host->flags & kFlagNonPosRz)
       throw Error(VSGB_ERR_SINGULAR,
@@ -888,6 +912,12 @@ void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStr
     res.rel = host->rel;
     res.converged = (host->flags & kFlagConverged) != 0;
     res.breakdown = (host->flags & kFlagBreakdown) != 0;
+    if (err_target_ > 0.0) {
+      res.err_est = (host->err2 >= 0.0 && host->total2 > 0.0)
+                        ? std::sqrt(host->err2 / host->total2)
+                        : (host->flags & kFlagZeroRhs ? 0.0 : -1.0);
+      res.err_met = (host->flags & kFlagErrTarget) != 0;
+    }
     return;
   }
   set_limits(s, 0, tol, max_iters);
@@ -947,6 +977,12 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
   res.rel = outer.rel;
   double prev = 0.0;
   bool have_prev = false;
+  // Error-controlled refinement (persistent solve only): the first inner
+  // solve stops on its residual (inner_tol), every later one on the error
+  // estimate of errest.cuh; the loop ends when a step met the error target.
+  const bool err_control = err_target_ > 0.0 && resident;
+  if (err_control) ensure_diag32(s);
+  double prev_uD2 = 0.0, prev_scale = 1.0;
   for (int step = 0; step < max_solves; ++step) {
     // Inexact refinement: the correction only has to bring the true residual
     // (outer.rel, relative to ||f||) below tol, so its inner solve may stop
@@ -962,9 +998,23 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       // The true residual is launched right behind it, and both records come
       // back after one synchronisation (the residual is not used when the
       // inner solve failed).
+      ResidentCtl ctl;
+      ctl.tol = itol;
+      ctl.max_iters = max_iters;
+      ctl.block_jacobi = bj;
+      ctl.spin_limit = spin_limit_;
+      if (err_control && step > 0) {
+        // refinement step: the correction's error must fall below
+        // (target / safety) ||u||_D of the current iterate; the relative
+        // floor keeps an FP32 solve from chasing more than it can deliver
+        // (another refinement step follows instead)
+        ctl.err_mode = kErrAbsolute;
+        ctl.err_target = err_target_ / kErrSafety;
+        ctl.err_rel = kErrRelFloor;
+      }
       resident_begin(s, bsr_.val32.ptr, static_cast<size_t>(bsr_.steps) * 288 * sizeof(float));
-      resident_solve32(bsr_, res_, r_.ptr, u_.ptr, scal_.ptr, scal_.ptr + 1, itol,
-                       max_iters, s, op_->dinv.ptr, bj);
+      resident_solve32(bsr_, res_, r_.ptr, u_.ptr, scal_.ptr, scal_.ptr + 1, ctl, s,
+                       op_->dinv.ptr);
       VSGB_CUDA(cudaEventRecord(rev_[1], s));
       ++launches_;
       launch_residual64(s, d_f);
@@ -981,7 +1031,7 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
         res.rel = 0.0;
         return;
       }
-      if (host->flags & kFlagResidentAbort)
+      if ((host->flags & kFlagResidentAbort) || host->abort)
         throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
       if (host->flags & kFlagNonPosRz)
         throw Error(VSGB_ERR_SINGULAR,
@@ -996,6 +1046,20 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
         return;
       }
       res.rel = outer.rel;
+      if (err_control) {
+        // the step's estimate of its own error, relative to ||u||_D of the
+        // iterate it corrected
+        if (step > 0 && host->err2 >= 0.0 && prev_uD2 > 0.0)
+          res.err_est = std::sqrt(host->err2 / prev_uD2) / prev_scale;
+        prev_uD2 = outer.uD2;
+        prev_scale = outer.scale;
+        if (step > 0 && (host->flags & kFlagErrTarget)) {
+          res.converged = true;
+          res.err_met = true;
+          break;
+        }
+        continue;  // first solve, or the relative floor only: refine again
+      }
       if (outer.rel <= tol) {
         res.converged = true;
         break;
@@ -1134,24 +1198,36 @@ static_assert(sizeof(PcgScalars) <= kNoAllocScalarsBytes, "scalar record");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Device address of g_noalloc_scratch per device (a host-side copy of the
-// symbol is only a stand-in, never a device address).
+// symbol is only a stand-in, never a device address).  The address belongs to
+// the device's primary context as it was when the first call resolved it: a
+// cudaDeviceReset (or anything else that destroys that context) leaves the
+// cached address stale, so after one the library has to be loaded anew
+// (a new process) before this entry point is called again on that device.
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
 struct NoAllocError {
-  int code;  // 0 ok, 2 column out of range, 4 zero diagonal, 5 missing diagonal
+  int code;  // 0 ok, 2 column out of range, 4 zero diagonal, 5 missing diagonal, 6 bad row_ptr
   int index;
 };
 
-// Column range check and Jacobi inverse diagonal of a full-storage CSR
-// (first entry with col == row, as build_jacobi_diagonal).
-__global__ void k_noalloc_diag(int n, const int* __restrict__ rp, const int* __restrict__ ci,
-                               const double* __restrict__ v, double* __restrict__ dinv,
-                               NoAllocError* err) {
+// Row pointer, column range check and Jacobi inverse diagonal of a
+// full-storage CSR (first entry with col == row, as build_jacobi_diagonal).
+// Row r reads only rp[r], rp[r+1] (inside the caller's n+1 entries) until its
+// extent is known to lie in [0, nnz): a bad row pointer is reported before any
+// column or value is read through it.
+__global__ void k_noalloc_diag(int n, int nnz, const int* __restrict__ rp,
+                               const int* __restrict__ ci, const double* __restrict__ v,
+                               double* __restrict__ dinv, NoAllocError* err) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const int b = rp[r], e = rp[r + 1];
+  if (b < 0 || b > e || e > nnz || (r == 0 && b != 0) || (r == n - 1 && e != nnz)) {
+    if (atomicCAS(&err->code, 0, 6) == 0) err->index = r;
+    dinv[r] = 0.0;
+    return;
+  }
   bool found = false;
   for (int k = b; k < e; ++k) {
     const int c = ci[k];
@@ -1264,14 +1340,20 @@ extern "C" int vsgb_pcg_solve_noalloc(int n, int nnz, const int* d_row_ptr, cons
   h.max_iters = max_iters > 0 ? max_iters : 10000;
   if ((e = cudaMemcpyAsync(S, &h, sizeof(PcgScalars), cudaMemcpyHostToDevice, s)) != cudaSuccess)
     return cuda_fail(e, "write limits");
-  k_noalloc_diag<<<grid_for(n, kThreads, 1 << 30), kThreads, 0, s>>>(n, d_row_ptr, d_col_ind,
-                                                                      d_values, dinv, derr);
+  k_noalloc_diag<<<grid_for(n, kThreads, 1 << 30), kThreads, 0, s>>>(n, nnz, d_row_ptr,
+                                                                      d_col_ind, d_values, dinv,
+                                                                      derr);
   NoAllocError herr{};
   if ((e = cudaMemcpyAsync(&herr, derr, sizeof(herr), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
     return cuda_fail(e, "diagonal check");
   if (herr.code == 2) {
     noalloc_err(err, errlen, "column index out of range in row " + std::to_string(herr.index));
+    return VSGB_ERR_INVALID;
+  }
+  if (herr.code == 6) {
+    noalloc_err(err, errlen, "row_ptr is not a valid CSR row pointer (0 = row_ptr[0] <= ... <= "
+                             "row_ptr[n] = nnz) at row " + std::to_string(herr.index));
     return VSGB_ERR_INVALID;
   }
   if (herr.code == 4 || herr.code == 5) {
@@ -1306,12 +1388,22 @@ extern "C" int vsgb_pcg_solve_noalloc(int n, int nnz, const int* d_row_ptr, cons
       return cuda_fail(e, "PCG iteration");
     if (h.flags & kFlagDone) break;
   }
-  if (iterations_out) *iterations_out = h.iter;
+  // A non-positive p*Ap stops the solve as the reference does
+  // (cuda_pcg_backend_impl.hpp:1932-1939): the iteration count reported is
+  // max_iters and the did-not-converge error follows, here with the p*Ap
+  // value and the iteration it was met at appended.
+  const bool breakdown = (h.flags & kFlagBreakdown) != 0;
+  if (iterations_out) *iterations_out = breakdown ? h.max_iters : h.iter;
   if (rel_residual_out) *rel_residual_out = h.rel;
-  if (!(h.flags & kFlagConverged) || h.iter >= h.max_iters) {
-    noalloc_err(err, errlen, "CUDA PCG: did not converge after " + std::to_string(h.max_iters) +
-                                 " iterations (relative residual " + std::to_string(h.rel) +
-                                 " > tolerance " + std::to_string(h.tol) + ")");
+  if (breakdown || !(h.flags & kFlagConverged) || h.iter >= h.max_iters) {
+    std::string m = "CUDA PCG: did not converge after " + std::to_string(h.max_iters) +
+                    " iterations (relative residual " + std::to_string(h.rel) + " > tolerance " +
+                    std::to_string(h.tol) +
+                    "). Consider increasing max iterations or using a direct solver.";
+    if (breakdown)
+      m += " (non-positive p*Ap=" + std::to_string(h.pAp) + " at iteration " +
+           std::to_string(h.iter) + ")";
+    noalloc_err(err, errlen, m);
     return VSGB_ERR_NOT_CONVERGED;
   }
   return VSGB_OK;

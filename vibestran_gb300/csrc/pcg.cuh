@@ -19,7 +19,17 @@ struct SolveResult {
   bool stalled = false;
   bool inner_failed = false;
   double rel = 0.0;
+  double err_est = -1.0;  // error-controlled solve: estimated relative error (< 0: none)
+  bool err_met = false;   // error-controlled solve: the error target was met
 };
+
+// Error-controlled stopping (errest.cuh): a solve aims at target / kErrSafety
+// so that an estimate low by up to that factor still meets the target; a
+// refinement step stops at the relative floor kErrRelFloor of its own
+// correction at the latest (FP32 cannot deliver much more) and the next step
+// continues from the FP64 residual.
+constexpr double kErrSafety = 3.0;
+constexpr double kErrRelFloor = 1e-4;
 
 class PcgEngine {
  public:
@@ -63,6 +73,13 @@ class PcgEngine {
   // 0: scalar Jacobi; 1: 3x3 block Jacobi (persistent solve on the block
   // operator only).
   void set_precond(int p) { precond_ = p; }
+  // Relative displacement error target of error-controlled solves (<= 0:
+  // the reference's residual test).  Persistent solves only.
+  void set_error_target(double e) { err_target_ = e; }
+  double error_target() const { return err_target_; }
+  // Polls of a grid wait of the persistent solve before it gives up and the
+  // solve fails with VSGB_ERR_CUDA (<= 0: the default, ~1 s).
+  void set_spin_limit(long long k) { spin_limit_ = k > 0 ? k : kDefaultSpinLimit; }
   int precond() const { return precond_; }
   bool resident_used(bool mixed) const {
     return resident_ && use_bsr_ && (mixed ? res_.ok32 : res_.ok64);
@@ -95,6 +112,7 @@ class PcgEngine {
   void launch_batch32(cudaStream_t s);
   void iterate(cudaStream_t s, bool fp32, PcgScalars* host);
   bool block_jacobi(bool mixed, cudaStream_t s);  // builds the blocks on first use
+  void ensure_diag32(cudaStream_t s);             // FP32 Jacobi diagonal for the estimate
 
   int num_sms_;
   const AssembledCsr* op_ = nullptr;
@@ -138,6 +156,9 @@ class PcgEngine {
   bool adaptive_inner_ = true;
   int precond_ = 0;
   unsigned bj_gen_ = ~0u;  // operator generation the block inverses belong to
+  unsigned diag_gen_ = ~0u;  // operator generation of res_.diag32
+  double err_target_ = 0.0;
+  long long spin_limit_ = kDefaultSpinLimit;
   bool l2_window_set_ = false;
   size_t l2_persist_max_ = 0;   // device limit (0: not supported)
   size_t l2_window_max_ = 0;

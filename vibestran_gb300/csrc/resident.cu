@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <climits>
 
+#include "errest.cuh"
 #include "kernels.cuh"
 #include "resident.cuh"
 
@@ -29,7 +30,6 @@ namespace {
 
 constexpr int kResThreads = 512;
 constexpr int kResWarps = kResThreads / 32;
-constexpr long long kSpinLimit = 1LL << 22;  // ~1 s of polling, then abort
 constexpr int kFlagAbort = 64;
 
 template <typename T>
@@ -57,6 +57,14 @@ struct ResArgs {
   int max_iters;
   int rows_max;  // own-row stride of the shared-memory vectors
   T* u_glob;     // solution accumulator in global memory (null: in shared memory)
+  long long spin_limit;  // polls of a grid wait before it gives up
+  // error-controlled stop (errest.cuh): p.Mp per iteration with M = the Jacobi
+  // diagonal (diag32) or the 3x3 node blocks (bjd32, upper triangles)
+  int err_mode;          // ErrMode
+  double err_target;     // kErrAbsolute: target relative to ||u||_D of the outer record O
+  double err_rel;        // relative floor (kErrAbsolute) or relative target (kErrRelative)
+  const float* __restrict__ diag32;
+  const float* __restrict__ bjd32;
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -108,7 +116,8 @@ __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
 // wait an acquire load; the CTA barrier after the wait hands the acquired
 // writes to the other threads.  The abort flag is polled every 64 spins and
 // the loop backs off only after the first 4096.
-__device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, int* s_ok) {
+__device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, int* s_ok,
+                          long long spin_limit) {
   target += gridDim.x;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -121,7 +130,7 @@ __device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, in
         ok = 0;
         break;
       }
-      if (spins > kSpinLimit) {
+      if (spins > spin_limit) {
         atomicExch(abort_flag, 1);
         ok = 0;
         break;
@@ -145,7 +154,7 @@ __device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, in
 template <typename A, int NV, typename Fin>
 __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned* count,
                                unsigned& target, int* abort_flag, double* sm, int* s_ok,
-                               Fin&& fin) {
+                               long long spin_limit, Fin&& fin) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
@@ -166,7 +175,7 @@ __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned*
 #pragma unroll
       for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = w[k];
   }
-  const bool ok = grid_sync(count, target, abort_flag, s_ok);
+  const bool ok = grid_sync(count, target, abort_flag, s_ok, spin_limit);
   if (threadIdx.x < 32) {
     // Lane l adds the partials of CTAs l, l+32, ... in that order; the loads
     // of a round are all issued before the first add (one L2 round trip per
@@ -246,7 +255,8 @@ __device__ __forceinline__ int fx_scale(double prev, bool& usable) {
 template <int NV, typename Fin>
 __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], double* partials,
                                   int slot, unsigned long long* fx, int red, int* abort_flag,
-                                  double* sm, int* s_ok, int* s_fb, double* s_tot, Fin&& fin) {
+                                  double* sm, int* s_ok, int* s_fb, double* s_tot,
+                                  long long spin_limit, Fin&& fin) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
@@ -310,7 +320,7 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
           ok = 0;
           break;
         }
-        if (spins > kSpinLimit) {
+        if (spins > spin_limit) {
           atomicExch(abort_flag, 1);
           ok = 0;
           break;
@@ -352,12 +362,14 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
   return ok;
 }
 
-// Per-slice sum slots between the own-row vectors and the window: one per
-// slice of the largest CTA range (rows_max = 24 * max_slices), padded so the
-// window stays 16/32-byte aligned.
-__host__ __device__ __forceinline__ int slot_count(int rows_max) {
+// Per-slice sum slots between the own-row vectors and the window: two per
+// slice of the largest CTA range (rows_max = 24 * max_slices) — p.Ap and, for
+// an error-controlled solve, p.Mp (stored as T) — padded so the window stays
+// 16/32-byte aligned.
+__host__ __device__ __forceinline__ int slot_half(int rows_max) {
   return ((rows_max / 24) + 3) & ~3;
 }
+__host__ __device__ __forceinline__ int slot_count(int rows_max) { return 2 * slot_half(rows_max); }
 
 __device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double rfma(double a, double b, double c) { return fma(a, b, c); }
@@ -434,7 +446,9 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   T* D = AP + a.rows_max;
   T* U = a.u_glob ? a.u_glob + g0 : D + a.rows_max;
   T* SL = D + (a.u_glob ? 1 : 2) * a.rows_max;  // per-slice p.Ap sums (slices are handed out dynamically)
+  T* SLm = SL + slot_half(a.rows_max);           // per-slice p.Mp sums (error-controlled solve)
   T* win = SL + slot_count(a.rows_max);  // 4 per node when kWindow
+  const bool err_on = a.err_mode != kErrOff;
   const int wb = a.cta_win[2 * c], we = a.cta_win[2 * c + 1];
   unsigned target = 0;
   int slot = 0;
@@ -495,17 +509,30 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   __shared__ int s_flags;
   // Recurrence scalars: thread 0 only, in shared memory so that they hold no
   // registers of the other threads across the SpMV.
-  __shared__ double norm_b, rz, rel, pAp, rr, beta, alpha, rr_stop;
+  __shared__ double norm_b, rz, rel, pAp, rr, beta, alpha, rr_stop, pMp;
+  // Error-controlled stop: the Hestenes-Stiefel estimate (errest.cuh) and its
+  // targets, thread 0 only (every CTA computes the same values).
+  __shared__ ErrEst s_err;
+  __shared__ double s_err_t2, s_err_rel2;
   if (tid == 0) {
-    norm_b = rz = pAp = rr = beta = alpha = rr_stop = 0.0;
+    norm_b = rz = pAp = rr = beta = alpha = rr_stop = pMp = 0.0;
     rel = 1.0;
+    err_reset(s_err);
+    s_err_t2 = 0.0;
+    s_err_rel2 = a.err_rel * a.err_rel;
+    if (a.err_mode == kErrAbsolute) {
+      // the inner solve's unknown is scale * (correction of u): its error
+      // target is scale * err_target * ||u||_D of the outer iterate
+      const double t = a.err_target * scale;
+      s_err_t2 = t * t * (kMixed ? a.O->uD2 : 0.0);
+    }
   }
   int flags = 0, it = 0;
   int fx_red = 0;  // fused reductions done (FP32)
   T* p_old = a.p4a;
   T* p_new = a.p4b;
   ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok,
-                            [&](const double (&t)[2], bool good) {
+                            a.spin_limit, [&](const double (&t)[2], bool good) {
                               norm_b = sqrt(fabs(t[0]));
                               rz = t[1];
                               rr = t[0];
@@ -639,6 +666,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       const int r = lane >> 2, q = lane & 3;
       const int R = 8 * sl + r;
       T part = T(0);
+      float pf = 0.f;
       if (q < 3 && R < a.nb) {
         const int lr = 24 * ls + 3 * r + q;
         const T yq = q == 0 ? y0 : (q == 1 ? y1 : y2);
@@ -648,25 +676,57 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         AP[lr] = yq;
         if (!(kWindow && kKeepWindowP)) p_new[4 * R + q] = pn;
         part = pn * yq;
+        pf = static_cast<float>(pn);
+      }
+      // p.Mp for the error estimate, in FP32 (an estimate needs no more):
+      // M = the Jacobi diagonal, or the node's 3x3 diagonal block, whose
+      // three rows sit on lanes 4r..4r+2
+      float partm = 0.f;
+      if (err_on) {
+        if (kBJ) {
+          const int g4 = lane & ~3;
+          const float p0 = __shfl_sync(0xffffffffu, pf, g4);
+          const float p1 = __shfl_sync(0xffffffffu, pf, g4 + 1);
+          const float p2 = __shfl_sync(0xffffffffu, pf, g4 + 2);
+          if (q < 3 && R < a.nb) {
+            const float* bd = a.bjd32 + 6 * static_cast<size_t>(R);
+            const float k0 = __ldg(bd + (q == 0 ? 0 : (q == 1 ? 1 : 2)));
+            const float k1 = __ldg(bd + (q == 0 ? 1 : (q == 1 ? 3 : 4)));
+            const float k2 = __ldg(bd + (q == 0 ? 2 : (q == 1 ? 4 : 5)));
+            partm = pf * fmaf(k0, p0, fmaf(k1, p1, k2 * p2));
+          }
+        } else if (q < 3 && R < a.nb) {
+          partm = pf * pf * __ldg(a.diag32 + 24 * static_cast<size_t>(sl) + 3 * r + q);
+        }
+        partm = warp_sum(partm);
       }
       part = warp_sum(part);
       int nxt = 0;
       if (lane == 0) {
         SL[ls] = part;
+        if (err_on) SLm[ls] = static_cast<T>(partm);
         nxt = atomicAdd(&s_next, 1);
       }
       lq = __shfl_sync(0xffffffffu, nxt, 0);
     }
-    // p.Ap of the CTA in slice order, whichever warp computed each slice.
+    // p.Ap (and p.Mp) of the CTA in slice order, whichever warp computed each slice.
     __syncthreads();
+    T accm = T(0);
     if (warp == 0) {
-      T s = T(0);
-      for (int k = lane; k < ns; k += 32) s += SL[k];
+      T s = T(0), sm = T(0);
+      for (int k = lane; k < ns; k += 32) {
+        s += SL[k];
+        if (err_on) sm += SLm[k];
+      }
       s = warp_sum(s);
-      if (lane == 0) accp[0] = s;
+      if (err_on) sm = warp_sum(sm);
+      if (lane == 0) {
+        accp[0] = s;
+        accm = sm;
+      }
     }
-    auto fin1 = [&](const double (&t)[1], bool good) {
-      pAp = t[0];
+    auto fin1 = [&](double pApv, double pMpv, bool good) {
+      pAp = pApv;
       if (!good) {
         flags |= kFlagDone | kFlagAbort;
       } else if (!(pAp > 0.0)) {
@@ -675,22 +735,43 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         alpha = kFastScalars32 && sizeof(T) == 4
                     ? static_cast<double>(static_cast<float>(rz) / static_cast<float>(pAp))
                     : rz / pAp;
+        if (err_on) {
+          pMp = pMpv;
+          err_record(s_err, rz, pAp, pMp);
+        }
       }
       s_flags = flags;
       s_sc[0] = alpha;
     };
-    if constexpr (sizeof(T) == 4) {
+    auto fin1a = [&](const double (&t)[1], bool good) { fin1(t[0], 0.0, good); };
+    auto fin1b = [&](const double (&t)[2], bool good) { fin1(t[0], t[1], good); };
+    if (err_on) {
+      T accb[2] = {accp[0], accm};
+      if constexpr (sizeof(T) == 4) {
+        if (a.fx) {
+          const double prev[2] = {pAp, pMp};
+          ok = grid_allreduce_fx<2>(accb, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
+                                    red, &s_ok, &s_fb, s_tot, a.spin_limit, fin1b);
+        } else {
+          ok = grid_allreduce<T, 2>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
+                                    &s_ok, a.spin_limit, fin1b);
+        }
+      } else {
+        ok = grid_allreduce<T, 2>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
+                                  &s_ok, a.spin_limit, fin1b);
+      }
+    } else if constexpr (sizeof(T) == 4) {
       if (a.fx) {
         const double prev[1] = {pAp};
         ok = grid_allreduce_fx<1>(accp, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
-                                  red, &s_ok, &s_fb, s_tot, fin1);
+                                  red, &s_ok, &s_fb, s_tot, a.spin_limit, fin1a);
       } else {
         ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
-                                  &s_ok, fin1);
+                                  &s_ok, a.spin_limit, fin1a);
       }
     } else {
       ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
-                                &s_ok, fin1);
+                                &s_ok, a.spin_limit, fin1a);
     }
     slot ^= 1;
     flags = s_flags;
@@ -736,7 +817,21 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       } else {
         rr = t[1];
         bool conv;
-        if (kFastScalars32 && sizeof(T) == 4) {
+        if (err_on) {
+          // Error-controlled: the residual test is not used; the solve stops
+          // when two consecutive blocks' estimates meet the target, or when
+          // the residual is zero to working precision.
+          conv = err_block_end(s_err, s_err_t2, s_err_rel2);
+          bool met = conv && (a.err_mode == kErrRelative ||
+                              (s_err.est2 <= s_err_t2 && s_err.lag2 <= s_err_t2));
+          // residual at working-precision zero: converged (an FP32 refinement
+          // step then leaves the decision to the next step's estimate)
+          if (!(fabs(rr) > (sizeof(T) == 4 ? 1e-20 : 1e-28) * norm_b * norm_b)) {
+            conv = true;
+            met = met || sizeof(T) == 8;
+          }
+          if (met) flags |= kFlagErrTarget;
+        } else if (kFastScalars32 && sizeof(T) == 4) {
           // rel < tol as rr < (tol |b|)^2; rel itself at the exit
           conv = fabs(rr) < rr_stop;
         } else {
@@ -761,14 +856,14 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       if (a.fx) {
         const double prev[2] = {rz, rr};
         ok = grid_allreduce_fx<2>(acc2, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
-                                  red, &s_ok, &s_fb, s_tot, fin2);
+                                  red, &s_ok, &s_fb, s_tot, a.spin_limit, fin2);
       } else {
         ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
-                                  &s_ok, fin2);
+                                  &s_ok, a.spin_limit, fin2);
       }
     } else {
       ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
-                                &s_ok, fin2);
+                                &s_ok, a.spin_limit, fin2);
     }
     slot ^= 1;
     flags = s_flags;
@@ -790,7 +885,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     }
   }
   if (c == 0 && tid == 0) {
-    if (kFastScalars32 && sizeof(T) == 4 && norm_b > 1e-300) rel = sqrt(fabs(rr)) / norm_b;
+    if ((err_on || (kFastScalars32 && sizeof(T) == 4)) && norm_b > 1e-300)
+      rel = sqrt(fabs(rr)) / norm_b;
+    a.S->err2 = s_err.est2 >= 0.0 && s_err.lag2 >= 0.0 ? fmax(s_err.est2, s_err.lag2) : -1.0;
+    a.S->total2 = s_err.total2;
     a.S->iter = it;
     a.S->rel = rel;
     a.S->rr = rr;
@@ -845,7 +943,8 @@ __global__ void k_block_jacobi_inverse(int nb, const int* __restrict__ slice_ptr
                                        const int* __restrict__ rowlen,
                                        const int* __restrict__ cols,
                                        const double* __restrict__ v64, double* __restrict__ bj64,
-                                       float* __restrict__ bj32, int* __restrict__ bad) {
+                                       float* __restrict__ bj32, float* __restrict__ bjd32,
+                                       int* __restrict__ bad) {
   const int R = blockIdx.x * blockDim.x + threadIdx.x;
   if (R >= nb) return;
   const int sl = R >> 3, ln0 = (R & 7) * 4, len = rowlen[R];
@@ -861,6 +960,10 @@ __global__ void k_block_jacobi_inverse(int nb, const int* __restrict__ slice_ptr
   }
   const double a00 = v64[at], a01 = v64[at + 32], a02 = v64[at + 64];
   const double a11 = v64[at + 128], a12 = v64[at + 160], a22 = v64[at + 256];
+  // the block itself (upper triangle): the preconditioner's norm of the error estimate
+  const double blk[6] = {a00, a01, a02, a11, a12, a22};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) bjd32[6 * static_cast<size_t>(R) + k] = static_cast<float>(blk[k]);
   const double c00 = a11 * a22 - a12 * a12;
   const double c01 = a02 * a12 - a01 * a22;
   const double c02 = a01 * a12 - a02 * a11;
@@ -883,7 +986,7 @@ __global__ void k_block_jacobi_inverse(int nb, const int* __restrict__ slice_ptr
 
 template <typename T, bool kWindow, bool kMixed>
 void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const double* rhs,
-                     double* u, PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
+                     double* u, PcgScalars* S, const PcgScalars* O, const ResidentCtl& ctl,
                      T* z4, T* p4a, T* p4b, const double* dinv, const T* bj, size_t smem,
                      T* u_glob, cudaStream_t s) {
   ResArgs<T> a;
@@ -907,15 +1010,26 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   a.fx = (sizeof(T) == 4 && kFusedReductions && P.ctas <= 255) ? P.fx.ptr : nullptr;
   if (a.fx)
     VSGB_CUDA(cudaMemsetAsync(P.fx.ptr, 0, sizeof(unsigned long long) * kFxSlots * kFxWords, s));
-  a.abort_flag = P.abort_flag.ptr;
+  // The abort word lives in the solve's scalar record, which the host reads
+  // back after the launch: a CTA that gave up waiting is seen even when CTA 0
+  // finished normally.
+  a.abort_flag = &S->abort;
   a.S = S;
   a.O = O;
-  a.tol = tol;
-  a.max_iters = max_iters;
+  a.tol = ctl.tol;
+  a.max_iters = ctl.max_iters;
   a.rows_max = 24 * P.max_slices;
   a.u_glob = u_glob;
+  a.spin_limit = ctl.spin_limit > 0 ? ctl.spin_limit : kDefaultSpinLimit;
+  a.err_mode = ctl.err_mode;
+  a.err_target = ctl.err_target;
+  a.err_rel = ctl.err_rel;
+  a.diag32 = P.diag32.ptr;
+  a.bjd32 = P.bjd32.ptr;
+  if (ctl.err_mode != kErrOff && (bj ? !P.bjd32.ptr : !P.diag32.ptr))
+    throw Error(VSGB_ERR_STATE, "error-controlled solve without the preconditioner's diagonal");
   VSGB_CUDA(cudaMemsetAsync(P.barrier.ptr, 0, sizeof(unsigned), s));
-  VSGB_CUDA(cudaMemsetAsync(P.abort_flag.ptr, 0, sizeof(int), s));
+  VSGB_CUDA(cudaMemsetAsync(&S->abort, 0, sizeof(int), s));
   void* args[] = {&a};
   const void* fn = bj ? reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, true>)
                       : reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false>);
@@ -1015,7 +1129,6 @@ void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, Re
   P.partials.reserve(2 * static_cast<size_t>(G) * 2);
   P.fx.reserve(kFxSlots * kFxWords);
   P.barrier.reserve(1);
-  P.abort_flag.reserve(1);
   const size_t rows = 24 * static_cast<size_t>(max_slices);
   const size_t nodes4 = 4 * static_cast<size_t>(nb);
   auto fit = [&](size_t bytes) { return bytes <= static_cast<size_t>(smem_optin); };
@@ -1069,12 +1182,13 @@ int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, cudaSt
   const size_t m = 6 * static_cast<size_t>(B.nb > 0 ? B.nb : 1);
   P.bj64.reserve(m);
   if (need32) P.bj32.reserve(m);
+  P.bjd32.reserve(m);
   P.bj_bad.reserve(1);
   const int big = INT_MAX;
   VSGB_CUDA(cudaMemcpyAsync(P.bj_bad.ptr, &big, sizeof(int), cudaMemcpyHostToDevice, s));
   k_block_jacobi_inverse<<<(B.nb + 255) / 256, 256, 0, s>>>(
       B.nb, B.slice_ptr.ptr, B.rowlen.ptr, B.cols.ptr, B.val64.ptr, P.bj64.ptr,
-      need32 ? P.bj32.ptr : nullptr, P.bj_bad.ptr);
+      need32 ? P.bj32.ptr : nullptr, P.bjd32.ptr, P.bj_bad.ptr);
   VSGB_LAUNCH_CHECK();
   int bad = big;
   VSGB_CUDA(cudaMemcpyAsync(&bad, P.bj_bad.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1083,34 +1197,42 @@ int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, cudaSt
 }
 
 void resident_solve32(const BsrSell& B, ResidentPlan& P, const double* r64, double* u64,
-                      PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
-                      cudaStream_t s, const double* dinv, bool block_jacobi) {
+                      PcgScalars* S, const PcgScalars* O, const ResidentCtl& ctl, cudaStream_t s,
+                      const double* dinv) {
   float* ug = P.ug32 ? P.u32g.ptr : nullptr;
-  const float* bj = block_jacobi ? P.bj32.ptr : nullptr;
+  const float* bj = ctl.block_jacobi ? P.bj32.ptr : nullptr;
   if (P.win32)
-    launch_resident<float, true, true>(B, P, B.val32.ptr, r64, u64, S, O, tol, max_iters,
-                                       P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, bj, P.smem32, ug,
-                                       s);
+    launch_resident<float, true, true>(B, P, B.val32.ptr, r64, u64, S, O, ctl, P.z4f.ptr,
+                                       P.p4fa.ptr, P.p4fb.ptr, dinv, bj, P.smem32, ug, s);
   else
-    launch_resident<float, false, true>(B, P, B.val32.ptr, r64, u64, S, O, tol, max_iters,
-                                        P.z4f.ptr, P.p4fa.ptr, P.p4fb.ptr, dinv, bj, P.smem32,
-                                        ug, s);
+    launch_resident<float, false, true>(B, P, B.val32.ptr, r64, u64, S, O, ctl, P.z4f.ptr,
+                                        P.p4fa.ptr, P.p4fb.ptr, dinv, bj, P.smem32, ug, s);
 }
 
 void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double* u,
-                      PcgScalars* S, double tol, int max_iters, cudaStream_t s,
-                      const double* dinv, bool block_jacobi) {
+                      PcgScalars* S, const ResidentCtl& ctl, cudaStream_t s,
+                      const double* dinv) {
   // the FP64 solve accumulates straight into its output when u is global
   double* ug = P.ug64 ? u : nullptr;
-  const double* bj = block_jacobi ? P.bj64.ptr : nullptr;
+  const double* bj = ctl.block_jacobi ? P.bj64.ptr : nullptr;
   if (P.win64)
-    launch_resident<double, true, false>(B, P, B.val64.ptr, f, u, S, nullptr, tol, max_iters,
-                                         P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, bj, P.smem64,
-                                         ug, s);
+    launch_resident<double, true, false>(B, P, B.val64.ptr, f, u, S, nullptr, ctl, P.z4d.ptr,
+                                         P.p4da.ptr, P.p4db.ptr, dinv, bj, P.smem64, ug, s);
   else
-    launch_resident<double, false, false>(B, P, B.val64.ptr, f, u, S, nullptr, tol, max_iters,
-                                          P.z4d.ptr, P.p4da.ptr, P.p4db.ptr, dinv, bj, P.smem64,
-                                          ug, s);
+    launch_resident<double, false, false>(B, P, B.val64.ptr, f, u, S, nullptr, ctl, P.z4d.ptr,
+                                          P.p4da.ptr, P.p4db.ptr, dinv, bj, P.smem64, ug, s);
+}
+
+// diag32 = 1 / dinv (the Jacobi diagonal, FP32) for the error estimate.
+__global__ void k_recip_f32(int n, const double* __restrict__ dinv, float* __restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    d[i] = static_cast<float>(1.0 / dinv[i]);
+}
+
+void resident_diag(ResidentPlan& P, const double* dinv, int n, int num_sms, cudaStream_t s) {
+  P.diag32.reserve(static_cast<size_t>(n > 0 ? n : 1));
+  k_recip_f32<<<num_sms * 4, 256, 0, s>>>(n, dinv, P.diag32.ptr);
+  VSGB_LAUNCH_CHECK();
 }
 
 }  // namespace vsgb

@@ -7,6 +7,7 @@
 
 #include "bsr.cuh"
 #include "common.cuh"
+#include "errest.cuh"
 
 namespace vsgb {
 
@@ -23,7 +24,6 @@ struct ResidentPlan {
   DevBuf<double> partials;          // 2 barrier slots x ctas x up to 4 values
   DevBuf<unsigned> barrier;         // monotonic arrival counter
   DevBuf<unsigned long long> fx;    // FP32 solve: fused reduction words
-  DevBuf<int> abort_flag;           // set by a barrier that gave up waiting
   DevBuf<float> u32g;                       // FP32 solution accumulator when ug32
   DevBuf<float> z4f, p4fa, p4fb;    // node-padded FP32 vectors (4 per node)
   DevBuf<double> z4d, p4da, p4db;   // node-padded FP64 vectors
@@ -31,7 +31,23 @@ struct ResidentPlan {
   // (xx, xy, xz, yy, yz, zz), FP64 and its FP32 copy for the inner solve
   DevBuf<double> bj64;
   DevBuf<float> bj32;
+  DevBuf<float> bjd32;              // the diagonal blocks themselves (upper triangle, FP32)
   DevBuf<int> bj_bad;               // smallest node whose block is not SPD
+  DevBuf<float> diag32;             // Jacobi diagonal (FP32) for the error estimate
+};
+
+// Polls of a grid wait of the persistent solve before it gives up (~1 s).
+constexpr long long kDefaultSpinLimit = 1LL << 22;
+
+// Stopping and wait controls of one persistent solve.
+struct ResidentCtl {
+  double tol = 0.0;          // residual tolerance (err_mode == kErrOff)
+  int max_iters = 0;
+  int err_mode = 0;          // ErrMode (errest.cuh)
+  double err_target = 0.0;   // kErrAbsolute: target relative to ||u||_D of the outer record
+  double err_rel = 0.0;      // relative floor (kErrAbsolute) or relative target (kErrRelative)
+  long long spin_limit = kDefaultSpinLimit;
+  bool block_jacobi = false; // 3x3 block Jacobi instead of the scalar one
 };
 
 // Plans CTA ranges / windows and allocates the padded vectors; leaves both
@@ -45,16 +61,20 @@ void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, Re
 int resident_block_jacobi(const BsrSell& B, ResidentPlan& P, bool need32, cudaStream_t s);
 
 // One FP32 inner solve: rhs = (float)(r64 * O->scale); on convergence
-// u64 += delta / O->scale.  Final counts/flags land in *S.  block_jacobi
-// selects the 3x3 block preconditioner in P.bj32 instead of dinv.
+// u64 += delta / O->scale.  Final counts/flags land in *S (S->abort set when
+// any CTA's grid wait gave up).  ctl.block_jacobi selects the 3x3 block
+// preconditioner in P.bj32 instead of dinv.
 void resident_solve32(const BsrSell& B, ResidentPlan& P, const double* r64, double* u64,
-                      PcgScalars* S, const PcgScalars* O, double tol, int max_iters,
-                      cudaStream_t s, const double* dinv, bool block_jacobi = false);
+                      PcgScalars* S, const PcgScalars* O, const ResidentCtl& ctl, cudaStream_t s,
+                      const double* dinv);
 
 // One FP64 solve of K u = f; u written (zeros on a zero RHS).
 void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double* u,
-                      PcgScalars* S, double tol, int max_iters, cudaStream_t s,
-                      const double* dinv, bool block_jacobi = false);
+                      PcgScalars* S, const ResidentCtl& ctl, cudaStream_t s,
+                      const double* dinv);
+
+// P.diag32 = 1 / dinv (needed by error-controlled solves with scalar Jacobi).
+void resident_diag(ResidentPlan& P, const double* dinv, int n, int num_sms, cudaStream_t s);
 
 // Flag set in PcgScalars::flags when a grid barrier gave up waiting.
 constexpr int kFlagResidentAbort = 64;
