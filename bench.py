@@ -425,6 +425,11 @@ def profile_case(which):
         asm.upload_rhs(F)
         st = asm.solve_resident()
         print(f"inner solve: {st.kernel_iterations:.0f} iterations, {st.kernel_ms:.3f} ms")
+    if which == "solve64":
+        _fp64_error_controlled(B, be)
+        asm.upload_rhs(F)
+        st = asm.solve_resident()
+        print(f"FP64 solve: {st.kernel_iterations:.0f} iterations, {st.kernel_ms:.3f} ms")
 
 
 def cpu_reference(model, eq6, n, F, steps, warmup, threads):
@@ -511,12 +516,13 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 16-load-case, adjoint and jittered-mesh measurements")
-    ap.add_argument("--profile", choices=["assemble", "solve", "multi"], default=None,
+    ap.add_argument("--profile", choices=["assemble", "solve", "solve64", "multi"], default=None,
                     help="run one small case of a hot kernel for a profiler and exit "
                          "(no JSON line): assemble = 3 x element stiffness + block assembly "
                          "of cantilever_84k; solve = one FP32 inner solve (persistent "
-                         "kernel) of cantilever_84k; multi = 48 batched iterations of the "
-                         "16-load-case block")
+                         "kernel) of cantilever_84k; solve64 = one FP64 persistent solve of "
+                         "cantilever_84k (error target 1e-6); multi = 48 batched iterations "
+                         "of the 16-load-case block")
     a = ap.parse_args()
     if a.profile:
         profile_case(a.profile)
@@ -621,6 +627,18 @@ def main():
     be.set_option(B.OPT_PRECOND, B.PRECOND_JACOBI)
     _fp64_error_controlled(B, be)
 
+    # Phase split of the persistent iterations (global-timer marks by thread 0
+    # of every CTA, outside the timed region): FP32 inner solves of the mixed
+    # solve, then the FP64 solve.
+    be.set_option(B.OPT_PHASE_TRACE, 1)
+    _mixed_defaults(B, be)
+    asm.solve_resident()
+    split32 = B.phase_times(be)
+    _fp64_error_controlled(B, be)
+    asm.solve_resident()
+    split64 = B.phase_times(be)
+    be.set_option(B.OPT_PHASE_TRACE, 0)
+
     # Launch-path block SpMVs (not in the step) for comparison.
     spmv_ms, spmv_bytes = B.time_spmv(be, B.MIXED, 200)
     spmv64_ms, spmv64_bytes = B.time_spmv(be, B.FP64, 200)
@@ -705,7 +723,8 @@ def main():
                  # SpMV's 2 nnz_full FLOPs per iteration at GB300's FP64 rate
                  "us_per_iteration": fp64_us_it,
                  "fp64_pipe_floor_us": fp64_floor_us,
-                 "fp64_pipe_frac": fp64_floor_us / fp64_us_it if fp64_us_it > 0 else None},
+                 "fp64_pipe_frac": fp64_floor_us / fp64_us_it if fp64_us_it > 0 else None,
+                 "phase_split_us": split64},
         "speedup_mixed_vs_fp64_solve": statistics.median(fp64_solve) / statistics.median(mixed_solve),
         # The FP32 block operator (94 MB) stays in the 126 MB L2 across the
         # iterations of one launch, so DRAM carries ~1 % of the algorithmic
@@ -722,6 +741,11 @@ def main():
                      "dram_over_algorithmic": (
                          _traffic_per_iteration("k_resident_pcg_f32") / res_bytes_it
                          if _traffic_per_iteration("k_resident_pcg_f32") else None),
+                     "phase_split_us": split32,
+                     "reduction_share": ((split32["reduction1_us"] + split32["reduction2_us"]) /
+                                         max(sum(split32[k] for k in ("gather_us", "spmv_us",
+                                             "reduction1_us", "update_us", "reduction2_us")),
+                                             1e-12)),
                      "algorithmic_bytes": res_it * res_bytes_it / max(res_launches, 1),
                      "avg_launch_us": 1e3 * res_ms / max(res_launches, 1),
                      "iterations_per_launch": res_it / max(res_launches, 1),

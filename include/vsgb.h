@@ -103,6 +103,11 @@ extern "C" {
                                      it gives up and the solve returns VSGB_ERR_CUDA
                                      ("a grid barrier ... timed out"); <= 0: the default
                                      (2^22, about a second).  For tests of that path. */
+#define VSGB_OPT_PHASE_TRACE 16   /* 1: time the phases of every iteration of the
+                                     persistent solve (thread 0 of each CTA reads the
+                                     global timer at the phase boundaries; a few
+                                     instructions per iteration); read with
+                                     vsgb_phase_times.  Default 0. */
 
 #define VSGB_PRECOND_JACOBI 0
 #define VSGB_PRECOND_BLOCK_JACOBI 1
@@ -318,6 +323,13 @@ int vsgb_timer_stop(vsgb_ctx* ctx, double* ms);
 int vsgb_time_spmv(vsgb_ctx* ctx, int precision, int reps, double* avg_ms, double* bytes);
 /* Number of kernels this context launched since creation. */
 long long vsgb_kernel_launches(vsgb_ctx* ctx);
+/* With VSGB_OPT_PHASE_TRACE on: the last solve's persistent launches split
+ * into phases, per iteration and averaged over the CTAs (us): out7[0] gather
+ * of the x window, [1] block SpMV (+ the own-row p update and p.Ap), [2] the
+ * first grid reduction (p.Ap), [3] the u / r / z update, [4] the second grid
+ * reduction (r.z, r.r), [5] the slowest CTA's SpMV, [6] iterations timed.
+ * No reference counterpart (a measurement helper). */
+int vsgb_phase_times(vsgb_ctx* ctx, double* out7);
 
 /* Per-load-case outcome of the last solve (k < nrhs): PCG iterations
  * (mixed: summed over inner solves), relative residual, converged flag and

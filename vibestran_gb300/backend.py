@@ -59,6 +59,7 @@ OPT_ADAPTIVE_INNER = 12
 OPT_PRECOND = 13
 OPT_ERROR_TARGET = 14
 OPT_SPIN_LIMIT = 15
+OPT_PHASE_TRACE = 16
 
 PRECOND_JACOBI = 0
 PRECOND_BLOCK_JACOBI = 1
@@ -74,7 +75,8 @@ EXPORTS = (
     "vsgb_assemble_resident", "vsgb_rhs_upload", "vsgb_solve_resident",
     "vsgb_host_alloc", "vsgb_host_free",
     "vsgb_solution_download", "vsgb_element_sensitivity", "vsgb_timer_start",
-    "vsgb_timer_stop", "vsgb_time_spmv", "vsgb_kernel_launches", "vsgb_pcg_solve_noalloc",
+    "vsgb_timer_stop", "vsgb_time_spmv", "vsgb_kernel_launches", "vsgb_phase_times",
+    "vsgb_pcg_solve_noalloc",
 )
 NOALLOC_MAX_N = 65536  # VSGB_NOALLOC_MAX_N
 
@@ -160,6 +162,7 @@ def load_library(build_if_missing: bool = False):
     L.vsgb_time_spmv.argtypes = [vp, c_int, c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)]
     L.vsgb_kernel_launches.argtypes = [vp]
     L.vsgb_kernel_launches.restype = c_ll
+    L.vsgb_phase_times.argtypes = [vp, _f64p]
     L.vsgb_adjoint_gradients.argtypes = [vp, _f64p, vp, vp, vp, vp, vp, ctypes.POINTER(VsgbStats)]
     L.vsgb_solid_stress.argtypes = [vp, vp, c_int, _f64p, vp, ctypes.POINTER(c_dbl)]
     L.vsgb_bdf_read.argtypes = [cp, c_int, ctypes.POINTER(vp), cp, sz]
@@ -524,6 +527,15 @@ def timer_stop(backend) -> float:
     ms = ctypes.c_double()
     backend.context.check(load_library().vsgb_timer_stop(backend.context.ptr, ctypes.byref(ms)))
     return ms.value
+
+
+def phase_times(backend) -> dict:
+    """Per-iteration phase split of the last persistent solve (us, mean over
+    CTAs) when OPT_PHASE_TRACE is on."""
+    t = np.zeros(7)
+    backend.context.check(load_library().vsgb_phase_times(backend.context.ptr, t))
+    return {"gather_us": t[0], "spmv_us": t[1], "reduction1_us": t[2], "update_us": t[3],
+            "reduction2_us": t[4], "spmv_slowest_cta_us": t[5], "iterations": int(t[6])}
 
 
 def time_spmv(backend, precision: int, reps: int = 50):

@@ -458,6 +458,9 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
       case VSGB_OPT_SPIN_LIMIT:
         c->eng->set_spin_limit(static_cast<long long>(value));
         break;
+      case VSGB_OPT_PHASE_TRACE:
+        c->eng->set_phase_trace(value != 0.0);
+        break;
       default:
         throw Error(VSGB_ERR_INVALID, "unknown option " + std::to_string(option));
     }
@@ -851,6 +854,13 @@ int vsgb_time_spmv(vsgb_ctx* c, int precision, int reps, double* avg_ms, double*
 }
 
 long long vsgb_kernel_launches(vsgb_ctx* c) { return c ? c->eng->launches() : -1; }
+
+int vsgb_phase_times(vsgb_ctx* c, double* out7) {
+  if (!c || !out7) return VSGB_ERR_INVALID;
+  const double* t = c->eng->phase_times();
+  for (int k = 0; k < 7; ++k) out7[k] = t[k];
+  return VSGB_OK;
+}
 
 int vsgb_rhs_stats(vsgb_ctx* c, int k, int* iterations, double* rel_residual, int* converged,
                    int* batched) {

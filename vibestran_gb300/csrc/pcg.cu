@@ -871,6 +871,25 @@ bool PcgEngine::block_jacobi(bool mixed, cudaStream_t s) {
   return true;
 }
 
+void PcgEngine::trace_reset() {
+  for (double& v : phase_ns_) v = 0.0;
+  for (double& v : phase_us_) v = 0.0;
+  phase_its_ = 0;
+}
+
+void PcgEngine::trace_add(cudaStream_t s) {
+  if (!trace_) return;
+  double sums[5], mx = 0.0;
+  long long its = 0;
+  resident_trace(res_, s, sums, &mx, &its);
+  for (int k = 0; k < 5; ++k) phase_ns_[k] += sums[k];
+  phase_ns_[5] += mx;
+  phase_its_ += its;
+  const double d = phase_its_ > 0 ? 1e3 * static_cast<double>(phase_its_) : 1.0;
+  for (int k = 0; k < 6; ++k) phase_us_[k] = phase_ns_[k] / d;
+  phase_us_[6] = static_cast<double>(phase_its_);
+}
+
 void PcgEngine::ensure_diag32(cudaStream_t s) {
   if (diag_gen_ == generation_) return;
   resident_diag(res_, op_->dinv.ptr, n_, num_sms_, s);
@@ -890,6 +909,8 @@ void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStr
     ctl.max_iters = max_iters;
     ctl.block_jacobi = bj;
     ctl.spin_limit = spin_limit_;
+    ctl.trace = trace_;
+    trace_reset();
     if (err_target_ > 0.0) {
       // error-controlled: ||e||_M <= (target / safety) ||u||_M
       ensure_diag32(s);
@@ -902,6 +923,7 @@ void PcgEngine::solve_fp64(const double* d_f, double tol, int max_iters, cudaStr
     ++launches_;
     read_scalars(s, host, 0);
     resident_iters_ += host->iter;
+    trace_add(s);
     if ((host->flags & kFlagResidentAbort) || host->abort)
       throw Error(VSGB_ERR_CUDA, "GB300 PCG: a grid barrier of the persistent solve timed out");
     if (host->flags & kFlagNonPosRz)
@@ -982,6 +1004,7 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
   // estimate of errest.cuh; the loop ends when a step met the error target.
   const bool err_control = err_target_ > 0.0 && resident;
   if (err_control) ensure_diag32(s);
+  trace_reset();
   double prev_uD2 = 0.0, prev_scale = 1.0;
   for (int step = 0; step < max_solves; ++step) {
     // Inexact refinement: the correction only has to bring the true residual
@@ -1003,6 +1026,7 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       ctl.max_iters = max_iters;
       ctl.block_jacobi = bj;
       ctl.spin_limit = spin_limit_;
+      ctl.trace = trace_;
       if (err_control && step > 0) {
         // refinement step: the correction's error must fall below
         // (target / safety) ||u||_D of the current iterate; the relative
@@ -1026,6 +1050,7 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       resident_finish(s);
       outer = host[1];
       resident_iters_ += host->iter;
+      trace_add(s);
       if (step == 0 && (host->flags & kFlagZeroRhs)) {  // f = 0: u stays 0
         res.converged = true;
         res.rel = 0.0;

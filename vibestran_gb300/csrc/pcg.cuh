@@ -80,6 +80,12 @@ class PcgEngine {
   // Polls of a grid wait of the persistent solve before it gives up and the
   // solve fails with VSGB_ERR_CUDA (<= 0: the default, ~1 s).
   void set_spin_limit(long long k) { spin_limit_ = k > 0 ? k : kDefaultSpinLimit; }
+  // Time the phases of every persistent-solve iteration (globaltimer, thread
+  // 0 of each CTA); phase_times() then holds the last solve's per-iteration
+  // means over CTAs: gather, SpMV, first reduction, update, second
+  // reduction (us), the slowest CTA's SpMV (us) and the iterations.
+  void set_phase_trace(bool on) { trace_ = on; }
+  const double* phase_times() const { return phase_us_; }
   int precond() const { return precond_; }
   bool resident_used(bool mixed) const {
     return resident_ && use_bsr_ && (mixed ? res_.ok32 : res_.ok64);
@@ -159,6 +165,12 @@ class PcgEngine {
   unsigned diag_gen_ = ~0u;  // operator generation of res_.diag32
   double err_target_ = 0.0;
   long long spin_limit_ = kDefaultSpinLimit;
+  bool trace_ = false;
+  double phase_ns_[6] = {0, 0, 0, 0, 0, 0};  // sums over the traced launches
+  long long phase_its_ = 0;
+  double phase_us_[7] = {0, 0, 0, 0, 0, 0, 0};
+  void trace_reset();
+  void trace_add(cudaStream_t s);  // after a traced persistent launch completed
   bool l2_window_set_ = false;
   size_t l2_persist_max_ = 0;   // device limit (0: not supported)
   size_t l2_window_max_ = 0;

@@ -65,7 +65,17 @@ struct ResArgs {
   double err_rel;        // relative floor (kErrAbsolute) or relative target (kErrRelative)
   const float* __restrict__ diag32;
   const float* __restrict__ bjd32;
+  // phase timer (null: off): per CTA, nanoseconds summed over the iterations
+  // of gather, SpMV, first reduction, update, second reduction, then the
+  // iteration count (kTraceWords per CTA)
+  unsigned long long* trace;
 };
+
+__device__ __forceinline__ unsigned long long gtime() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
@@ -551,8 +561,19 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   slot ^= 1;
   flags = s_flags;
 
+  // phase timer, thread 0 only
+  const bool tr = a.trace != nullptr && tid == 0;
+  unsigned long long tsum[5] = {0ull, 0ull, 0ull, 0ull, 0ull}, tmark = 0ull;
+  auto tick = [&](int k) {
+    if (tr) {
+      const unsigned long long t = gtime();
+      if (k >= 0) tsum[k] += t - tmark;
+      tmark = t;
+    }
+  };
   while (!(flags & kFlagDone)) {
     // ── phase 1: x = z + beta p over the window, Ap = K x, own p update ──
+    tick(-1);
     const T tb = static_cast<T>(s_sc[1]);
     if (tid == 0) s_next = kResWarps;
     if (!kWindow) __syncthreads();
@@ -586,6 +607,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       }
       __syncthreads();
     }
+    tick(0);
     T accp[1] = {T(0)};
     // Slices are handed out dynamically (first one per warp statically), so
     // warps that drew short slices take more and the phase ends together.
@@ -711,6 +733,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     }
     // p.Ap (and p.Mp) of the CTA in slice order, whichever warp computed each slice.
     __syncthreads();
+    tick(1);
     T accm = T(0);
     if (warp == 0) {
       T s = T(0), sm = T(0);
@@ -775,6 +798,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     }
     slot ^= 1;
     flags = s_flags;
+    tick(2);
     if (flags & kFlagDone) break;
     const T ta = static_cast<T>(s_sc[0]);
     // ── phase 2: u, r, z updates on the own rows ──
@@ -811,6 +835,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       acc2[1] = rfma(rv, rv, acc2[1]);
     }
     ++it;
+    tick(3);
     auto fin2 = [&](const double (&t)[2], bool good) {
       if (!good) {
         flags |= kFlagDone | kFlagAbort;
@@ -867,12 +892,18 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     }
     slot ^= 1;
     flags = s_flags;
+    tick(4);
     if (flags & kFlagAbort) break;
     T* t = p_old;
     p_old = p_new;
     p_new = t;
   }
 
+  if (tr) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) a.trace[kTraceWords * c + k] = tsum[k];
+    a.trace[kTraceWords * c + 5] = static_cast<unsigned long long>(it);
+  }
   // ── results ──
   if (!(flags & kFlagAbort)) {
     const double inv_scale = kMixed ? 1.0 / scale : 1.0;
@@ -1026,6 +1057,11 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   a.err_rel = ctl.err_rel;
   a.diag32 = P.diag32.ptr;
   a.bjd32 = P.bjd32.ptr;
+  a.trace = nullptr;
+  if (ctl.trace) {
+    P.trace.reserve(static_cast<size_t>(kTraceWords) * P.ctas);
+    a.trace = P.trace.ptr;
+  }
   if (ctl.err_mode != kErrOff && (bj ? !P.bjd32.ptr : !P.diag32.ptr))
     throw Error(VSGB_ERR_STATE, "error-controlled solve without the preconditioner's diagonal");
   VSGB_CUDA(cudaMemsetAsync(P.barrier.ptr, 0, sizeof(unsigned), s));
@@ -1227,6 +1263,23 @@ void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double
 __global__ void k_recip_f32(int n, const double* __restrict__ dinv, float* __restrict__ d) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     d[i] = static_cast<float>(1.0 / dinv[i]);
+}
+
+void resident_trace(const ResidentPlan& P, cudaStream_t s, double* sums_ns, double* max_spmv_ns,
+                    long long* iterations) {
+  std::vector<unsigned long long> h(static_cast<size_t>(kTraceWords) * P.ctas);
+  VSGB_CUDA(cudaMemcpyAsync(h.data(), P.trace.ptr, sizeof(unsigned long long) * h.size(),
+                            cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  for (int k = 0; k < 5; ++k) sums_ns[k] = 0.0;
+  *max_spmv_ns = 0.0;
+  *iterations = 0;
+  for (int c = 0; c < P.ctas; ++c) {
+    const unsigned long long* t = h.data() + static_cast<size_t>(kTraceWords) * c;
+    for (int k = 0; k < 5; ++k) sums_ns[k] += static_cast<double>(t[k]) / P.ctas;
+    *max_spmv_ns = std::max(*max_spmv_ns, static_cast<double>(t[1]));
+    *iterations = static_cast<long long>(t[5]);
+  }
 }
 
 void resident_diag(ResidentPlan& P, const double* dinv, int n, int num_sms, cudaStream_t s) {

@@ -34,7 +34,10 @@ struct ResidentPlan {
   DevBuf<float> bjd32;              // the diagonal blocks themselves (upper triangle, FP32)
   DevBuf<int> bj_bad;               // smallest node whose block is not SPD
   DevBuf<float> diag32;             // Jacobi diagonal (FP32) for the error estimate
+  DevBuf<unsigned long long> trace; // phase timer, kTraceWords per CTA
 };
+
+constexpr int kTraceWords = 6;
 
 // Polls of a grid wait of the persistent solve before it gives up (~1 s).
 constexpr long long kDefaultSpinLimit = 1LL << 22;
@@ -48,6 +51,7 @@ struct ResidentCtl {
   double err_rel = 0.0;      // relative floor (kErrAbsolute) or relative target (kErrRelative)
   long long spin_limit = kDefaultSpinLimit;
   bool block_jacobi = false; // 3x3 block Jacobi instead of the scalar one
+  bool trace = false;        // time the phases of every iteration (P.trace)
 };
 
 // Plans CTA ranges / windows and allocates the padded vectors; leaves both
@@ -72,6 +76,12 @@ void resident_solve32(const BsrSell& B, ResidentPlan& P, const double* r64, doub
 void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double* u,
                       PcgScalars* S, const ResidentCtl& ctl, cudaStream_t s,
                       const double* dinv);
+
+// Phase times of the last traced launch: sums over its iterations, averaged
+// over the CTAs (gather, SpMV, first reduction, update, second reduction, in
+// ns), the largest CTA's SpMV sum and the iteration count.
+void resident_trace(const ResidentPlan& P, cudaStream_t s, double* sums_ns, double* max_spmv_ns,
+                    long long* iterations);
 
 // P.diag32 = 1 / dinv (needed by error-controlled solves with scalar Jacobi).
 void resident_diag(ResidentPlan& P, const double* dinv, int n, int num_sms, cudaStream_t s);
