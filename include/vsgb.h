@@ -324,12 +324,14 @@ int vsgb_time_spmv(vsgb_ctx* ctx, int precision, int reps, double* avg_ms, doubl
 /* Number of kernels this context launched since creation. */
 long long vsgb_kernel_launches(vsgb_ctx* ctx);
 /* With VSGB_OPT_PHASE_TRACE on: the last solve's persistent launches split
- * into phases, per iteration and averaged over the CTAs (us): out7[0] gather
- * of the x window, [1] block SpMV (+ the own-row p update and p.Ap), [2] the
- * first grid reduction (p.Ap), [3] the u / r / z update, [4] the second grid
- * reduction (r.z, r.r), [5] the slowest CTA's SpMV, [6] iterations timed.
- * No reference counterpart (a measurement helper). */
-int vsgb_phase_times(vsgb_ctx* ctx, double* out7);
+ * into phases, per iteration and averaged over the CTAs (us): out11[0] gather
+ * of the x window, [1] block SpMV (+ the own-row p update and p.Ap); the
+ * first grid reduction (p.Ap) as [2] the CTA's own sums up to its arrival,
+ * [3] the wait for the other CTAs, [4] the grid total and the recurrence;
+ * [5] the u / r / z update; the second grid reduction (r.z, r.r) as [6], [7],
+ * [8]; [9] the slowest CTA's SpMV; [10] iterations timed.  No reference
+ * counterpart (a measurement helper). */
+int vsgb_phase_times(vsgb_ctx* ctx, double* out11);
 
 /* Per-load-case outcome of the last solve (k < nrhs): PCG iterations
  * (mixed: summed over inner solves), relative residual, converged flag and

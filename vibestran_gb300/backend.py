@@ -532,10 +532,14 @@ def timer_stop(backend) -> float:
 def phase_times(backend) -> dict:
     """Per-iteration phase split of the last persistent solve (us, mean over
     CTAs) when OPT_PHASE_TRACE is on."""
-    t = np.zeros(7)
+    t = np.zeros(11)
     backend.context.check(load_library().vsgb_phase_times(backend.context.ptr, t))
-    return {"gather_us": t[0], "spmv_us": t[1], "reduction1_us": t[2], "update_us": t[3],
-            "reduction2_us": t[4], "spmv_slowest_cta_us": t[5], "iterations": int(t[6])}
+    return {"gather_us": t[0], "spmv_us": t[1],
+            "reduction1_us": t[2] + t[3] + t[4], "reduction1_cta_us": t[2],
+            "reduction1_wait_us": t[3], "reduction1_total_us": t[4], "update_us": t[5],
+            "reduction2_us": t[6] + t[7] + t[8], "reduction2_cta_us": t[6],
+            "reduction2_wait_us": t[7], "reduction2_total_us": t[8],
+            "spmv_slowest_cta_us": t[9], "iterations": int(t[10])}
 
 
 def time_spmv(backend, precision: int, reps: int = 50):

@@ -855,10 +855,10 @@ int vsgb_time_spmv(vsgb_ctx* c, int precision, int reps, double* avg_ms, double*
 
 long long vsgb_kernel_launches(vsgb_ctx* c) { return c ? c->eng->launches() : -1; }
 
-int vsgb_phase_times(vsgb_ctx* c, double* out7) {
-  if (!c || !out7) return VSGB_ERR_INVALID;
+int vsgb_phase_times(vsgb_ctx* c, double* out11) {
+  if (!c || !out11) return VSGB_ERR_INVALID;
   const double* t = c->eng->phase_times();
-  for (int k = 0; k < 7; ++k) out7[k] = t[k];
+  for (int k = 0; k < vsgb::kTracePhases + 2; ++k) out11[k] = t[k];
   return VSGB_OK;
 }
 

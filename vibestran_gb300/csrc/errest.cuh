@@ -76,11 +76,13 @@ __host__ __device__ inline void err_reset(ErrEst& e) {
   e.pass_prev = 0;
 }
 
-// One iteration's coefficients; pAp > 0 (the caller stops on a breakdown).
-__device__ inline void err_record(ErrEst& e, double gamma, double pAp, double pMp) {
+// One iteration's coefficients a = alpha gamma and c = p.Mp / p.Ap (the
+// caller forms them from the recurrence it already has, without a division
+// of its own on the critical path).
+__device__ inline void err_record(ErrEst& e, double a, double c) {
   if (e.n < kErrBlock) {
-    e.a[e.n] = gamma * gamma / pAp;  // alpha gamma with alpha = gamma / pAp
-    e.c[e.n] = pMp / pAp;
+    e.a[e.n] = a;
+    e.c[e.n] = c;
     ++e.n;
   }
 }

@@ -378,7 +378,7 @@ k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restr
           S->iters[k] = S->iter;
         } else {
           S->alpha[k] = S->rz[k] / pAp;
-          if (err_on) err_record(est[k], S->rz[k], pAp, s_tot[kP + k]);
+          if (err_on) err_record(est[k], S->rz[k] * S->alpha[k], s_tot[kP + k] / pAp);
         }
         S->flags[k] = f;
       } else {

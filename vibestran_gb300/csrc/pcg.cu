@@ -879,15 +879,15 @@ void PcgEngine::trace_reset() {
 
 void PcgEngine::trace_add(cudaStream_t s) {
   if (!trace_) return;
-  double sums[5], mx = 0.0;
+  double sums[kTracePhases], mx = 0.0;
   long long its = 0;
   resident_trace(res_, s, sums, &mx, &its);
-  for (int k = 0; k < 5; ++k) phase_ns_[k] += sums[k];
-  phase_ns_[5] += mx;
+  for (int k = 0; k < kTracePhases; ++k) phase_ns_[k] += sums[k];
+  phase_ns_[kTracePhases] += mx;
   phase_its_ += its;
   const double d = phase_its_ > 0 ? 1e3 * static_cast<double>(phase_its_) : 1.0;
-  for (int k = 0; k < 6; ++k) phase_us_[k] = phase_ns_[k] / d;
-  phase_us_[6] = static_cast<double>(phase_its_);
+  for (int k = 0; k <= kTracePhases; ++k) phase_us_[k] = phase_ns_[k] / d;
+  phase_us_[kTracePhases + 1] = static_cast<double>(phase_its_);
 }
 
 void PcgEngine::ensure_diag32(cudaStream_t s) {

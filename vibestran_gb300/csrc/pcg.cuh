@@ -82,8 +82,9 @@ class PcgEngine {
   void set_spin_limit(long long k) { spin_limit_ = k > 0 ? k : kDefaultSpinLimit; }
   // Time the phases of every persistent-solve iteration (globaltimer, thread
   // 0 of each CTA); phase_times() then holds the last solve's per-iteration
-  // means over CTAs: gather, SpMV, first reduction, update, second
-  // reduction (us), the slowest CTA's SpMV (us) and the iterations.
+  // means over CTAs (us): gather, SpMV, first reduction (CTA sums, wait for
+  // the other CTAs, total and recurrence), update, second reduction (same
+  // parts), then the slowest CTA's SpMV (us) and the iterations.
   void set_phase_trace(bool on) { trace_ = on; }
   const double* phase_times() const { return phase_us_; }
   int precond() const { return precond_; }
@@ -166,9 +167,9 @@ class PcgEngine {
   double err_target_ = 0.0;
   long long spin_limit_ = kDefaultSpinLimit;
   bool trace_ = false;
-  double phase_ns_[6] = {0, 0, 0, 0, 0, 0};  // sums over the traced launches
+  double phase_ns_[kTracePhases + 1] = {};  // sums over the traced launches (+ slowest SpMV)
   long long phase_its_ = 0;
-  double phase_us_[7] = {0, 0, 0, 0, 0, 0, 0};
+  double phase_us_[kTracePhases + 2] = {};
   void trace_reset();
   void trace_add(cudaStream_t s);  // after a traced persistent launch completed
   bool l2_window_set_ = false;

@@ -66,8 +66,9 @@ struct ResArgs {
   const float* __restrict__ diag32;
   const float* __restrict__ bjd32;
   // phase timer (null: off): per CTA, nanoseconds summed over the iterations
-  // of gather, SpMV, first reduction, update, second reduction, then the
-  // iteration count (kTraceWords per CTA)
+  // of gather, SpMV, first reduction (CTA sums, wait for the other CTAs,
+  // total and recurrence), update, second reduction (same three parts), then
+  // the iteration count (kTraceWords per CTA)
   unsigned long long* trace;
 };
 
@@ -75,6 +76,36 @@ __device__ __forceinline__ unsigned long long gtime() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
+}
+
+// Phase-timer marks of thread 0 inside a grid reduction: [0] its arrival
+// (partial published), [1] the release (all CTAs arrived); [2] != 0 while the
+// kernel's trace is on.  Thread 0 writes and reads them.
+__device__ __forceinline__ unsigned long long* tmarks() {
+  __shared__ unsigned long long m[3];
+  return m;
+}
+
+// 1/b and a/b in FP64 without the division instruction sequence, whose long
+// dependent chain sits on the critical path of every grid reduction (thread
+// 0, GB300's FP64 pipe).  Newton-Raphson from the correctly rounded FP32
+// reciprocal: y <- y + y (1 - b y) twice takes the seed's ~2^-24 relative
+// error below FP64 rounding; the quotient gets Markstein's residual
+// correction q <- q + y (a - b q), which leaves it within an ulp of the
+// correctly rounded a / b.  Outside the FP32 exponent range of b the division
+// is used.
+__device__ __forceinline__ double rcp_nr2(double b) {
+  const double ab = fabs(b);
+  if (!(ab > 1e-30 && ab < 1e30)) return 1.0 / b;
+  double y = static_cast<double>(__frcp_rn(static_cast<float>(b)));
+  y = fma(y, fma(-b, y, 1.0), y);
+  return fma(y, fma(-b, y, 1.0), y);
+}
+__device__ __forceinline__ double div_nr(double a, double b, double y /* rcp_nr2(b) */) {
+  const double ab = fabs(b);
+  if (!(ab > 1e-30 && ab < 1e30)) return a / b;
+  const double q = a * y;
+  return fma(y, fma(-b, q, a), q);
 }
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -127,11 +158,13 @@ __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
 // writes to the other threads.  The abort flag is polled every 64 spins and
 // the loop backs off only after the first 4096.
 __device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, int* s_ok,
-                          long long spin_limit) {
+                          long long spin_limit, bool sync_first = true) {
   target += gridDim.x;
-  __syncthreads();
+  if (sync_first) __syncthreads();
   if (threadIdx.x == 0) {
     red_release_add_u32(count, 1u);
+    unsigned long long* tm = tmarks();
+    if (tm[2]) tm[0] = gtime();
     int ok = 1;
     long long spins = 0;
     while (ld_acquire_u32(count) < target) {
@@ -147,6 +180,7 @@ __device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, in
       }
       if (spins > 4096) __nanosleep(64);
     }
+    if (tm[2]) tm[1] = gtime();
     *s_ok = ok;
   }
   __syncthreads();
@@ -161,31 +195,46 @@ __device__ bool grid_sync(unsigned* count, unsigned& target, int* abort_flag, in
 // in the FP32 solve: GB300 runs FP64 at 1/58 of the FP32 rate), then the
 // kResWarps warp sums (a fixed shuffle tree in warp 0) and the CTA partials
 // are added in FP64.
-template <typename A, int NV, typename Fin>
+// kW: the warps 0..kW-1 hold per-thread partials (the others hold none and
+// skip the warp sums: on GB300 every warp-wide FP64 add costs the SM's FP64
+// pipe ~17 cycles whatever the lanes); kW = 0: thread 0 already holds the
+// CTA totals, so there is neither a CTA tree nor a CTA barrier before the
+// arrival (the caller's last CTA barrier orders the CTA's writes).
+template <typename A, int NV, int kW = kResWarps, typename Fin>
 __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned* count,
                                unsigned& target, int* abort_flag, double* sm, int* s_ok,
                                long long spin_limit, Fin&& fin) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (kW > 0) {
+    if (wid < kW) {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
-  if (lane == 0)
+      for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+      if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < NV; ++k) sm[wid * NV + k] = static_cast<double>(v[k]);
-  __syncthreads();
+        for (int k = 0; k < NV; ++k) sm[wid * NV + k] = static_cast<double>(v[k]);
+    }
+    __syncthreads();
+  }
   double* part = partials + static_cast<size_t>(slot) * gridDim.x * NV;
   if (wid == 0) {
     double w[NV];
+    if (kW > 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) w[k] = lane < kResWarps ? sm[lane * NV + k] : 0.0;
+      for (int k = 0; k < NV; ++k) w[k] = lane < kW ? sm[lane * NV + k] : 0.0;
 #pragma unroll
-    for (int o = kResWarps / 2; o > 0; o >>= 1)
+      for (int o = 16; o > 0; o >>= 1)
+        if (o < kW)
 #pragma unroll
-      for (int k = 0; k < NV; ++k) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
+          for (int k = 0; k < NV; ++k) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) w[k] = static_cast<double>(v[k]);
+    }
     if (lane == 0)
 #pragma unroll
       for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = w[k];
   }
-  const bool ok = grid_sync(count, target, abort_flag, s_ok, spin_limit);
+  const bool ok = grid_sync(count, target, abort_flag, s_ok, spin_limit, kW > 0);
   if (threadIdx.x < 32) {
     // Lane l adds the partials of CTAs l, l+32, ... in that order; the loads
     // of a round are all issued before the first add (one L2 round trip per
@@ -262,29 +311,40 @@ __device__ __forceinline__ int fx_scale(double prev, bool& usable) {
 // (ring slot red % kFxSlots of kFxWords words, NV of them used): prev[k] > 0 is the previous total
 // of value k (<= 0: none, fall back).  CTA 0 clears the slot two reductions
 // ahead (its last readers all arrived at the reduction before this one).
-template <int NV, typename Fin>
+// kW as in grid_allreduce.
+template <int NV, int kW = kResWarps, typename Fin>
 __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], double* partials,
                                   int slot, unsigned long long* fx, int red, int* abort_flag,
                                   double* sm, int* s_ok, int* s_fb, double* s_tot,
                                   long long spin_limit, Fin&& fin) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (kW > 0) {
+    if (wid < kW) {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
-  if (lane == 0)
+      for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+      if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < NV; ++k) sm[wid * NV + k] = static_cast<double>(v[k]);
-  __syncthreads();
+        for (int k = 0; k < NV; ++k) sm[wid * NV + k] = static_cast<double>(v[k]);
+    }
+    __syncthreads();
+  }
   double* part = partials + static_cast<size_t>(slot) * gridDim.x * NV;
   static_assert(NV <= kFxWords, "a fused reduction sums at most kFxWords values");
   unsigned long long* words = fx + static_cast<size_t>(red % kFxSlots) * kFxWords;
   if (wid == 0) {
     double w[NV];
+    if (kW > 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) w[k] = lane < kResWarps ? sm[lane * NV + k] : 0.0;
+      for (int k = 0; k < NV; ++k) w[k] = lane < kW ? sm[lane * NV + k] : 0.0;
 #pragma unroll
-    for (int o = kResWarps / 2; o > 0; o >>= 1)
+      for (int o = 16; o > 0; o >>= 1)
+        if (o < kW)
 #pragma unroll
-      for (int k = 0; k < NV; ++k) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
+          for (int k = 0; k < NV; ++k) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) w[k] = static_cast<double>(v[k]);
+    }
     if (lane == 0) {
 #pragma unroll
       for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = w[k];
@@ -314,6 +374,8 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
         red_release_add_u64(words + k, add);
       }
       // wait for every arrival on every word
+      unsigned long long* tm = tmarks();
+      if (tm[2]) tm[0] = gtime();
       int ok = 1;
       long long spins = 0;
       unsigned long long got[NV];
@@ -338,6 +400,7 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
         if (spins > 4096) __nanosleep(64);
       }
       fence_acq_rel_gpu();
+      if (tm[2]) tm[1] = gtime();
       int fb = fx_ok ? 0 : 1;
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
@@ -377,7 +440,8 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
 // an error-controlled solve, p.Mp (stored as T) — padded so the window stays
 // 16/32-byte aligned.
 __host__ __device__ __forceinline__ int slot_half(int rows_max) {
-  return ((rows_max / 24) + 3) & ~3;
+  const int s = ((rows_max / 24) + 3) & ~3;
+  return s > kResWarps ? s : kResWarps;  // per-warp sums of the FP64 solve
 }
 __host__ __device__ __forceinline__ int slot_count(int rows_max) { return 2 * slot_half(rows_max); }
 
@@ -459,6 +523,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   T* SLm = SL + slot_half(a.rows_max);           // per-slice p.Mp sums (error-controlled solve)
   T* win = SL + slot_count(a.rows_max);  // 4 per node when kWindow
   const bool err_on = a.err_mode != kErrOff;
+  // Phase 2 (u, r, z and the r.z, r.r partials): all warps in the FP32
+  // solve; in the FP64 solve kP2Warps of them, which keep the FP64 pipe as
+  // busy (the phase is bound by it) and leave a quarter of the warp sums for
+  // the reduction.
+  constexpr int kP2Warps = sizeof(T) == 8 ? 4 : kResWarps;
+  constexpr int kP2Threads = 32 * kP2Warps;
   const int wb = a.cta_win[2 * c], we = a.cta_win[2 * c + 1];
   unsigned target = 0;
   int slot = 0;
@@ -527,6 +597,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   if (tid == 0) {
     norm_b = rz = pAp = rr = beta = alpha = rr_stop = pMp = 0.0;
     rel = 1.0;
+    tmarks()[2] = a.trace != nullptr ? 1ull : 0ull;
     err_reset(s_err);
     s_err_t2 = 0.0;
     s_err_rel2 = a.err_rel * a.err_rel;
@@ -561,13 +632,29 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   slot ^= 1;
   flags = s_flags;
 
-  // phase timer, thread 0 only
+  // phase timer, thread 0 only: tick(k) closes phase k; a reduction's time
+  // is split at its arrival and release marks
   const bool tr = a.trace != nullptr && tid == 0;
-  unsigned long long tsum[5] = {0ull, 0ull, 0ull, 0ull, 0ull}, tmark = 0ull;
+  __shared__ unsigned long long tsum[kTracePhases];  // thread 0's sums (no registers held)
+  __shared__ unsigned long long tmark;
+  if (tid == 0) {
+    tmarks()[2] = tr ? 1ull : 0ull;
+    for (int k = 0; k < kTracePhases; ++k) tsum[k] = 0ull;
+    tmark = 0ull;
+  }
   auto tick = [&](int k) {
     if (tr) {
       const unsigned long long t = gtime();
       if (k >= 0) tsum[k] += t - tmark;
+      tmark = t;
+    }
+  };
+  auto tick_red = [&](int k) {  // closes a reduction: phases k, k+1, k+2
+    if (tr) {
+      const unsigned long long t = gtime(), *m = tmarks();
+      tsum[k] += m[0] - tmark;
+      tsum[k + 1] += m[1] - m[0];
+      tsum[k + 2] += t - m[1];
       tmark = t;
     }
   };
@@ -609,8 +696,17 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     }
     tick(0);
     T accp[1] = {T(0)};
-    // Slices are handed out dynamically (first one per warp statically), so
-    // warps that drew short slices take more and the phase ends together.
+    // FP32: slices are handed out dynamically (first one per warp
+    // statically), so warps that drew short slices take more and the phase
+    // ends together; the p.Ap of each slice is then stored by slice, so the
+    // CTA sum is in slice order whichever warp computed it.  FP64: the SpMV
+    // is bound by the FP64 pipe, where the per-slice warp sum (5 FP64 adds of
+    // the whole warp) is a tenth of the slice's work; the slices go to the
+    // warps round-robin instead and each lane accumulates its p.Ap across
+    // them, one warp sum per warp at the end (fixed order either way).
+    constexpr bool kStatic = sizeof(T) == 8;
+    T part_acc = T(0);
+    float partm_acc = 0.f;
     for (int lq = warp; lq < ns;) {
       // kSnake: odd iterations walk the CTA's slices backwards, so the lines
       // touched last (most likely still in L2) are read first
@@ -720,7 +816,13 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         } else if (q < 3 && R < a.nb) {
           partm = pf * pf * __ldg(a.diag32 + 24 * static_cast<size_t>(sl) + 3 * r + q);
         }
-        partm = warp_sum(partm);
+        if (!kStatic) partm = warp_sum(partm);
+      }
+      if (kStatic) {
+        part_acc += part;
+        partm_acc += partm;
+        lq += kResWarps;
+        continue;
       }
       part = warp_sum(part);
       int nxt = 0;
@@ -731,13 +833,23 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       }
       lq = __shfl_sync(0xffffffffu, nxt, 0);
     }
-    // p.Ap (and p.Mp) of the CTA in slice order, whichever warp computed each slice.
+    if (kStatic) {
+      part_acc = warp_sum(part_acc);
+      if (err_on) partm_acc = warp_sum(partm_acc);
+      if (lane == 0) {
+        SL[warp] = part_acc;
+        if (err_on) SLm[warp] = static_cast<T>(partm_acc);
+      }
+    }
+    // p.Ap (and p.Mp) of the CTA in slice order (FP64: in warp order),
+    // whichever warp computed each slice.
     __syncthreads();
     tick(1);
     T accm = T(0);
     if (warp == 0) {
       T s = T(0), sm = T(0);
-      for (int k = lane; k < ns; k += 32) {
+      const int nsum = kStatic ? kResWarps : ns;
+      for (int k = lane; k < nsum; k += 32) {
         s += SL[k];
         if (err_on) sm += SLm[k];
       }
@@ -755,12 +867,17 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       } else if (!(pAp > 0.0)) {
         flags |= kFlagDone | kFlagBreakdown;
       } else {
-        alpha = kFastScalars32 && sizeof(T) == 4
-                    ? static_cast<double>(static_cast<float>(rz) / static_cast<float>(pAp))
-                    : rz / pAp;
+        double rp;  // 1 / pAp
+        if (kFastScalars32 && sizeof(T) == 4) {
+          alpha = static_cast<double>(static_cast<float>(rz) / static_cast<float>(pAp));
+          rp = static_cast<double>(__frcp_rn(static_cast<float>(pAp)));
+        } else {
+          rp = rcp_nr2(pAp);
+          alpha = div_nr(rz, pAp, rp);
+        }
         if (err_on) {
           pMp = pMpv;
-          err_record(s_err, rz, pAp, pMp);
+          err_record(s_err, rz * alpha, pMp * rp);
         }
       }
       s_flags = flags;
@@ -773,38 +890,38 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       if constexpr (sizeof(T) == 4) {
         if (a.fx) {
           const double prev[2] = {pAp, pMp};
-          ok = grid_allreduce_fx<2>(accb, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
+          ok = grid_allreduce_fx<2, 0>(accb, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
                                     red, &s_ok, &s_fb, s_tot, a.spin_limit, fin1b);
         } else {
-          ok = grid_allreduce<T, 2>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
+          ok = grid_allreduce<T, 2, 0>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
                                     &s_ok, a.spin_limit, fin1b);
         }
       } else {
-        ok = grid_allreduce<T, 2>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
+        ok = grid_allreduce<T, 2, 0>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
                                   &s_ok, a.spin_limit, fin1b);
       }
     } else if constexpr (sizeof(T) == 4) {
       if (a.fx) {
         const double prev[1] = {pAp};
-        ok = grid_allreduce_fx<1>(accp, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
+        ok = grid_allreduce_fx<1, 0>(accp, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
                                   red, &s_ok, &s_fb, s_tot, a.spin_limit, fin1a);
       } else {
-        ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
+        ok = grid_allreduce<T, 1, 0>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
                                   &s_ok, a.spin_limit, fin1a);
       }
     } else {
-      ok = grid_allreduce<T, 1>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
+      ok = grid_allreduce<T, 1, 0>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
                                 &s_ok, a.spin_limit, fin1a);
     }
     slot ^= 1;
     flags = s_flags;
-    tick(2);
+    tick_red(2);
     if (flags & kFlagDone) break;
     const T ta = static_cast<T>(s_sc[0]);
     // ── phase 2: u, r, z updates on the own rows ──
     acc2[0] = acc2[1] = T(0);
     if (kBJ) {
-      for (int ln = tid; 3 * ln < nrows; ln += kResThreads) {
+      for (int ln = tid; tid < kP2Threads && 3 * ln < nrows; ln += kP2Threads) {
         const int lr = 3 * ln, R = 8 * s0 + ln;
         T rv[3], zv[3];
 #pragma unroll
@@ -823,7 +940,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         st3(a.z4 + 4 * static_cast<size_t>(R), zv[0], zv[1], zv[2]);
       }
     }
-    for (int lr = tid; !kBJ && lr < nrows; lr += kResThreads) {
+    for (int lr = tid; !kBJ && tid < kP2Threads && lr < nrows; lr += kP2Threads) {
       const int g = g0 + lr;
       const int R = g / 3, q = g - 3 * R;
       U[lr] = rfma(ta, P[lr], U[lr]);
@@ -835,7 +952,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       acc2[1] = rfma(rv, rv, acc2[1]);
     }
     ++it;
-    tick(3);
+    tick(5);
     auto fin2 = [&](const double (&t)[2], bool good) {
       if (!good) {
         flags |= kFlagDone | kFlagAbort;
@@ -856,12 +973,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
             met = met || sizeof(T) == 8;
           }
           if (met) flags |= kFlagErrTarget;
-        } else if (kFastScalars32 && sizeof(T) == 4) {
-          // rel < tol as rr < (tol |b|)^2; rel itself at the exit
-          conv = fabs(rr) < rr_stop;
         } else {
-          rel = sqrt(fabs(rr)) / norm_b;
-          conv = rel < a.tol;
+          // rel < tol as rr < (tol |b|)^2 (no square root or division on the
+          // critical path); rel itself at the exit
+          conv = fabs(rr) < rr_stop;
         }
         if (conv) {
           flags |= kFlagDone | kFlagConverged;
@@ -869,7 +984,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         } else {
           beta = kFastScalars32 && sizeof(T) == 4
                      ? static_cast<double>(static_cast<float>(t[0]) / static_cast<float>(rz))
-                     : t[0] / rz;
+                     : div_nr(t[0], rz, rcp_nr2(rz));
           if (it >= a.max_iters) flags |= kFlagDone | kFlagMaxIters;
         }
         rz = t[0];
@@ -887,12 +1002,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
                                   &s_ok, a.spin_limit, fin2);
       }
     } else {
-      ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
-                                &s_ok, a.spin_limit, fin2);
+      ok = grid_allreduce<T, 2, kP2Warps>(acc2, a.partials, slot, a.count, target, a.abort_flag,
+                                          red, &s_ok, a.spin_limit, fin2);
     }
     slot ^= 1;
     flags = s_flags;
-    tick(4);
+    tick_red(6);
     if (flags & kFlagAbort) break;
     T* t = p_old;
     p_old = p_new;
@@ -900,9 +1015,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   }
 
   if (tr) {
-#pragma unroll
-    for (int k = 0; k < 5; ++k) a.trace[kTraceWords * c + k] = tsum[k];
-    a.trace[kTraceWords * c + 5] = static_cast<unsigned long long>(it);
+    for (int k = 0; k < kTracePhases; ++k) a.trace[kTraceWords * c + k] = tsum[k];
+    a.trace[kTraceWords * c + kTracePhases] = static_cast<unsigned long long>(it);
   }
   // ── results ──
   if (!(flags & kFlagAbort)) {
@@ -916,8 +1030,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     }
   }
   if (c == 0 && tid == 0) {
-    if ((err_on || (kFastScalars32 && sizeof(T) == 4)) && norm_b > 1e-300)
-      rel = sqrt(fabs(rr)) / norm_b;
+    if (norm_b > 1e-300) rel = sqrt(fabs(rr)) / norm_b;
     a.S->err2 = s_err.est2 >= 0.0 && s_err.lag2 >= 0.0 ? fmax(s_err.est2, s_err.lag2) : -1.0;
     a.S->total2 = s_err.total2;
     a.S->iter = it;
@@ -1271,14 +1384,14 @@ void resident_trace(const ResidentPlan& P, cudaStream_t s, double* sums_ns, doub
   VSGB_CUDA(cudaMemcpyAsync(h.data(), P.trace.ptr, sizeof(unsigned long long) * h.size(),
                             cudaMemcpyDeviceToHost, s));
   VSGB_CUDA(cudaStreamSynchronize(s));
-  for (int k = 0; k < 5; ++k) sums_ns[k] = 0.0;
+  for (int k = 0; k < kTracePhases; ++k) sums_ns[k] = 0.0;
   *max_spmv_ns = 0.0;
   *iterations = 0;
   for (int c = 0; c < P.ctas; ++c) {
     const unsigned long long* t = h.data() + static_cast<size_t>(kTraceWords) * c;
-    for (int k = 0; k < 5; ++k) sums_ns[k] += static_cast<double>(t[k]) / P.ctas;
+    for (int k = 0; k < kTracePhases; ++k) sums_ns[k] += static_cast<double>(t[k]) / P.ctas;
     *max_spmv_ns = std::max(*max_spmv_ns, static_cast<double>(t[1]));
-    *iterations = static_cast<long long>(t[5]);
+    *iterations = static_cast<long long>(t[kTracePhases]);
   }
 }
 

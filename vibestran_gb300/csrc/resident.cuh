@@ -37,7 +37,8 @@ struct ResidentPlan {
   DevBuf<unsigned long long> trace; // phase timer, kTraceWords per CTA
 };
 
-constexpr int kTraceWords = 6;
+constexpr int kTracePhases = 9;  // gather, SpMV, 3 x reduction 1, update, 3 x reduction 2
+constexpr int kTraceWords = 10;  // the phases and the iteration count
 
 // Polls of a grid wait of the persistent solve before it gives up (~1 s).
 constexpr long long kDefaultSpinLimit = 1LL << 22;
@@ -78,8 +79,9 @@ void resident_solve64(const BsrSell& B, ResidentPlan& P, const double* f, double
                       const double* dinv);
 
 // Phase times of the last traced launch: sums over its iterations, averaged
-// over the CTAs (gather, SpMV, first reduction, update, second reduction, in
-// ns), the largest CTA's SpMV sum and the iteration count.
+// over the CTAs (kTracePhases values in ns: gather, SpMV, first reduction as
+// CTA sums / wait for the other CTAs / total and recurrence, update, second
+// reduction likewise), the largest CTA's SpMV sum and the iteration count.
 void resident_trace(const ResidentPlan& P, cudaStream_t s, double* sums_ns, double* max_spmv_ns,
                     long long* iterations);
 
