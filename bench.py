@@ -192,9 +192,10 @@ def extra_multi_rhs(B, C, device):
     out = {"workload": "block_160k_16rhs", "elements": m.n_elem, "dofs": n, "rhs": 16,
            "seed": m.seed, "error_target": ERROR_TARGET,
            "reference": "converged FP64 PCG fingerprints (tests/golden/block_160k_16rhs_ref.json)"}
-    for mode, flag in (("batched", 2), ("sequential", 0)):
+    for mode, flag, tiles in (("batched", 2, 1), ("batched_untiled", 2, 0), ("sequential", 0, 1)):
         be.set_option(B.OPT_BATCHED, flag)
-        asm.solve_resident()  # warm-up (graph capture, buffers)
+        be.set_option(B.OPT_BATCH_TILES, tiles)
+        asm.solve_resident()  # warm-up (graph capture, buffers, tile size)
         B.timer_start(be)
         st = asm.solve_resident()
         ms = B.timer_stop(be)
@@ -205,6 +206,9 @@ def extra_multi_rhs(B, C, device):
         out[mode] = {"solve_s": ms / 1e3, "iterations_max": max(its),
                      "iterations_sum": int(sum(its)), "rel_residual_max": st.rel_residual,
                      "est_rel_error_max": st.est_rel_error, "max_rel_err": max(errs)}
+        if flag == 2:
+            out[mode]["tile_rows"] = st.batch_tile_rows
+    be.set_option(B.OPT_BATCH_TILES, 1)
     out["speedup_batched_vs_sequential"] = out["sequential"]["solve_s"] / out["batched"]["solve_s"]
     # FP64 batched at the same error target
     _fp64_error_controlled(B, be)
@@ -523,9 +527,21 @@ def main():
                          "kernel) of cantilever_84k; solve64 = one FP64 persistent solve of "
                          "cantilever_84k (error target 1e-6); multi = 48 batched iterations "
                          "of the 16-load-case block")
+    ap.add_argument("--extra", choices=["multi_rhs", "adjoint", "stress", "bdf"], default=None,
+                    help="run one of the additional workloads alone, print its JSON and exit")
     a = ap.parse_args()
     if a.profile:
         profile_case(a.profile)
+        return
+    if a.extra:
+        from vibestran_gb300 import backend as B
+        from vibestran_gb300 import cantilever as C
+        B.load_library(build_if_missing=True)
+        fn = {"multi_rhs": lambda: extra_multi_rhs(B, C, 0),
+              "adjoint": lambda: extra_adjoint(B, C, 0),
+              "stress": lambda: extra_stress(B, C, 0),
+              "bdf": lambda: extra_bdf(B, C)}[a.extra]
+        print(json.dumps(fn()))
         return
 
     from vibestran_gb300 import cantilever as C

@@ -54,7 +54,8 @@ extern "C" {
 #define VSGB_OPT_PRECISION 3      /* VSGB_FP64 or VSGB_MIXED */
 #define VSGB_OPT_INNER_TOL 4      /* mixed: inner FP32 tolerance (<=0: 1e-3 when error-controlled,
                                      otherwise clamp(100*tol,1e-4,1e-2) as cuda-pcg-mixed) */
-#define VSGB_OPT_MAX_SOLVES 5     /* mixed: max inner solves (default 3 = 1 + 2 corrections) */
+#define VSGB_OPT_MAX_SOLVES 5     /* mixed: max inner solves (<= 0: default, 3 = 1 + 2
+                                     corrections; 5 when error-controlled) */
 #define VSGB_OPT_CHECK_EVERY 6    /* iterations launched between host convergence checks */
 #define VSGB_OPT_USE_GRAPH 7      /* 1: replay iteration batches as CUDA graphs (default 1) */
 #define VSGB_OPT_FORMAT 8         /* 0 auto, 1 scalar CSR, 2 3x3 node blocks */
@@ -108,6 +109,15 @@ extern "C" {
                                      global timer at the phase boundaries; a few
                                      instructions per iteration); read with
                                      vsgb_phase_times.  Default 0. */
+#define VSGB_OPT_BATCH_TILES 17   /* batched mixed solve on the uploaded mesh: each FP32
+                                     inner solve of up to 16 load cases as one persistent
+                                     launch over spatially compact tiles of block rows
+                                     (recursive coordinate bisection of the node
+                                     coordinates) whose neighbour nodes are staged in
+                                     shared memory.  0 (default): off, one launch per
+                                     kernel (measured faster on GB300); 1: tile size timed
+                                     on the first solve of a sparsity pattern; 8..65536:
+                                     fixed rows per tile. */
 
 #define VSGB_PRECOND_JACOBI 0
 #define VSGB_PRECOND_BLOCK_JACOBI 1
@@ -131,6 +141,8 @@ typedef struct vsgb_stats {
   double kernel_iterations; /* PCG iterations those launches ran */
   double est_rel_error;  /* error-controlled solve: estimated relative displacement
                             error (max over load cases); -1 when not estimated */
+  int batch_tile_rows;   /* batched solve: rows per tile of the persistent tiled
+                            FP32 solve (0: one launch per kernel, or not batched) */
 } vsgb_stats;
 
 /* Create a context on `device` (cuda-pcg uses device 0,

@@ -1,0 +1,180 @@
+"""Tiled batched FP32 solve (mres.cu): every inner solve of up to 16 load
+cases as one persistent launch over Morton-ordered tiles of block rows, the
+tile's neighbour nodes staged in shared memory as z + beta p.
+
+It runs the same per-case recurrence and stopping tests as the
+launch-per-kernel batched path (linear_static.cpp:212-275 solves the cases
+one after another; each case here keeps its own alpha, beta and test), so
+each case must meet the same bars: error-controlled defaults within 1e-6 of
+the sparse-direct answer, the residual test to its tolerance, a fixed tile
+size bitwise reproducible, and re-assembled values (same sparsity pattern)
+giving what a fresh build gives.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N_CASES = 20  # one batch of 16 and one of 4
+
+
+@pytest.fixture(scope="module")
+def tile_model(vsgb, oracle):
+    from vibestran_gb300 import cantilever as C
+    # 41 x 17 x 17 nodes (n = 34 680): 2..8 tiles per CTA give 4 tile sizes
+    m = C.small_block(40, 16, 16, 0.05, seed=11, jitter=0.1, hetero=True)
+    m.loads = C.face_random_loads(m, N_CASES, np.random.default_rng(3))
+    eq6, n = vsgb.build_dof_map(m)
+    F = np.stack([vsgb.apply_forces(m, eq6, n, k) for k in range(N_CASES)], axis=1)
+    eq_o, n_o = oracle.dof_map(m)
+    K = oracle.assemble_chexa8(m, eq_o, n_o)
+    U = oracle.sparse_direct_solve(K, F)
+    return m, eq6, n, F, U
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def _backend(vsgb, tiles, tol=0.0):
+    be = vsgb.Gb300MixedPcgSolverBackend.try_create(tol, 20000)
+    be.set_option(vsgb.OPT_BATCHED, 2)
+    be.set_option(vsgb.OPT_BATCH_TILES, tiles)
+    return be
+
+
+def test_tiled_defaults_match_direct_and_untiled(vsgb, tile_model):
+    m, eq6, n, F, U = tile_model
+    be = _backend(vsgb, 1)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    Ut = asm.solve(F)
+    rows = be.last_stats.batch_tile_rows
+    assert rows >= 8 and rows % 8 == 0
+    its_t = [be.rhs_stats(k)["iterations"] for k in range(N_CASES)]
+    for k in range(N_CASES):
+        s = be.rhs_stats(k)
+        assert s["batched"] and s["converged"], (k, s)
+        assert _rel(Ut[:, k], U[:, k]) <= 1e-6, k
+    assert 0.0 <= be.last_stats.est_rel_error <= 6.7e-7
+    # the autotuned size is kept for the pattern: a second solve reuses it
+    # and is bitwise identical
+    assert np.array_equal(asm.solve(F), Ut)
+    assert be.last_stats.batch_tile_rows == rows
+    # launch-per-kernel path: same bars, iteration counts close
+    be.set_option(vsgb.OPT_BATCH_TILES, 0)
+    Uk = asm.solve(F)
+    assert be.last_stats.batch_tile_rows == 0
+    for k in range(N_CASES):
+        assert _rel(Uk[:, k], U[:, k]) <= 1e-6, k
+        ik = be.rhs_stats(k)["iterations"]
+        assert abs(ik - its_t[k]) <= max(16, ik // 10), (k, ik, its_t[k])
+    be.close()
+
+
+@pytest.mark.parametrize("rows", [8, 48, 96])
+def test_tiled_fixed_sizes_reproducible(vsgb, tile_model, rows):
+    m, eq6, n, F, U = tile_model
+    be = _backend(vsgb, rows)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    Ut = asm.solve(F[:, :16])
+    assert be.last_stats.batch_tile_rows == rows
+    for k in range(16):
+        assert _rel(Ut[:, k], U[:, k]) <= 1e-6, k
+    assert np.array_equal(asm.solve(F[:, :16]), Ut)
+    be.close()
+
+
+def test_tiled_residual_test(vsgb, tile_model):
+    """A residual tolerance chosen by the caller: the reference's stopping
+    test on the true FP64 residual of every case."""
+    m, eq6, n, F, U = tile_model
+    be = _backend(vsgb, 1, tol=1e-8)
+    be.set_option(vsgb.OPT_INNER_TOL, 1e-3)
+    be.set_option(vsgb.OPT_MAX_SOLVES, 8)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    Ut = asm.solve(F[:, :16])
+    assert be.last_stats.batch_tile_rows > 0
+    for k in range(16):
+        s = be.rhs_stats(k)
+        assert s["converged"] and s["rel_residual"] <= 1e-8, (k, s)
+        assert _rel(Ut[:, k], U[:, k]) <= 1e-6, k
+    be.close()
+
+
+def test_tiled_values_regathered_after_reassembly(vsgb, tile_model):
+    """Re-assembly with new moduli keeps the sparsity pattern: the tiles are
+    kept and only their values gathered again; the result must equal that
+    of a fresh context on the new model, bit for bit."""
+    import copy
+    m, eq6, n, F, U = tile_model
+    m2 = copy.copy(m)
+    m2.E = m.E * (1.0 + 0.5 * np.random.default_rng(9).random(m.n_elem))
+    be = _backend(vsgb, 64)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    asm.solve(F[:, :8])
+    asm.assemble(m2, eq6, n)
+    U1 = asm.solve(F[:, :8])
+    be.close()
+    be2 = _backend(vsgb, 64)
+    asm2 = vsgb.ChexaAssembler(be2)
+    asm2.assemble(m2, eq6, n)
+    U2 = asm2.solve(F[:, :8])
+    be2.close()
+    assert np.array_equal(U1, U2)
+
+
+def test_tiled_zero_and_ragged_cases(vsgb, tile_model):
+    m, eq6, n, F, U = tile_model
+    G = F[:, :3].copy()
+    G[:, 1] = 0.0
+    be = _backend(vsgb, 1)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    Ut = asm.solve(G)
+    assert be.last_stats.batch_tile_rows > 0
+    s1 = be.rhs_stats(1)
+    assert s1["iterations"] == 0 and s1["converged"]
+    assert np.abs(Ut[:, 1]).max() == 0.0
+    assert _rel(Ut[:, 0], U[:, 0]) <= 1e-6 and _rel(Ut[:, 2], U[:, 2]) <= 1e-6
+    be.close()
+
+
+def test_tiled_grid_wait_limit(vsgb, tile_model):
+    """The tiled kernel's bounded grid waits: one poll makes the first CTA at
+    a grid reduction give up; the solve fails with VSGB_ERR_CUDA and the same
+    context solves correctly with the default limit."""
+    m, eq6, n, F, U = tile_model
+    be = _backend(vsgb, 1)
+    try:
+        asm = vsgb.ChexaAssembler(be)
+        asm.assemble(m, eq6, n)
+        be.set_option(vsgb.OPT_SPIN_LIMIT, 1)
+        with pytest.raises(vsgb.SolverError) as e:
+            asm.solve(F[:, :4])
+        assert e.value.code == vsgb.VSGB_ERR_CUDA
+        assert "grid barrier of the persistent solve timed out" in str(e.value)
+        be.set_option(vsgb.OPT_SPIN_LIMIT, 0)
+        Ut = asm.solve(F[:, :4])
+        assert be.last_stats.batch_tile_rows > 0
+        for k in range(4):
+            assert _rel(Ut[:, k], U[:, k]) <= 1e-6, k
+    finally:
+        be.close()
+
+
+def test_tile_too_large_for_shared_memory_falls_back(vsgb, tile_model):
+    """A fixed tile size whose window does not fit shared memory: the batched
+    solve runs the launch-per-kernel path (tile rows 0) with the same bars."""
+    m, eq6, n, F, U = tile_model
+    be = _backend(vsgb, 1024)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    Ut = asm.solve(F[:, :4])
+    assert be.last_stats.batch_tile_rows == 0
+    for k in range(4):
+        assert _rel(Ut[:, k], U[:, k]) <= 1e-6, k
+    be.close()

@@ -60,6 +60,7 @@ OPT_PRECOND = 13
 OPT_ERROR_TARGET = 14
 OPT_SPIN_LIMIT = 15
 OPT_PHASE_TRACE = 16
+OPT_BATCH_TILES = 17
 
 PRECOND_JACOBI = 0
 PRECOND_BLOCK_JACOBI = 1
@@ -106,7 +107,7 @@ class VsgbStats(ctypes.Structure):
                 ("rel_residual", ctypes.c_double), ("solve_ms", ctypes.c_double),
                 ("setup_ms", ctypes.c_double), ("spmv_bytes", ctypes.c_double),
                 ("kernel_ms", ctypes.c_double), ("kernel_iterations", ctypes.c_double),
-                ("est_rel_error", ctypes.c_double)]
+                ("est_rel_error", ctypes.c_double), ("batch_tile_rows", ctypes.c_int)]
 
 
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

@@ -35,7 +35,7 @@ struct vsgb_ctx {
   int max_iters = 10000;
   int precision = VSGB_FP64;
   double inner_tol = 0.0;
-  int max_solves = 3;
+  int max_solves = 0;  // 0: 3, or 5 for an error-controlled mixed solve
   double err_target = -1.0;  // < 0: automatic (mixed 1e-6 unless tol was set, FP64 off)
   bool tol_explicit = false; // the caller chose the residual tolerance
   int format = 0;
@@ -72,6 +72,11 @@ struct vsgb_ctx {
   bool blocks_prebuilt = false;        // the engine's block operator came from assemble_blocks
   bool last_batched = false;
   std::vector<vsgb::SolveResult> rhs;  // per-load-case results of the last solve
+  // tiled batched solve: coordinates of the block rows of the uploaded mesh
+  // (3 per row; empty when the equations are not node-aligned triples) and a
+  // key of its sparsity pattern (node count, element count, equations, conn)
+  std::vector<float> block_xyz;
+  unsigned long long pattern_key = 0;
 };
 
 namespace {
@@ -107,6 +112,14 @@ double default_tol(int precision) { return precision == VSGB_MIXED ? 1e-6 : 1e-8
 double error_target(const vsgb_ctx* c) {
   if (c->err_target >= 0.0) return c->err_target;
   return (c->precision == VSGB_MIXED && !c->tol_explicit) ? 1e-6 : 0.0;
+}
+
+// Inner solves of a mixed solve: the option, else 3 (the reference's 1 + 2
+// corrections) or, error-controlled, 5 (a refinement step may be repeated
+// when the FP32 operator's share of the error is not yet below the target).
+int max_solves(const vsgb_ctx* c) {
+  if (c->max_solves > 0) return c->max_solves;
+  return (c->precision == VSGB_MIXED && error_target(c) > 0.0) ? 5 : 3;
 }
 
 double inner_tolerance(const vsgb_ctx* c, bool batched) {
@@ -196,15 +209,19 @@ void run_batched(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
   c->u.reserve(static_cast<size_t>(n) * nrhs);
   const bool mixed = c->precision == VSGB_MIXED;
   c->eng->set_error_target(error_target(c));
+  // the tiled batched solve needs the mesh the operator was assembled from
+  c->eng->set_block_coords(c->assembled && !c->block_xyz.empty() ? &c->block_xyz : nullptr,
+                           c->pattern_key);
   VSGB_CUDA(cudaEventRecord(c->ev[0], c->stream));
   c->eng->solve_multi(c->f.ptr, nrhs, c->u.ptr, mixed, c->tol, inner_tolerance(c, true), c->max_iters,
-                      c->max_solves, c->stream, c->rhs);
+                      max_solves(c), c->stream, c->rhs);
   VSGB_CUDA(cudaEventRecord(c->ev[1], c->stream));
   VSGB_CUDA(cudaEventSynchronize(c->ev[1]));
   float ms = 0.f;
   VSGB_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
   c->last_batched = true;
   vsgb_stats st{};
+  st.batch_tile_rows = c->eng->batch_tile_rows();
   st.format = c->eng->format_used();
   st.converged = 1;
   st.est_rel_error = -1.0;
@@ -263,7 +280,7 @@ void run_solves(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
     vsgb::SolveResult res;
     VSGB_CUDA(cudaEventRecord(c->ev[0], c->stream));
     if (c->precision == VSGB_MIXED) {
-      c->eng->solve_mixed(fk, c->tol, inner_tolerance(c, false), c->max_iters, c->max_solves,
+      c->eng->solve_mixed(fk, c->tol, inner_tolerance(c, false), c->max_iters, max_solves(c),
                           c->stream,
                           c->h_scal, res);
     } else {
@@ -416,7 +433,7 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
         c->inner_tol = value;
         break;
       case VSGB_OPT_MAX_SOLVES:
-        c->max_solves = value >= 1 ? static_cast<int>(value) : 3;
+        c->max_solves = value >= 1 ? static_cast<int>(value) : 0;
         break;
       case VSGB_OPT_CHECK_EVERY:
         c->eng->set_check_every(static_cast<int>(value));
@@ -457,6 +474,11 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
         break;
       case VSGB_OPT_SPIN_LIMIT:
         c->eng->set_spin_limit(static_cast<long long>(value));
+        break;
+      case VSGB_OPT_BATCH_TILES:
+        if (!(value == 0.0 || value == 1.0 || (value >= 8.0 && value <= 65536.0)))
+          throw Error(VSGB_ERR_INVALID, "VSGB_OPT_BATCH_TILES: 0, 1 or 8..65536 rows per tile");
+        c->eng->set_batch_tiles(static_cast<int>(value));
         break;
       case VSGB_OPT_PHASE_TRACE:
         c->eng->set_phase_trace(value != 0.0);
@@ -585,6 +607,27 @@ int vsgb_mesh_upload(vsgb_ctx* c, int n_nodes, const double* node_xyz, const int
     if (c->h_bad[1] != INT_MAX)
       throw Error(VSGB_ERR_INVALID, "equation index out of range at node index " +
                                         std::to_string(c->h_bad[1] / 3));
+    // Block-row coordinates and the sparsity-pattern key of the tiled batched
+    // solve (host side, one pass over the uploaded arrays).
+    unsigned long long key = 1469598103934665603ULL;  // FNV-1a, 32-bit words
+    auto mix = [&key](unsigned v) { key = (key ^ v) * 1099511628211ULL; };
+    mix(static_cast<unsigned>(n_nodes));
+    mix(static_cast<unsigned>(n_elem));
+    mix(static_cast<unsigned>(n_dof));
+    for (long long k = 0; k < n_eq; ++k) mix(static_cast<unsigned>(node_eq3[k]));
+    for (long long k = 0; k < n_conn; ++k) mix(static_cast<unsigned>(conn[k]));
+    c->pattern_key = key;
+    c->block_xyz.clear();
+    if (n_dof % 3 == 0) {
+      c->block_xyz.assign(static_cast<size_t>(n_dof), 0.f);
+      for (int i = 0; i < n_nodes; ++i) {
+        const int e0 = node_eq3[3 * i];
+        if (e0 >= 0 && e0 % 3 == 0 && e0 + 2 < n_dof && node_eq3[3 * i + 1] == e0 + 1 &&
+            node_eq3[3 * i + 2] == e0 + 2)
+          for (int d = 0; d < 3; ++d)
+            c->block_xyz[static_cast<size_t>(e0) + d] = static_cast<float>(node_xyz[3 * i + d]);
+      }
+    }
     c->mesh_ok = true;
   });
 }

@@ -129,4 +129,19 @@ __device__ inline bool err_block_end(ErrEst& e, double target2_abs, double rel2)
   return stop;
 }
 
+// Refinement with an FP32 operator K32 = K + dK (mixed precision): a step's
+// correction d_j solves K32 d = r, so besides the inner solve's error the
+// step leaves (K^-1 - K32^-1) r ~ K^-1 dK d_j, which no estimate of the inner
+// solve sees.  Its contraction rho = ||K^-1 dK d|| / ||d|| is a property of
+// the operator (largest on the smooth modes, ~1e-4 to 1e-3 measured on these
+// meshes); the ratio of successive corrections estimates it from above
+// (the correction of a step is the error the step before left, the
+// FP32-operator part plus that step's inner error): rho <= ||d_j|| /
+// ||d_{j-1}||.  Squared bound on the FP32-operator part of the error after
+// step j: (rho ||d_j||)^2 <= ||d_j||^4 / ||d_{j-1}||^2.
+__host__ __device__ inline double refine_bound2(double dn2, double dprev2) {
+  if (!(dn2 > 0.0)) return 0.0;
+  return dprev2 > 0.0 ? dn2 * (dn2 / dprev2) : dn2;
+}
+
 }  // namespace vsgb

@@ -28,45 +28,15 @@
 #include <vector>
 
 #include "errest.cuh"
+#include "multi.cuh"
 #include "pcg.cuh"
 
 namespace vsgb {
 
 namespace {
 
-constexpr int kP = 16;     // panel width (load cases per batch)
 constexpr int kMT = 256;   // threads per block of the SpMM / transpose kernels
 constexpr int kVT = 1024;  // threads per block of the panel vector kernels (one block per SM)
-constexpr int kFlagStalled = 128;   // refinement stopped improving (outer record)
-constexpr int kFlagInactive = 256;  // column not part of this solve
-
-struct MultiState {
-  int done;       // every column finished
-  int iter;       // iterations run in this solve
-  int max_iters;
-  int ncols;
-  double tol;
-  double rz[kP], pAp[kP], alpha[kP], beta[kP], rr[kP], rel[kP], norm_b[kP];
-  double tolk[kP];  // per-column stopping tolerance of this solve
-  int flags[kP];
-  int iters[kP];  // iteration count at which the column finished
-  // error-controlled stop (errest.cuh): mode, per-column absolute target^2,
-  // relative target^2 (or floor), and the scale^2 ||u||_D^2 the absolute
-  // target refers to (for reporting the estimate relative to ||u||)
-  int err_mode;
-  double err_t2[kP];
-  double err_rel2;
-  double err_norm2[kP];
-};
-
-struct MultiOuter {
-  double norm_f[kP], rel[kP], prev[kP], scale[kP];
-  double uD2[kP];  // ||u||_D^2 of each column's outer iterate
-  int flags[kP];
-  int active[kP];  // column takes part in the current inner solve
-  int done;
-  int pad;
-};
 
 struct MView {
   int nb, nslices;
@@ -393,14 +363,17 @@ k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restr
 // r = f - K u (FP64) and ||r|| per column; updates the refinement record:
 // convergence (rel <= tol), stagnation (rel >= 0.9 * previous) and the scale
 // 1/||r|| of the next inner right-hand side.
-// With err_stop the residual test is replaced by the inner solve's outcome: a
-// column is done when its (refinement) inner solve met the error target.
+// err_stop replaces the residual test by the error control of the
+// refinement (err_goal = target / safety, relative): 2 after the first inner
+// solve (records ||d_0||_D = ||u||_D), 1 after a refinement step, when a
+// column is done if its inner solve met the error target and the
+// FP32-operator part of the error is below the goal too (refine_bound).
 template <int G>
 __global__ void __launch_bounds__(kMT)
 k_mresidual(MView B, const double* __restrict__ vals, const double* __restrict__ u,
             const double* __restrict__ f, const double* __restrict__ dinv,
-            double* __restrict__ r, MultiOuter* O, const MultiState* S, int err_stop,
-            double tol, double* partials, unsigned* counter) {
+            double* __restrict__ r, MultiOuter* O, const MultiState* S, const ErrEst* est,
+            int err_stop, double err_goal, double tol, double* partials, unsigned* counter) {
   __shared__ double s_red[kMT];
   __shared__ double s_tot[2 * kP];
   constexpr int RN = G / 4;
@@ -438,12 +411,25 @@ k_mresidual(MView B, const double* __restrict__ vals, const double* __restrict__
       if (O->active[k]) {
         const double rn = sqrt(fabs(s_tot[k]));
         const double rel = O->norm_f[k] > 1e-300 ? rn / O->norm_f[k] : rn;
+        const double uD2 = s_tot[kP + k];
         int fl = O->flags[k];
+        if (err_stop == 1) {
+          // the step's correction d = x / scale (||x||_M^2 from the estimate)
+          const double sc = O->scale[k];
+          const double dn2 = est[k].total2 / (sc * sc);
+          const double pb2 = refine_bound2(dn2, O->dD2[k]);
+          O->pert[k] = uD2 > 0.0 ? sqrt(pb2 / uD2) : -1.0;
+          if ((S->flags[k] & kFlagErrTarget) && pb2 <= err_goal * err_goal * uD2)
+            fl |= kFlagDone | kFlagConverged;
+          O->dD2[k] = dn2;
+        } else if (err_stop == 2) {
+          O->dD2[k] = uD2;
+          O->pert[k] = -1.0;
+        }
         O->rel[k] = rel;
         O->scale[k] = rn > 0.0 ? 1.0 / rn : 1.0;
-        O->uD2[k] = s_tot[kP + k];
+        O->uD2[k] = uD2;
         if (err_stop) {
-          if (S->flags[k] & kFlagErrTarget) fl |= kFlagDone | kFlagConverged;
         } else if (rel <= tol) {
           fl |= kFlagDone | kFlagConverged;
         } else if (O->prev[k] > 0.0 && rel >= O->prev[k] * 0.9) {
@@ -499,6 +485,8 @@ k_mouter_init(int n, int ncols, const double* __restrict__ f, double* __restrict
       O->prev[k] = 0.0;
       O->scale[k] = nb > 1e-300 ? 1.0 / nb : 1.0;
       O->uD2[k] = 0.0;
+      O->dD2[k] = 0.0;
+      O->pert[k] = -1.0;
       O->flags[k] = fl;
       O->active[k] = (fl & kFlagDone) ? 0 : 1;
     }
@@ -748,6 +736,15 @@ namespace vsgb {
 struct MultiWork {
   DevBuf<double> f, r64, u64, p64, Ap64;  // FP64 panels
   DevBuf<float> r32, u32, p32, Ap32;      // FP32 panels (mixed inner solves)
+  DevBuf<float> p32b;                     // second direction panel (tiled solve)
+  DevBuf<unsigned long long> trace;       // tiled solve phase timer (ctas x 8)
+  std::vector<unsigned long long> htrace;
+  DevBuf<double> mpart;                   // tiled solve: 2 x ctas x 32 partials
+  MultiTiles tiles[2];                    // tiled solve: chosen + candidate
+  int tbest = -1;                         // tiles[tbest] in use (-1: none fit)
+  unsigned long long tile_key = 0;        // sparsity pattern the tiles belong to
+  int tile_mode = -1, tile_nb = -1;
+  long long tile_steps = -1;
   DevBuf<MultiState> S;
   DevBuf<MultiOuter> O;
   DevBuf<ErrEst> est;  // per-column error estimate (kP)
@@ -793,9 +790,141 @@ void launch_multi_iter(const MView& B, const T* vals, const T* dinv, const float
 
 }  // namespace
 
+bool PcgEngine::ensure_tiles(MultiWork& W, int ncols, cudaStream_t s) {
+  tile_rows_used_ = 0;
+  const int nb = bsr_.nb;
+  if (batch_tiles_ == 0 || !coords_ || coords_->size() != static_cast<size_t>(nb) * 3 ||
+      nb <= 0)
+    return false;
+  const size_t np = static_cast<size_t>(n_) * kP;
+  const size_t npart = static_cast<size_t>(num_sms_) * 2 * 2 * kP;
+  if (W.p32b.cap < np || W.mpart.cap < npart) {
+    W.p32b.reserve(np);
+    W.mpart.reserve(npart);
+    ++W.epoch;
+  }
+  if (W.tile_key == pattern_key_ && W.tile_mode == batch_tiles_ && W.tile_nb == nb &&
+      W.tile_steps == bsr_.steps) {
+    if (W.tbest < 0) return false;  // no tile size fits this pattern
+    MultiTiles& T = W.tiles[W.tbest];
+    if (T.gen != generation_) {
+      mres_gather_values(bsr_, dinv32_.ptr, T, s);
+      launches_ += 1;
+      T.gen = generation_;
+    }
+    tile_rows_used_ = T.tn;
+    return true;
+  }
+  // New sparsity pattern: build the candidate tile sizes (rows per tile for
+  // 2..8 tiles per CTA, or the fixed size asked for) and keep the fastest
+  // over a fixed number of iterations of the current load cases.
+  W.tile_key = 0;
+  W.tile_mode = -1;
+  W.tbest = -1;
+  W.tiles[0].release();
+  W.tiles[1].release();
+  int dev = 0;
+  VSGB_CUDA(cudaGetDevice(&dev));
+  const size_t cap = mres_smem_cap(dev);
+  const int ctas = num_sms_;
+  auto up8 = [](long long v) { return static_cast<int>(std::max(8LL, (v + 7) / 8 * 8)); };
+  std::vector<int> cands;
+  if (batch_tiles_ >= 8) {
+    cands.push_back(up8(batch_tiles_));
+  } else {
+    for (int m : {4, 6, 8, 10, 12, 16}) {
+      const int tn = up8((static_cast<long long>(nb) + static_cast<long long>(ctas) * m - 1) /
+                         (static_cast<long long>(ctas) * m));
+      if (std::find(cands.begin(), cands.end(), tn) == cands.end()) cands.push_back(tn);
+    }
+  }
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  VSGB_CUDA(cudaEventCreate(&ev[0]));
+  VSGB_CUDA(cudaEventCreate(&ev[1]));
+  float best_ms = 0.f;
+  try {
+    for (int tn : cands) {
+      const int slot = W.tbest == 0 ? 1 : 0;
+      MultiTiles& T = W.tiles[slot];
+      T.release();
+      if (!mres_build_tiles(bsr_, dinv32_.ptr, *coords_, tn, ctas, cap, T, s)) continue;
+      if (mres_ctas(num_sms_, T.smem) < 1) {
+        T.release();
+        continue;
+      }
+      T.gen = generation_;
+      launches_ += 1;
+      if (cands.size() == 1) {
+        W.tbest = slot;
+        break;
+      }
+      MresSolve q{};
+      q.r64 = W.r64.ptr;
+      q.u64 = W.u64.ptr;
+      q.r = W.r32.ptr;
+      q.u = W.u32.ptr;
+      q.pa = W.p32.ptr;
+      q.pb = W.p32b.ptr;
+      q.Ap = W.Ap32.ptr;
+      q.dinv32 = dinv32_.ptr;
+      q.diag32 = nullptr;
+      q.S = W.S.ptr;
+      q.O = W.O.ptr;
+      q.est = W.est.ptr;
+      q.partials = W.mpart.ptr;
+      q.count = W.counters.ptr + 6;
+      q.tol = 0.0;
+      q.outer_tol = 0.0;
+      q.max_iters = 24;
+      q.ncols = ncols;
+      q.err_mode = kErrOff;
+      q.spin_limit = spin_limit_;
+      q.accumulate = 0;
+      mres_solve(T, n_, q, s);  // warm-up
+      VSGB_CUDA(cudaEventRecord(ev[0], s));
+      mres_solve(T, n_, q, s);
+      VSGB_CUDA(cudaEventRecord(ev[1], s));
+      launches_ += 2;
+      VSGB_CUDA(cudaEventSynchronize(ev[1]));
+      VSGB_CUDA(cudaMemcpyAsync(W.hS, W.S.ptr, sizeof(MultiState), cudaMemcpyDeviceToHost, s));
+      VSGB_CUDA(cudaStreamSynchronize(s));
+      for (int k = 0; k < kP; ++k)
+        if (W.hS->flags[k] & kFlagResidentAbort)
+          throw Error(VSGB_ERR_CUDA,
+                      "GB300 PCG: a grid barrier of the persistent solve timed out (tiled batched solve)");
+      float ms = 0.f;
+      VSGB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      if (W.tbest < 0 || ms < best_ms) {
+        if (W.tbest >= 0) W.tiles[W.tbest].release();
+        W.tbest = slot;
+        best_ms = ms;
+      } else {
+        T.release();
+      }
+    }
+  } catch (...) {
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    W.tiles[0].release();
+    W.tiles[1].release();
+    W.tbest = -1;  // the next solve builds them again
+    throw;
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  W.tile_key = pattern_key_;
+  W.tile_mode = batch_tiles_;
+  W.tile_nb = nb;
+  W.tile_steps = bsr_.steps;
+  if (W.tbest < 0) return false;
+  tile_rows_used_ = W.tiles[W.tbest].tn;
+  return true;
+}
+
 void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed, double tol,
                             double inner_tol, int max_iters, int max_solves, cudaStream_t s,
                             std::vector<SolveResult>& res) {
+  tile_rows_used_ = 0;
   if (!use_bsr_) throw Error(VSGB_ERR_STATE, "batched PCG needs the 3x3 block operator");
   if (precond_ != 0)
     throw Error(VSGB_ERR_INVALID, "the batched PCG runs the scalar Jacobi preconditioner only");
@@ -969,23 +1098,102 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
       ++launches_;
       read_outer();
       for (int k = 0; k < nc; ++k) res[static_cast<size_t>(k0 + k)].inner_solves = 0;
+      // the persistent tiled kernel runs each inner solve in one launch
+      const bool tiled = !W.hO->done && ensure_tiles(W, nc, s);
+      if (tiled && trace_ && k0 == 0) {
+        for (double& v : tile_ns_) v = 0.0;
+        tile_its_ = 0;
+      }
       for (int step = 0; step < max_solves && !W.hO->done; ++step) {
         const bool err_step = err_control && step > 0;
-        k_minit<float><<<vgrid, kVT, 0, s>>>(
-            n_, nc, W.r64.ptr, W.O.ptr, dinv32_.ptr, W.r32.ptr, W.u32.ptr, W.p32.ptr, W.S.ptr,
-            W.est.ptr, err_step ? kErrAbsolute : kErrOff, err_goal, kErrRelFloor, inner_tol,
-            (adaptive_inner_ && !err_control) ? tol : 0.0, max_iters, W.partials.ptr,
-            W.counters.ptr);
-        VSGB_LAUNCH_CHECK();
-        ++launches_;
-        read_state();
-        check_start();
-        if (!W.hS->done) iterate_all(true);
-        read_state();
+        const double outer = (adaptive_inner_ && !err_control) ? tol : 0.0;
+        if (tiled) {
+          MresSolve q{};
+          q.r64 = W.r64.ptr;
+          q.u64 = W.u64.ptr;
+          q.r = W.r32.ptr;
+          q.u = W.u32.ptr;
+          q.pa = W.p32.ptr;
+          q.pb = W.p32b.ptr;
+          q.Ap = W.Ap32.ptr;
+          q.dinv32 = dinv32_.ptr;
+          q.diag32 = err_control ? diag32 : nullptr;
+          q.S = W.S.ptr;
+          q.O = W.O.ptr;
+          q.est = W.est.ptr;
+          q.partials = W.mpart.ptr;
+          q.count = W.counters.ptr + 6;
+          q.tol = inner_tol;
+          q.outer_tol = outer;
+          q.max_iters = max_iters;
+          q.ncols = nc;
+          q.err_mode = err_step ? kErrAbsolute : kErrOff;
+          q.err_target = err_goal;
+          q.err_rel = kErrRelFloor;
+          q.spin_limit = spin_limit_;
+          q.accumulate = 1;
+          const size_t ntr = static_cast<size_t>(W.tiles[W.tbest].ctas) * 8;
+          if (trace_) {
+            W.trace.reserve(ntr);
+            q.trace = W.trace.ptr;
+          }
+          mres_solve(W.tiles[W.tbest], n_, q, s);
+          ++launches_;
+          read_state();
+          if (trace_) {
+            // per-iteration means over CTAs (us): staging, multiply, first
+            // reduction, update, second reduction; slowest CTA's multiply
+            W.htrace.resize(ntr);
+            VSGB_CUDA(cudaMemcpy(W.htrace.data(), W.trace.ptr, ntr * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost));
+            const int ct = W.tiles[W.tbest].ctas;
+            double sum[5] = {}, mx = 0.0;
+            long long its = 0;
+            for (int c = 0; c < ct; ++c) {
+              for (int k = 0; k < 5; ++k) sum[k] += static_cast<double>(W.htrace[8 * c + k]);
+              mx = std::max(mx, static_cast<double>(W.htrace[8 * c + 1]));
+              its = std::max(its, static_cast<long long>(W.htrace[8 * c + 5]));
+            }
+            tile_ns_[0] += sum[0] / ct;
+            tile_ns_[1] += sum[1] / ct;
+            tile_ns_[2] += sum[2] / ct;
+            tile_ns_[3] += sum[3] / ct;
+            tile_ns_[4] += sum[4] / ct;
+            tile_ns_[5] += mx;
+            tile_its_ += its;
+            const double d = tile_its_ > 0 ? 1e3 * static_cast<double>(tile_its_) : 1.0;
+            for (double& v : phase_us_) v = 0.0;
+            phase_us_[0] = tile_ns_[0] / d;
+            phase_us_[1] = tile_ns_[1] / d;
+            phase_us_[4] = tile_ns_[2] / d;
+            phase_us_[5] = tile_ns_[3] / d;
+            phase_us_[8] = tile_ns_[4] / d;
+            phase_us_[kTracePhases] = tile_ns_[5] / d;
+            phase_us_[kTracePhases + 1] = static_cast<double>(tile_its_);
+          }
+          for (int k = 0; k < kP; ++k)
+            if (W.hS->flags[k] & kFlagResidentAbort)
+              throw Error(VSGB_ERR_CUDA,
+                      "GB300 PCG: a grid barrier of the persistent solve timed out (tiled batched solve)");
+          check_start();
+        } else {
+          k_minit<float><<<vgrid, kVT, 0, s>>>(
+              n_, nc, W.r64.ptr, W.O.ptr, dinv32_.ptr, W.r32.ptr, W.u32.ptr, W.p32.ptr,
+              W.S.ptr, W.est.ptr, err_step ? kErrAbsolute : kErrOff, err_goal, kErrRelFloor,
+              inner_tol, outer, max_iters, W.partials.ptr, W.counters.ptr);
+          VSGB_LAUNCH_CHECK();
+          ++launches_;
+          read_state();
+          check_start();
+          if (!W.hS->done) iterate_all(true);
+          read_state();
+        }
         if (err_step) read_est();
         bool failed = false;
+        int stepped[kP] = {};
         for (int k = 0; k < nc; ++k) {
           if (!W.hO->active[k]) continue;
+          stepped[k] = 1;
           SolveResult& R = res[static_cast<size_t>(k0 + k)];
           ++R.inner_solves;
           R.iterations += W.hS->iters[k];
@@ -1003,14 +1211,25 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
           }
         }
         if (failed) return;
-        k_maccumulate<<<num_sms_, kVT, 0, s>>>(n_, W.u64.ptr, W.u32.ptr, W.O.ptr);
+        if (!tiled) {
+          k_maccumulate<<<num_sms_, kVT, 0, s>>>(n_, W.u64.ptr, W.u32.ptr, W.O.ptr);
+          ++launches_;
+        }
         k_mresidual<8><<<gres, kMT, 0, s>>>(B, bsr_.val64.ptr, W.u64.ptr, W.f.ptr,
                                             op_->dinv.ptr, W.r64.ptr, W.O.ptr, W.S.ptr,
-                                            err_step ? 1 : 0, err_control ? 0.0 : tol,
+                                            W.est.ptr, err_control ? (err_step ? 1 : 2) : 0,
+                                            err_goal, err_control ? 0.0 : tol,
                                             W.partials.ptr, W.counters.ptr + 4);
         VSGB_LAUNCH_CHECK();
-        launches_ += 2;
+        ++launches_;
         read_outer();
+        // reported error: the inner estimate plus the FP32-operator bound
+        if (err_step)
+          for (int k = 0; k < nc; ++k) {
+            SolveResult& R = res[static_cast<size_t>(k0 + k)];
+            if (stepped[k] && W.hO->pert[k] >= 0.0 && R.err_est >= 0.0)
+              R.err_est += W.hO->pert[k];
+          }
       }
       for (int k = 0; k < nc; ++k) {
         SolveResult& R = res[static_cast<size_t>(k0 + k)];

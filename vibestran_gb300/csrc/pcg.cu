@@ -1005,7 +1005,7 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
   const bool err_control = err_target_ > 0.0 && resident;
   if (err_control) ensure_diag32(s);
   trace_reset();
-  double prev_uD2 = 0.0, prev_scale = 1.0;
+  double prev_uD2 = 0.0, prev_scale = 1.0, prev_d2 = 0.0;
   for (int step = 0; step < max_solves; ++step) {
     // Inexact refinement: the correction only has to bring the true residual
     // (outer.rel, relative to ||f||) below tol, so its inner solve may stop
@@ -1076,14 +1076,25 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
         // iterate it corrected
         if (step > 0 && host->err2 >= 0.0 && prev_uD2 > 0.0)
           res.err_est = std::sqrt(host->err2 / prev_uD2) / prev_scale;
+        // ||d||^2 of this step's correction (the first one is u itself) and
+        // the bound on the error the FP32 operator left (refine_bound2)
+        const double dn2 = step == 0 ? outer.uD2 : host->total2 / (prev_scale * prev_scale);
+        bool done = false;
+        if (step > 0) {
+          const double pb2 = refine_bound2(dn2, prev_d2);
+          if (res.err_est >= 0.0 && outer.uD2 > 0.0) res.err_est += std::sqrt(pb2 / outer.uD2);
+          const double goal = err_target_ / kErrSafety;
+          done = (host->flags & kFlagErrTarget) && pb2 <= goal * goal * outer.uD2;
+        }
+        prev_d2 = dn2;
         prev_uD2 = outer.uD2;
         prev_scale = outer.scale;
-        if (step > 0 && (host->flags & kFlagErrTarget)) {
+        if (done) {
           res.converged = true;
           res.err_met = true;
           break;
         }
-        continue;  // first solve, or the relative floor only: refine again
+        continue;  // first solve, the relative floor only, or the FP32 operator's share
       }
       if (outer.rel <= tol) {
         res.converged = true;

@@ -1,6 +1,8 @@
 // vibestran_gb300/csrc/pcg.cuh — PCG engine over a resident full-storage CSR.
 #pragma once
 
+#include <vector>
+
 #include "bsr.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
@@ -84,7 +86,9 @@ class PcgEngine {
   // 0 of each CTA); phase_times() then holds the last solve's per-iteration
   // means over CTAs (us): gather, SpMV, first reduction (CTA sums, wait for
   // the other CTAs, total and recurrence), update, second reduction (same
-  // parts), then the slowest CTA's SpMV (us) and the iterations.
+  // parts), then the slowest CTA's SpMV (us) and the iterations.  For the
+  // tiled batched solve: [0] window staging, [1] multiply, [4] first
+  // reduction, [5] update, [8] second reduction, [9] slowest multiply.
   void set_phase_trace(bool on) { trace_ = on; }
   const double* phase_times() const { return phase_us_; }
   int precond() const { return precond_; }
@@ -104,6 +108,20 @@ class PcgEngine {
   // column-major n x nrhs device arrays (load case k at F + k*n).  Mixed
   // precision runs FP32 inner solves with per-case FP64 refinement.
   bool multi_supported() const { return use_bsr_; }
+  // Coordinates of the block rows (3 floats each) for the tiled batched
+  // solve, and a key of the sparsity pattern they belong to (tiles are
+  // rebuilt when it changes, their values re-gathered when the operator
+  // does).  The vector must outlive the solves; null: no tiles.
+  void set_block_coords(const std::vector<float>* xyz, unsigned long long pattern_key) {
+    coords_ = xyz;
+    pattern_key_ = pattern_key;
+  }
+  // Tiled batched FP32 solve: 0 off (default: the launch-per-kernel path
+  // measured faster), 1 automatic (tile size timed on first use of a
+  // sparsity pattern), >= 8 fixed rows per tile.
+  void set_batch_tiles(int mode) { batch_tiles_ = mode; }
+  // Rows per tile of the last batched solve (0: the launch-per-kernel path).
+  int batch_tile_rows() const { return tile_rows_used_; }
   void solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed, double tol,
                    double inner_tol, int max_iters, int max_solves, cudaStream_t s,
                    std::vector<SolveResult>& res);
@@ -150,6 +168,15 @@ class PcgEngine {
   PcgScalars* graph_host_[2] = {nullptr, nullptr};
 
   MultiWork* multi_ = nullptr;  // batched-solve buffers (multi.cu)
+  const std::vector<float>* coords_ = nullptr;
+  unsigned long long pattern_key_ = 0;
+  int batch_tiles_ = 0;
+  int tile_rows_used_ = 0;
+  // the tiles of the batched FP32 solve for the current operator (false:
+  // none fit, or no coordinates); autotunes on first use of a pattern
+  bool ensure_tiles(MultiWork& W, int ncols, cudaStream_t s);
+  double tile_ns_[6] = {};  // tiled-solve phase sums (ns, means over CTAs) + slowest multiply
+  long long tile_its_ = 0;
 
   // Events around each persistent launch; the host syncs after every launch
   // anyway to read the scalar record.
