@@ -77,6 +77,8 @@ struct vsgb_ctx {
   // key of its sparsity pattern (node count, element count, equations, conn)
   std::vector<float> block_xyz;
   unsigned long long pattern_key = 0;
+  bool coords_ready = false;  // block_xyz / pattern_key belong to the uploaded mesh
+  int batch_tiles = 0;        // VSGB_OPT_BATCH_TILES
 };
 
 namespace {
@@ -204,14 +206,60 @@ std::string not_converged_text(const vsgb_ctx* c, double rel) {
 }
 
 // nrhs > 1 on the block operator: one batched PCG for all load cases.
+// Block-row coordinates (3 floats per block row, node-aligned equation
+// triples only) and a key of the sparsity pattern (FNV-1a over the node
+// count, element count, equations and connectivity) for the tiled batched
+// solve, from host copies of the mesh arrays.
+void block_coords(vsgb_ctx* c, const double* xyz, const int* eq3, const int* conn) {
+  const int n_nodes = c->n_nodes, n_dof = c->n_dof;
+  unsigned long long key = 1469598103934665603ULL;
+  auto mix = [&key](unsigned v) { key = (key ^ v) * 1099511628211ULL; };
+  mix(static_cast<unsigned>(n_nodes));
+  mix(static_cast<unsigned>(c->n_elem));
+  mix(static_cast<unsigned>(n_dof));
+  for (long long k = 0; k < 3LL * n_nodes; ++k) mix(static_cast<unsigned>(eq3[k]));
+  for (long long k = 0; k < 8LL * c->n_elem; ++k) mix(static_cast<unsigned>(conn[k]));
+  c->pattern_key = key;
+  c->block_xyz.clear();
+  if (n_dof % 3 == 0) {
+    c->block_xyz.assign(static_cast<size_t>(n_dof), 0.f);
+    for (int i = 0; i < n_nodes; ++i) {
+      const int e0 = eq3[3 * i];
+      if (e0 >= 0 && e0 % 3 == 0 && e0 + 2 < n_dof && eq3[3 * i + 1] == e0 + 1 &&
+          eq3[3 * i + 2] == e0 + 2)
+        for (int d = 0; d < 3; ++d)
+          c->block_xyz[static_cast<size_t>(e0) + d] = static_cast<float>(xyz[3 * i + d]);
+    }
+  }
+  c->coords_ready = true;
+}
+
+// The same from the device copies of the uploaded mesh (the option was off
+// at upload time).
+void block_coords_from_device(vsgb_ctx* c) {
+  std::vector<double> xyz(3 * static_cast<size_t>(c->n_nodes));
+  std::vector<int> eq3(3 * static_cast<size_t>(c->n_nodes)), conn(8 * static_cast<size_t>(c->n_elem));
+  VSGB_CUDA(cudaMemcpyAsync(xyz.data(), c->xyz.ptr, sizeof(double) * xyz.size(),
+                            cudaMemcpyDeviceToHost, c->stream));
+  VSGB_CUDA(cudaMemcpyAsync(eq3.data(), c->eq3.ptr, sizeof(int) * eq3.size(),
+                            cudaMemcpyDeviceToHost, c->stream));
+  VSGB_CUDA(cudaMemcpyAsync(conn.data(), c->conn.ptr, sizeof(int) * conn.size(),
+                            cudaMemcpyDeviceToHost, c->stream));
+  VSGB_CUDA(cudaStreamSynchronize(c->stream));
+  block_coords(c, xyz.data(), eq3.data(), conn.data());
+}
+
 void run_batched(vsgb_ctx* c, int nrhs, vsgb_stats* stats) {
   const int n = c->K.n;
   c->u.reserve(static_cast<size_t>(n) * nrhs);
   const bool mixed = c->precision == VSGB_MIXED;
   c->eng->set_error_target(error_target(c));
   // the tiled batched solve needs the mesh the operator was assembled from
-  c->eng->set_block_coords(c->assembled && !c->block_xyz.empty() ? &c->block_xyz : nullptr,
-                           c->pattern_key);
+  if (c->batch_tiles != 0 && mixed && c->assembled && c->mesh_ok && !c->coords_ready)
+    block_coords_from_device(c);
+  c->eng->set_block_coords(
+      c->assembled && c->coords_ready && !c->block_xyz.empty() ? &c->block_xyz : nullptr,
+      c->pattern_key);
   VSGB_CUDA(cudaEventRecord(c->ev[0], c->stream));
   c->eng->solve_multi(c->f.ptr, nrhs, c->u.ptr, mixed, c->tol, inner_tolerance(c, true), c->max_iters,
                       max_solves(c), c->stream, c->rhs);
@@ -478,7 +526,8 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
       case VSGB_OPT_BATCH_TILES:
         if (!(value == 0.0 || value == 1.0 || (value >= 8.0 && value <= 65536.0)))
           throw Error(VSGB_ERR_INVALID, "VSGB_OPT_BATCH_TILES: 0, 1 or 8..65536 rows per tile");
-        c->eng->set_batch_tiles(static_cast<int>(value));
+        c->batch_tiles = static_cast<int>(value);
+        c->eng->set_batch_tiles(c->batch_tiles);
         break;
       case VSGB_OPT_PHASE_TRACE:
         c->eng->set_phase_trace(value != 0.0);
@@ -607,27 +656,10 @@ int vsgb_mesh_upload(vsgb_ctx* c, int n_nodes, const double* node_xyz, const int
     if (c->h_bad[1] != INT_MAX)
       throw Error(VSGB_ERR_INVALID, "equation index out of range at node index " +
                                         std::to_string(c->h_bad[1] / 3));
-    // Block-row coordinates and the sparsity-pattern key of the tiled batched
-    // solve (host side, one pass over the uploaded arrays).
-    unsigned long long key = 1469598103934665603ULL;  // FNV-1a, 32-bit words
-    auto mix = [&key](unsigned v) { key = (key ^ v) * 1099511628211ULL; };
-    mix(static_cast<unsigned>(n_nodes));
-    mix(static_cast<unsigned>(n_elem));
-    mix(static_cast<unsigned>(n_dof));
-    for (long long k = 0; k < n_eq; ++k) mix(static_cast<unsigned>(node_eq3[k]));
-    for (long long k = 0; k < n_conn; ++k) mix(static_cast<unsigned>(conn[k]));
-    c->pattern_key = key;
-    c->block_xyz.clear();
-    if (n_dof % 3 == 0) {
-      c->block_xyz.assign(static_cast<size_t>(n_dof), 0.f);
-      for (int i = 0; i < n_nodes; ++i) {
-        const int e0 = node_eq3[3 * i];
-        if (e0 >= 0 && e0 % 3 == 0 && e0 + 2 < n_dof && node_eq3[3 * i + 1] == e0 + 1 &&
-            node_eq3[3 * i + 2] == e0 + 2)
-          for (int d = 0; d < 3; ++d)
-            c->block_xyz[static_cast<size_t>(e0) + d] = static_cast<float>(node_xyz[3 * i + d]);
-      }
-    }
+    // the tiled batched solve's coordinates: now from the caller's arrays
+    // when it is on, else from the device copies on its first use
+    c->coords_ready = false;
+    if (c->batch_tiles != 0) block_coords(c, node_xyz, node_eq3, conn);
     c->mesh_ok = true;
   });
 }
