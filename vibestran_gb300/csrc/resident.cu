@@ -202,6 +202,7 @@ constexpr int kFxWords = 2;          // words per slot (the most values one redu
 constexpr int kFxScaleBits = 36;
 constexpr double kFxPartMax = 549755813888.0;   // 2^39
 constexpr long long kFxTotalMin = 1LL << 30;
+constexpr int kFxPartSlot = 64;      // sm[64..65]: the CTA's FP64 partials (sm holds 96)
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
   unsigned long long v;
@@ -210,6 +211,9 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
 }
 __device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
   asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_relaxed_add_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ void fence_acq_rel_gpu() {
   asm volatile("fence.acq_rel.gpu;" ::: "memory");
@@ -231,11 +235,20 @@ __device__ __forceinline__ int fx_scale(double prev, bool& usable) {
 // of value k (<= 0: none, fall back).  CTA 0 clears the slot two reductions
 // ahead (its last readers all arrived at the reduction before this one).
 // kW as in grid_allreduce.
-template <int NV, int kW = kResWarps, typename Fin>
+// kRelease false: the arrival is a relaxed reduction and the wait has no
+// acquire fence — for a reduction that publishes nothing but its sums (the
+// fixed-point words carry them; GB300 spends ~0.8 us in a release fence
+// whose store has yet to reach L2).  The FP64 partials of the fallback sum
+// are written only when it is needed (every CTA sees the same words) and
+// ordered by a counter barrier (count, target).
+// The fx slot cleared two reductions ahead is ordered by the release of the
+// reduction in between, so two relaxed reductions must not follow each other.
+template <int NV, int kW = kResWarps, bool kRelease = true, typename Fin>
 __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], double* partials,
                                   int slot, unsigned long long* fx, int red, int* abort_flag,
                                   double* sm, int* s_ok, int* s_fb, double* s_tot,
-                                  long long spin_limit, Fin&& fin) {
+                                  long long spin_limit, unsigned* count, unsigned& target,
+                                  Fin&& fin) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (kW > 0) {
     if (wid < kW) {
@@ -249,6 +262,7 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
   }
   double* part = partials + static_cast<size_t>(slot) * gridDim.x * NV;
   static_assert(NV <= kFxWords, "a fused reduction sums at most kFxWords values");
+  static_assert(kW * NV <= kFxPartSlot, "warp sums overlap the partial slots");
   unsigned long long* words = fx + static_cast<size_t>(red % kFxSlots) * kFxWords;
   if (wid == 0) {
     double w[NV];
@@ -266,7 +280,7 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
     }
     if (lane == 0) {
 #pragma unroll
-      for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = w[k];
+      for (int k = 0; k < NV; ++k) sm[kFxPartSlot + k] = w[k];  // for the fallback
       if (blockIdx.x == 0) {
         unsigned long long* ahead = fx + static_cast<size_t>((red + 2) % kFxSlots) * kFxWords;
 #pragma unroll
@@ -290,7 +304,10 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
           else
             add += 1ull << 8;
         }
-        red_release_add_u64(words + k, add);
+        if (kRelease)
+          red_release_add_u64(words + k, add);
+        else
+          red_relaxed_add_u64(words + k, add);
       }
       // wait for every arrival on every word
       unsigned long long* tm = tmarks();
@@ -318,7 +335,7 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
         }
         if (spins > 4096) __nanosleep(64);
       }
-      fence_acq_rel_gpu();
+      if (kRelease) fence_acq_rel_gpu();
       if (tm[2]) tm[1] = gtime();
       int fb = fx_ok ? 0 : 1;
 #pragma unroll
@@ -332,10 +349,20 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
     }
   }
   __syncthreads();
-  const bool ok = *s_ok != 0;
+  bool ok = *s_ok != 0;
+  const bool fb = *s_fb != 0;
+  if (fb && ok) {
+    // every CTA takes this branch (the same words): publish the FP64
+    // partials behind a counter barrier (no store sits before the fast
+    // path's arrival, whose release would wait for it)
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = sm[kFxPartSlot + k];
+    ok = grid_sync(count, target, abort_flag, s_ok, spin_limit);
+  }
   if (threadIdx.x < 32) {
     double acc[NV];
-    if (*s_fb) {
+    if (fb) {
       // fixed-order sum of the FP64 partials, as grid_allreduce
 #pragma unroll
       for (int k = 0; k < NV; ++k) acc[k] = 0.0;
@@ -809,8 +836,9 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       if constexpr (sizeof(T) == 4) {
         if (a.fx) {
           const double prev[2] = {pAp, pMp};
-          ok = grid_allreduce_fx<2, 0>(accb, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
-                                    red, &s_ok, &s_fb, s_tot, a.spin_limit, fin1b);
+          ok = grid_allreduce_fx<2, 0, false>(accb, prev, a.partials, slot, a.fx, fx_red++,
+                                              a.abort_flag, red, &s_ok, &s_fb, s_tot,
+                                              a.spin_limit, a.count, target, fin1b);
         } else {
           ok = grid_allreduce<T, 2, 0>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
                                     &s_ok, a.spin_limit, fin1b);
@@ -822,8 +850,9 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     } else if constexpr (sizeof(T) == 4) {
       if (a.fx) {
         const double prev[1] = {pAp};
-        ok = grid_allreduce_fx<1, 0>(accp, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
-                                  red, &s_ok, &s_fb, s_tot, a.spin_limit, fin1a);
+        ok = grid_allreduce_fx<1, 0, false>(accp, prev, a.partials, slot, a.fx, fx_red++,
+                                            a.abort_flag, red, &s_ok, &s_fb, s_tot, a.spin_limit,
+                                            a.count, target, fin1a);
       } else {
         ok = grid_allreduce<T, 1, 0>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
                                   &s_ok, a.spin_limit, fin1a);
@@ -915,7 +944,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       if (a.fx) {
         const double prev[2] = {rz, rr};
         ok = grid_allreduce_fx<2>(acc2, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
-                                  red, &s_ok, &s_fb, s_tot, a.spin_limit, fin2);
+                                  red, &s_ok, &s_fb, s_tot, a.spin_limit, a.count, target, fin2);
       } else {
         ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
                                   &s_ok, a.spin_limit, fin2);
