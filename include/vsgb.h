@@ -118,6 +118,11 @@ extern "C" {
                                      kernel (measured faster on GB300); 1: tile size timed
                                      on the first solve of a sparsity pattern; 8..65536:
                                      fixed rows per tile. */
+#define VSGB_OPT_COARSE 18        /* error-controlled mixed solves: 1 (default) adds the
+                                     Galerkin correction in the span of the lowest Ritz
+                                     vectors of the operator's first inner solve after
+                                     every FP64 residual (the smooth modes the FP32 inner
+                                     solves resolve last); 0: off. */
 
 #define VSGB_PRECOND_JACOBI 0
 #define VSGB_PRECOND_BLOCK_JACOBI 1

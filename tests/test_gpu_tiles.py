@@ -46,6 +46,9 @@ def _backend(vsgb, tiles, tol=0.0):
 def test_tiled_defaults_match_direct_and_untiled(vsgb, tile_model):
     m, eq6, n, F, U = tile_model
     be = _backend(vsgb, 1)
+    # same recurrence on both paths: without the coarse correction, whose
+    # basis only the launch-per-kernel path records
+    be.set_option(vsgb.OPT_COARSE, 0)
     asm = vsgb.ChexaAssembler(be)
     asm.assemble(m, eq6, n)
     Ut = asm.solve(F)

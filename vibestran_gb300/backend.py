@@ -61,6 +61,7 @@ OPT_ERROR_TARGET = 14
 OPT_SPIN_LIMIT = 15
 OPT_PHASE_TRACE = 16
 OPT_BATCH_TILES = 17
+OPT_COARSE = 18
 
 PRECOND_JACOBI = 0
 PRECOND_BLOCK_JACOBI = 1

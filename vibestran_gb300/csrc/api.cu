@@ -529,6 +529,9 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
         c->batch_tiles = static_cast<int>(value);
         c->eng->set_batch_tiles(c->batch_tiles);
         break;
+      case VSGB_OPT_COARSE:
+        c->eng->set_coarse(value != 0.0);
+        break;
       case VSGB_OPT_PHASE_TRACE:
         c->eng->set_phase_trace(value != 0.0);
         break;

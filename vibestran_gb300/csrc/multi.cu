@@ -27,6 +27,7 @@
 #include <string>
 #include <vector>
 
+#include "coarse.cuh"
 #include "errest.cuh"
 #include "multi.cuh"
 #include "pcg.cuh"
@@ -42,6 +43,14 @@ struct MView {
   int nb, nslices;
   const int* __restrict__ slice_ptr;
   const int* __restrict__ cols;
+};
+
+// Lanczos record of one column of the FP32 batched solve (coarse.cuh): z_k
+// of column col for k < max (n floats each) and alpha_k, beta_k, r_k.z_k.
+struct MultiRecord {
+  float* hist = nullptr;
+  double* coef = nullptr;
+  int col = -1, max = 0;
 };
 
 // Fixed-order grid reduction of per-column sums.  acc[Q][R] holds this
@@ -510,7 +519,8 @@ __global__ void __launch_bounds__(kVT, 1)
 k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
         const T* __restrict__ dinv, T* __restrict__ r, T* __restrict__ u, T* __restrict__ p,
         MultiState* S, ErrEst* est, int err_mode, double err_target, double err_rel,
-        double tol, double outer_tol, int max_iters, double* partials, unsigned* counter) {
+        double tol, double outer_tol, int max_iters, double* partials, unsigned* counter,
+        const MultiRecord rec = MultiRecord{}) {
   __shared__ double s_red[kVT];
   __shared__ double s_tot[2 * kP];
   const int cb = 4 * (threadIdx.x & 3);
@@ -539,6 +549,8 @@ k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
       rz[j] = fmaT(rv[j], zv[j], rz[j]);
       rr[j] = fmaT(rv[j], rv[j], rr[j]);
     }
+    if (rec.hist && rec.col >= cb && rec.col < cb + 4)
+      rec.hist[i] = static_cast<float>(zv[rec.col - cb]);
     st4(r + o, rv);
     st4(u + o, zero);
     st4(p + o, zv);
@@ -577,6 +589,7 @@ k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
       S->err_norm2[k] = un2;
       S->rz[k] = rzk;
       S->rr[k] = rrk;
+      if (rec.coef && k == rec.col) rec.coef[2] = rzk;
       S->norm_b[k] = nb;
       S->rel[k] = (fl & kFlagDone) ? 0.0 : 1.0;
       S->alpha[k] = S->beta[k] = S->pAp[k] = 0.0;
@@ -603,8 +616,12 @@ template <typename T>
 __global__ void __launch_bounds__(kVT, 1)
 k_mupdate(int n, T* __restrict__ u, T* __restrict__ r, const T* __restrict__ p,
           const T* __restrict__ Ap, const T* __restrict__ dinv, MultiState* S, ErrEst* est,
-          double* partials, unsigned* counter) {
+          double* partials, unsigned* counter, const MultiRecord rec = MultiRecord{}) {
   if (S->done) return;
+  // iteration of this update (the last block advances S->iter when every
+  // block has read it)
+  const int it0 = S->iter;
+  const bool keep = rec.hist && it0 + 1 < rec.max;
   __shared__ double s_red[kVT];
   __shared__ double s_tot[2 * kP];
   const int cb = 4 * (threadIdx.x & 3);
@@ -630,6 +647,8 @@ k_mupdate(int n, T* __restrict__ u, T* __restrict__ r, const T* __restrict__ p,
       const T z = rv[j] * d;
       rz[j] = fmaT(rv[j], z, rz[j]);
       rr[j] = fmaT(rv[j], rv[j], rr[j]);
+      if (keep && cb + j == rec.col)
+        rec.hist[static_cast<size_t>(it0 + 1) * n + i] = static_cast<float>(z);
     }
     st4(u + o, uv);
     st4(r + o, rv);
@@ -673,6 +692,11 @@ k_mupdate(int n, T* __restrict__ u, T* __restrict__ r, const T* __restrict__ p,
             fl |= kFlagDone | kFlagMaxIters;
             S->iters[k] = it;
           }
+        }
+        if (rec.coef && k == rec.col && it0 < rec.max) {
+          rec.coef[3 * it0] = S->alpha[k];
+          rec.coef[3 * it0 + 1] = S->beta[k];
+          if (it0 + 1 < rec.max) rec.coef[3 * (it0 + 1) + 2] = rzn;
         }
         S->rz[k] = rzn;
         S->flags[k] = fl;
@@ -738,6 +762,7 @@ struct MultiWork {
   DevBuf<float> r32, u32, p32, Ap32;      // FP32 panels (mixed inner solves)
   DevBuf<float> p32b;                     // second direction panel (tiled solve)
   DevBuf<unsigned long long> trace;       // tiled solve phase timer (ctas x 8)
+  DevBuf<int> cmask;                      // columns of a step (coarse correction)
   std::vector<unsigned long long> htrace;
   DevBuf<double> mpart;                   // tiled solve: 2 x ctas x 32 partials
   MultiTiles tiles[2];                    // tiled solve: chosen + candidate
@@ -780,11 +805,11 @@ int occupancy_grid(const void* fn, int num_sms) {
 template <typename T, int G>
 void launch_multi_iter(const MView& B, const T* vals, const T* dinv, const float* diag32, T* r,
                        T* u, T* p, T* Ap, MultiWork& W, int n, dim3 sgrid, int vgrid,
-                       cudaStream_t s) {
+                       cudaStream_t s, const MultiRecord& rec = MultiRecord{}) {
   k_mspmm<T, G><<<sgrid, kMT, 0, s>>>(B, vals, p, Ap, diag32, W.S.ptr, W.est.ptr,
                                       W.partials.ptr, W.counters.ptr + 1);
   k_mupdate<T><<<vgrid, kVT, 0, s>>>(n, u, r, p, Ap, dinv, W.S.ptr, W.est.ptr, W.partials.ptr,
-                                     W.counters.ptr + 2);
+                                     W.counters.ptr + 2, rec);
   k_mdirection<T><<<vgrid, kVT, 0, s>>>(n, r, dinv, p, W.S.ptr);
 }
 
@@ -991,11 +1016,12 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
     VSGB_CUDA(cudaMemcpyAsync(W.hO, W.O.ptr, sizeof(MultiOuter), cudaMemcpyDeviceToHost, s));
     VSGB_CUDA(cudaStreamSynchronize(s));
   };
-  auto batch = [&](bool fp32) {
+  auto batch = [&](bool fp32, const MultiRecord& rec) {
     for (int k = 0; k < check_every_; ++k) {
       if (fp32)
         launch_multi_iter<float, 16>(B, bsr_.val32.ptr, dinv32_.ptr, diag32, W.r32.ptr,
-                                     W.u32.ptr, W.p32.ptr, W.Ap32.ptr, W, n_, g32, vgrid, s);
+                                     W.u32.ptr, W.p32.ptr, W.Ap32.ptr, W, n_, g32, vgrid, s,
+                                     rec);
       else
         launch_multi_iter<double, 8>(B, bsr_.val64.ptr, op_->dinv.ptr, diag32, W.r64.ptr,
                                      W.u64.ptr, W.p64.ptr, W.Ap64.ptr, W, n_, g64, vgrid, s);
@@ -1005,9 +1031,11 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
   };
   // Batches of check_every iterations (a cached CUDA graph) until every
   // column reports done; the device stops itself at max_iters.
-  auto iterate_all = [&](bool fp32) {
+  // (a recorded solve launches directly: the record is not part of the graph)
+  auto iterate_all = [&](bool fp32, const MultiRecord& rec = MultiRecord{}) {
     const int key = fp32 ? 1 : 0;
-    if (use_graph_ && (W.exec[key] == nullptr || W.exec_epoch[key] != W.epoch ||
+    const bool graph = use_graph_ && rec.hist == nullptr;
+    if (graph && (W.exec[key] == nullptr || W.exec_epoch[key] != W.epoch ||
                        W.exec_batch[key] != check_every_)) {
       if (W.exec[key]) {
         cudaGraphExecDestroy(W.exec[key]);
@@ -1016,7 +1044,7 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
       cudaGraph_t g = nullptr;
       VSGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       try {
-        batch(fp32);
+        batch(fp32, MultiRecord{});
       } catch (...) {
         cudaStreamEndCapture(s, &g);
         if (g) cudaGraphDestroy(g);
@@ -1033,10 +1061,10 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
     for (long long b = 0;; ++b) {
       if (b > max_batches)
         throw Error(VSGB_ERR_CUDA, "batched PCG device state did not report completion");
-      if (use_graph_)
+      if (graph)
         VSGB_CUDA(cudaGraphLaunch(W.exec[key], s));
       else
-        batch(fp32);
+        batch(fp32, rec);
       launches_ += 3LL * check_every_;
       VSGB_CUDA(cudaStreamSynchronize(s));
       if (W.hS->done) break;
@@ -1100,6 +1128,24 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
       for (int k = 0; k < nc; ++k) res[static_cast<size_t>(k0 + k)].inner_solves = 0;
       // the persistent tiled kernel runs each inner solve in one launch
       const bool tiled = !W.hO->done && ensure_tiles(W, nc, s);
+      // Coarse correction (coarse.cuh) after every FP64 residual; without a
+      // basis for this operator the first active column's first inner solve
+      // (launch-per-kernel path) records its Lanczos vectors for one.
+      const bool coarse = err_control && coarse_on_;
+      if (coarse && coarse_.gen != generation_) coarse_.valid = false;
+      MultiRecord rec;
+      if (coarse && coarse_.gen != generation_ && !tiled)
+        for (int k = 0; k < nc; ++k)
+          if (W.hO->active[k]) {
+            rec.col = k;
+            rec.max = std::min(kCoarseHistMax, max_iters + 1);
+            hist_.reserve(static_cast<size_t>(rec.max) * n);
+            coef_.reserve(static_cast<size_t>(3) * rec.max);
+            rec.hist = hist_.ptr;
+            rec.coef = coef_.ptr;
+            break;
+          }
+      if (coarse) W.cmask.reserve(kP);
       if (tiled && trace_ && k0 == 0) {
         for (double& v : tile_ns_) v = 0.0;
         tile_its_ = 0;
@@ -1177,16 +1223,19 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
                       "GB300 PCG: a grid barrier of the persistent solve timed out (tiled batched solve)");
           check_start();
         } else {
+          const MultiRecord r0 = step == 0 ? rec : MultiRecord{};
           k_minit<float><<<vgrid, kVT, 0, s>>>(
               n_, nc, W.r64.ptr, W.O.ptr, dinv32_.ptr, W.r32.ptr, W.u32.ptr, W.p32.ptr,
               W.S.ptr, W.est.ptr, err_step ? kErrAbsolute : kErrOff, err_goal, kErrRelFloor,
-              inner_tol, outer, max_iters, W.partials.ptr, W.counters.ptr);
+              inner_tol, outer, max_iters, W.partials.ptr, W.counters.ptr, r0);
           VSGB_LAUNCH_CHECK();
           ++launches_;
           read_state();
           check_start();
-          if (!W.hS->done) iterate_all(true);
+          if (!W.hS->done) iterate_all(true, r0);
           read_state();
+          if (r0.hist && (W.hS->flags[r0.col] & kFlagConverged))
+            coarse_from_record(std::min(W.hS->iters[r0.col], r0.max), s, false);
         }
         if (err_step) read_est();
         bool failed = false;
@@ -1215,6 +1264,10 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
           k_maccumulate<<<num_sms_, kVT, 0, s>>>(n_, W.u64.ptr, W.u32.ptr, W.O.ptr);
           ++launches_;
         }
+        const bool corrected = coarse && coarse_.valid;
+        if (corrected)  // the columns of this step, before the residual retires some
+          VSGB_CUDA(cudaMemcpyAsync(W.cmask.ptr, W.O.ptr->active, sizeof(int) * kP,
+                                    cudaMemcpyDeviceToDevice, s));
         k_mresidual<8><<<gres, kMT, 0, s>>>(B, bsr_.val64.ptr, W.u64.ptr, W.f.ptr,
                                             op_->dinv.ptr, W.r64.ptr, W.O.ptr, W.S.ptr,
                                             W.est.ptr, err_control ? (err_step ? 1 : 2) : 0,
@@ -1222,6 +1275,12 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
                                             W.partials.ptr, W.counters.ptr + 4);
         VSGB_LAUNCH_CHECK();
         ++launches_;
+        if (corrected) {
+          MultiOuter* O = W.O.ptr;
+          coarse_apply_panel(coarse_, W.u64.ptr, W.r64.ptr, op_->dinv.ptr, W.cmask.ptr,
+                             O->norm_f, O->rel, O->scale, O->uD2, num_sms_, s);
+          launches_ += 2;
+        }
         read_outer();
         // reported error: the inner estimate plus the FP32-operator bound
         if (err_step)

@@ -890,6 +890,30 @@ void PcgEngine::trace_add(cudaStream_t s) {
   phase_us_[kTracePhases + 1] = static_cast<double>(phase_its_);
 }
 
+void PcgEngine::coarse_from_record(int count, cudaStream_t s, bool padded) {
+  coarse_.gen = generation_;  // built (or found unusable) once per operator
+  coarse_.valid = false;
+  if (count < 8) return;
+  coef_h_.resize(static_cast<size_t>(3) * count);
+  VSGB_CUDA(cudaMemcpyAsync(coef_h_.data(), coef_.ptr, sizeof(double) * coef_h_.size(),
+                            cudaMemcpyDeviceToHost, s));
+  VSGB_CUDA(cudaStreamSynchronize(s));
+  // K z with a scratch record (the SpMV kernel skips its work once the
+  // record it is given reports done, as the inner record now does)
+  coarse_scal_.reserve(1);
+  VSGB_CUDA(cudaMemsetAsync(coarse_scal_.ptr, 0, sizeof(PcgScalars), s));
+  coarse_build(coarse_, hist_.ptr, padded, coef_h_, count, n_ / 3, 4,
+               [&](const double* x, double* y) {
+                 k_bsr_spmv64<<<bsr_grid_, kSpmvThreads, 0, s>>>(
+                     view_of(bsr_), bsr_.val64.ptr, x, y, coarse_scal_.ptr, partials_.ptr,
+                     counters_.ptr + 1);
+                 VSGB_LAUNCH_CHECK();
+                 ++launches_;
+               },
+               num_sms_, s);
+  launches_ += 2;
+}
+
 void PcgEngine::ensure_diag32(cudaStream_t s) {
   if (diag_gen_ == generation_) return;
   resident_diag(res_, op_->dinv.ptr, n_, num_sms_, s);
@@ -1004,6 +1028,16 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
   // estimate of errest.cuh; the loop ends when a step met the error target.
   const bool err_control = err_target_ > 0.0 && resident;
   if (err_control) ensure_diag32(s);
+  // Coarse correction (coarse.cuh): the first inner solve on this operator
+  // records its Lanczos vectors for the basis.
+  const bool coarse = err_control && coarse_on_ && use_bsr_;
+  const bool record = coarse && coarse_.gen != generation_;
+  if (record) coarse_.valid = false;  // a basis of an earlier operator
+  const int hist_max = std::min(kCoarseHistMax, max_iters + 1);
+  if (record) {
+    hist_.reserve(static_cast<size_t>(hist_max) * 4 * (n_ / 3));
+    coef_.reserve(static_cast<size_t>(3) * hist_max);
+  }
   trace_reset();
   double prev_uD2 = 0.0, prev_scale = 1.0, prev_d2 = 0.0;
   for (int step = 0; step < max_solves; ++step) {
@@ -1027,6 +1061,11 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       ctl.block_jacobi = bj;
       ctl.spin_limit = spin_limit_;
       ctl.trace = trace_;
+      if (record && step == 0) {
+        ctl.hist = hist_.ptr;
+        ctl.coef = coef_.ptr;
+        ctl.hist_max = hist_max;
+      }
       if (err_control && step > 0) {
         // refinement step: the correction's error must fall below
         // (target / safety) ||u||_D of the current iterate; the relative
@@ -1044,6 +1083,14 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       launch_residual64(s, d_f);
       VSGB_LAUNCH_CHECK();
       ++launches_;
+      // Galerkin correction in the coarse space right behind the residual
+      // (the next inner solve reads the refreshed outer record on the device;
+      // after a failed inner solve the iterate is not used)
+      const bool corrected = coarse && coarse_.valid;
+      if (corrected) {
+        coarse_apply(coarse_, u_.ptr, r_.ptr, op_->dinv.ptr, scal_.ptr + 1, num_sms_, s);
+        launches_ += 2;
+      }
       VSGB_CUDA(cudaMemcpyAsync(host, scal_.ptr, 2 * sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                 s));
       VSGB_CUDA(cudaStreamSynchronize(s));
@@ -1069,6 +1116,18 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
         res.rel = host->rel;
         res.inner_failed = true;
         return;
+      }
+      if (coarse && !corrected && record && step == 0) {
+        // the basis of this operator, from the solve just recorded
+        coarse_from_record(std::min(host->iter, hist_max), s);
+        if (coarse_.valid) {
+          coarse_apply(coarse_, u_.ptr, r_.ptr, op_->dinv.ptr, scal_.ptr + 1, num_sms_, s);
+          launches_ += 2;
+          VSGB_CUDA(cudaMemcpyAsync(host + 1, scal_.ptr + 1, sizeof(PcgScalars),
+                                    cudaMemcpyDeviceToHost, s));
+          VSGB_CUDA(cudaStreamSynchronize(s));
+          outer = host[1];
+        }
       }
       res.rel = outer.rel;
       if (err_control) {

@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "bsr.cuh"
+#include "coarse.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 #include "resident.cuh"
@@ -116,6 +117,10 @@ class PcgEngine {
     coords_ = xyz;
     pattern_key_ = pattern_key;
   }
+  // Coarse (Ritz) correction of error-controlled mixed solves (coarse.cuh):
+  // on by default; off for comparisons.
+  void set_coarse(bool on) { coarse_on_ = on; }
+  int coarse_size() const { return coarse_.valid ? coarse_.m : 0; }
   // Tiled batched FP32 solve: 0 off (default: the launch-per-kernel path
   // measured faster), 1 automatic (tile size timed on first use of a
   // sparsity pattern), >= 8 fixed rows per tile.
@@ -168,6 +173,16 @@ class PcgEngine {
   PcgScalars* graph_host_[2] = {nullptr, nullptr};
 
   MultiWork* multi_ = nullptr;  // batched-solve buffers (multi.cu)
+  // coarse correction: the basis, and the Lanczos record it is built from
+  CoarseSpace coarse_;
+  bool coarse_on_ = true;
+  DevBuf<float> hist_;
+  DevBuf<double> coef_;
+  DevBuf<PcgScalars> coarse_scal_;  // scratch record of the basis SpMVs
+  std::vector<double> coef_h_;
+  // the first inner solve of an operator records its Lanczos vectors; this
+  // builds the basis from them (count = iterations recorded)
+  void coarse_from_record(int count, cudaStream_t s, bool padded = true);
   const std::vector<float>* coords_ = nullptr;
   unsigned long long pattern_key_ = 0;
   int batch_tiles_ = 0;

@@ -71,6 +71,12 @@ struct ResArgs {
   // total and recurrence), update, second reduction (same three parts), then
   // the iteration count (kTraceWords per CTA)
   unsigned long long* trace;
+  // Lanczos record of the FP32 solve (null: off): z_k of every row for
+  // k < hist_max (node-padded, 4 * nb floats per k) and, CTA 0, the
+  // recurrence scalars alpha_k, beta_k, r_k.z_k (3 doubles per k)
+  float* hist;
+  double* coef;
+  int hist_max;
 };
 
 // Cost of a slice beyond its steps, in steps, when slice ranges are split
@@ -198,7 +204,7 @@ __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned*
 // (a drop of more than 64x, where the fixed point has too few digits).
 constexpr bool kFusedReductions = true;
 constexpr int kFxSlots = 4;          // reductions in flight before a word is reused
-constexpr int kFxWords = 2;          // words per slot (the most values one reduction sums)
+constexpr int kFxWords = 4;          // words per slot (2 values, 2 words each in the FP64 solve)
 constexpr int kFxScaleBits = 36;
 constexpr double kFxPartMax = 549755813888.0;   // 2^39
 constexpr long long kFxTotalMin = 1LL << 30;
@@ -222,6 +228,28 @@ __device__ __forceinline__ void fence_acq_rel_gpu() {
 __device__ __forceinline__ double pow2i(int e) {
   return __longlong_as_double(static_cast<long long>(e + 1023) << 52);
 }
+// round(v 2^sc) for an FP32 v by integer operations (the FP32 solve's CTA
+// totals: no FP64 instruction on the reduction's critical path); ok = false
+// when the result would reach 2^39 (or v is not finite).  Ties round up in
+// magnitude; every CTA and run rounds alike.
+__device__ __forceinline__ long long f32_fixed(float v, int sc, bool& ok) {
+  const unsigned b = __float_as_uint(v);
+  const int e = static_cast<int>((b >> 23) & 0xFFu);
+  if (e == 0) return 0;  // zero or subnormal: far below the total's resolution
+  const int sh = e - 150 + sc;  // |v| 2^sc = m 2^sh, m < 2^24
+  if (e == 0xFF || sh > 15) {
+    ok = false;
+    return 0;
+  }
+  const long long m = static_cast<long long>((b & 0x7FFFFFu) | 0x800000u);
+  long long r = 0;
+  if (sh >= 0)
+    r = m << sh;
+  else if (sh > -26)
+    r = (m + (1LL << (-sh - 1))) >> (-sh);
+  return (b >> 31) ? -r : r;
+}
+
 // Scale exponent for a total near `prev` (0: none usable)
 __device__ __forceinline__ int fx_scale(double prev, bool& usable) {
   const long long bits = __double_as_longlong(prev);
@@ -243,32 +271,42 @@ __device__ __forceinline__ int fx_scale(double prev, bool& usable) {
 // ordered by a counter barrier (count, target).
 // The fx slot cleared two reductions ahead is ordered by the release of the
 // reduction in between, so two relaxed reductions must not follow each other.
-template <int NV, int kW = kResWarps, bool kRelease = true, typename Fin>
-__device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], double* partials,
+// FP64 solve (TV = double): each value takes two words, the integer part of
+// the scaled CTA partial and its next 32 fraction bits (the low words' sum of
+// at most 255 CTAs stays below 2^40), so the total carries ~68 bits below
+// the previous total's leading bit and no FP64 partial sum is needed after
+// the barrier.
+template <int NV, int kW = kResWarps, bool kRelease = true, typename TV, typename Fin>
+__device__ bool grid_allreduce_fx(TV (&v)[NV], const double (&prev)[NV], double* partials,
                                   int slot, unsigned long long* fx, int red, int* abort_flag,
                                   double* sm, int* s_ok, int* s_fb, double* s_tot,
                                   long long spin_limit, unsigned* count, unsigned& target,
                                   Fin&& fin) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // CTA totals in the input type (FP32 solve: FP32 throughout, as its
+  // per-thread and per-warp sums are)
+  TV* smv = reinterpret_cast<TV*>(sm);
   if (kW > 0) {
     if (wid < kW) {
 #pragma unroll
       for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
       if (lane == 0)
 #pragma unroll
-        for (int k = 0; k < NV; ++k) sm[wid * NV + k] = static_cast<double>(v[k]);
+        for (int k = 0; k < NV; ++k) smv[wid * NV + k] = v[k];
     }
     __syncthreads();
   }
   double* part = partials + static_cast<size_t>(slot) * gridDim.x * NV;
-  static_assert(NV <= kFxWords, "a fused reduction sums at most kFxWords values");
+  constexpr bool kSplit = sizeof(TV) == 8;
+  constexpr int kWpv = kSplit ? 2 : 1;  // words per value
+  static_assert(NV * kWpv <= kFxWords, "a fused reduction sums at most kFxWords words");
   static_assert(kW * NV <= kFxPartSlot, "warp sums overlap the partial slots");
   unsigned long long* words = fx + static_cast<size_t>(red % kFxSlots) * kFxWords;
   if (wid == 0) {
-    double w[NV];
+    TV w[NV];
     if (kW > 0) {
 #pragma unroll
-      for (int k = 0; k < NV; ++k) w[k] = lane < kW ? sm[lane * NV + k] : 0.0;
+      for (int k = 0; k < NV; ++k) w[k] = lane < kW ? smv[lane * NV + k] : TV(0);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
         if (o < kW)
@@ -276,11 +314,9 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
           for (int k = 0; k < NV; ++k) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
     } else {
 #pragma unroll
-      for (int k = 0; k < NV; ++k) w[k] = static_cast<double>(v[k]);
+      for (int k = 0; k < NV; ++k) w[k] = v[k];
     }
     if (lane == 0) {
-#pragma unroll
-      for (int k = 0; k < NV; ++k) sm[kFxPartSlot + k] = w[k];  // for the fallback
       if (blockIdx.x == 0) {
         unsigned long long* ahead = fx + static_cast<size_t>((red + 2) % kFxSlots) * kFxWords;
 #pragma unroll
@@ -294,31 +330,47 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
         sc[k] = fx_scale(prev[k], u);
         fx_ok = fx_ok && u;
       }
+      unsigned long long adds[NV * kWpv];
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
-        unsigned long long add = 1ull;
+        unsigned long long add = 1ull, add_lo = 1ull;
         if (fx_ok) {
-          const double y = w[k] * pow2i(sc[k]);
-          if (fabs(y) < kFxPartMax)
-            add += static_cast<unsigned long long>(__double2ll_rn(y)) << 16;
-          else
-            add += 1ull << 8;
+          if constexpr (kSplit) {
+            const double y = w[k] * pow2i(sc[k]);
+            if (fabs(y) < kFxPartMax) {
+              const double hi = floor(y);
+              add += static_cast<unsigned long long>(static_cast<long long>(hi)) << 16;
+              add_lo += static_cast<unsigned long long>(__double2ll_rn((y - hi) * 4294967296.0))
+                        << 16;
+            } else {
+              add += 1ull << 8;
+            }
+          } else {
+            bool in_range = true;
+            const long long q = f32_fixed(w[k], sc[k], in_range);
+            add += in_range ? static_cast<unsigned long long>(q) << 16 : 1ull << 8;
+          }
         }
-        if (kRelease)
-          red_release_add_u64(words + k, add);
-        else
-          red_relaxed_add_u64(words + k, add);
+        adds[kWpv * k] = add;
+        if (kSplit) adds[kWpv * k + 1] = add_lo;
       }
+      // one fence orders the CTA's writes before all the words' adds (a
+      // release per word would wait once per word)
+      if (kRelease) fence_acq_rel_gpu();
+#pragma unroll
+      for (int k = 0; k < NV * kWpv; ++k) red_relaxed_add_u64(words + k, adds[k]);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) sm[kFxPartSlot + k] = static_cast<double>(w[k]);  // fallback
       // wait for every arrival on every word
       unsigned long long* tm = tmarks();
       if (tm[2]) tm[0] = gtime();
       int ok = 1;
       long long spins = 0;
-      unsigned long long got[NV];
+      unsigned long long got[NV * kWpv];
       for (;;) {
         bool all = true;
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
+        for (int k = 0; k < NV * kWpv; ++k) {
           got[k] = ld_relaxed_u64(words + k);
           all = all && (got[k] & 0xFFull) >= gridDim.x;
         }
@@ -340,9 +392,13 @@ __device__ bool grid_allreduce_fx(float (&v)[NV], const double (&prev)[NV], doub
       int fb = fx_ok ? 0 : 1;
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
-        const long long q = static_cast<long long>(got[k]) >> 16;
-        if (((got[k] >> 8) & 0xFFull) != 0ull || (q < kFxTotalMin && q > -kFxTotalMin)) fb = 1;
-        s_tot[k] = static_cast<double>(q) * pow2i(-sc[k]);
+        const unsigned long long g = got[kWpv * k];
+        const long long q = static_cast<long long>(g) >> 16;
+        if (((g >> 8) & 0xFFull) != 0ull || (q < kFxTotalMin && q > -kFxTotalMin)) fb = 1;
+        double t = static_cast<double>(q);
+        if (kSplit)
+          t += static_cast<double>(got[kWpv * k + 1] >> 16) * (1.0 / 4294967296.0);
+        s_tot[k] = t * pow2i(-sc[k]);
       }
       *s_ok = ok;
       *s_fb = fb;
@@ -504,6 +560,9 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         acc2[1] = rfma(rv[q], zv[q], acc2[1]);
       }
       st3(a.z4 + 4 * static_cast<size_t>(R), zv[0], zv[1], zv[2]);
+      if (kMixed && a.hist)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) a.hist[4 * static_cast<size_t>(R) + q] = static_cast<float>(zv[q]);
       st3(a.p4a + 4 * static_cast<size_t>(R), T(0), T(0), T(0));
       st3(a.p4b + 4 * static_cast<size_t>(R), T(0), T(0), T(0));
     }
@@ -521,6 +580,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     AP[lr] = T(0);
     D[lr] = dv;
     a.z4[4 * R + q] = zv;
+    if (kMixed && a.hist) a.hist[4 * R + q] = static_cast<float>(zv);
     a.p4a[4 * R + q] = T(0);
     a.p4b[4 * R + q] = T(0);
     acc2[0] = rfma(rv, rv, acc2[0]);
@@ -563,6 +623,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
                               norm_b = sqrt(fabs(t[0]));
                               rz = t[1];
                               rr = t[0];
+                              if (kMixed && a.coef && blockIdx.x == 0) a.coef[2] = rz;
                               rr_stop = (a.tol * norm_b) * (a.tol * norm_b);
                               if (!good) {
                                 flags = kFlagDone | kFlagAbort;
@@ -825,41 +886,34 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
           pMp = pMpv;
           err_record(s_err, rz * alpha, pMp * rp);
         }
+        if (kMixed && a.coef && blockIdx.x == 0 && it < a.hist_max) a.coef[3 * it] = alpha;
       }
       s_flags = flags;
       s_sc[0] = alpha;
     };
     auto fin1a = [&](const double (&t)[1], bool good) { fin1(t[0], 0.0, good); };
     auto fin1b = [&](const double (&t)[2], bool good) { fin1(t[0], t[1], good); };
+    // The first reduction publishes nothing but its sums (relaxed arrival,
+    // grid_allreduce_fx); without the fused words, the counter barrier.
     if (err_on) {
       T accb[2] = {accp[0], accm};
-      if constexpr (sizeof(T) == 4) {
-        if (a.fx) {
-          const double prev[2] = {pAp, pMp};
-          ok = grid_allreduce_fx<2, 0, false>(accb, prev, a.partials, slot, a.fx, fx_red++,
-                                              a.abort_flag, red, &s_ok, &s_fb, s_tot,
-                                              a.spin_limit, a.count, target, fin1b);
-        } else {
-          ok = grid_allreduce<T, 2, 0>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
-                                    &s_ok, a.spin_limit, fin1b);
-        }
+      if (a.fx) {
+        const double prev[2] = {pAp, pMp};
+        ok = grid_allreduce_fx<2, 0, false>(accb, prev, a.partials, slot, a.fx, fx_red++,
+                                            a.abort_flag, red, &s_ok, &s_fb, s_tot,
+                                            a.spin_limit, a.count, target, fin1b);
       } else {
         ok = grid_allreduce<T, 2, 0>(accb, a.partials, slot, a.count, target, a.abort_flag, red,
-                                  &s_ok, a.spin_limit, fin1b);
+                                     &s_ok, a.spin_limit, fin1b);
       }
-    } else if constexpr (sizeof(T) == 4) {
-      if (a.fx) {
-        const double prev[1] = {pAp};
-        ok = grid_allreduce_fx<1, 0, false>(accp, prev, a.partials, slot, a.fx, fx_red++,
-                                            a.abort_flag, red, &s_ok, &s_fb, s_tot, a.spin_limit,
-                                            a.count, target, fin1a);
-      } else {
-        ok = grid_allreduce<T, 1, 0>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
-                                  &s_ok, a.spin_limit, fin1a);
-      }
+    } else if (a.fx) {
+      const double prev[1] = {pAp};
+      ok = grid_allreduce_fx<1, 0, false>(accp, prev, a.partials, slot, a.fx, fx_red++,
+                                          a.abort_flag, red, &s_ok, &s_fb, s_tot, a.spin_limit,
+                                          a.count, target, fin1a);
     } else {
       ok = grid_allreduce<T, 1, 0>(accp, a.partials, slot, a.count, target, a.abort_flag, red,
-                                &s_ok, a.spin_limit, fin1a);
+                                   &s_ok, a.spin_limit, fin1a);
     }
     slot ^= 1;
     flags = s_flags;
@@ -886,6 +940,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
           acc2[1] = rfma(rv[q], rv[q], acc2[1]);
         }
         st3(a.z4 + 4 * static_cast<size_t>(R), zv[0], zv[1], zv[2]);
+        if (kMixed && a.hist && it + 1 < a.hist_max) {
+          float* h = a.hist + static_cast<size_t>(it + 1) * 4 * a.nb + 4 * static_cast<size_t>(R);
+#pragma unroll
+          for (int q = 0; q < 3; ++q) h[q] = static_cast<float>(zv[q]);
+        }
       }
     }
     for (int lr = tid; !kBJ && tid < kP2Threads && lr < nrows; lr += kP2Threads) {
@@ -896,6 +955,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       const T zv = rv * D[lr];
       RR[lr] = rv;
       a.z4[4 * R + q] = zv;
+      if (kMixed && a.hist && it + 1 < a.hist_max)
+        a.hist[static_cast<size_t>(it + 1) * 4 * a.nb + 4 * R + q] = static_cast<float>(zv);
       acc2[0] = rfma(rv, zv, acc2[0]);
       acc2[1] = rfma(rv, rv, acc2[1]);
     }
@@ -935,23 +996,24 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
                      : div_nr(t[0], rz, rcp_nr2(rz));
           if (it >= a.max_iters) flags |= kFlagDone | kFlagMaxIters;
         }
+        if (kMixed && a.coef && blockIdx.x == 0 && it < a.hist_max) {
+          a.coef[3 * (it - 1) + 1] = beta;  // it was incremented before the reduction
+          a.coef[3 * it + 2] = t[0];
+        }
         rz = t[0];
       }
       s_flags = flags;
       s_sc[1] = beta;
     };
-    if constexpr (sizeof(T) == 4) {
-      if (a.fx) {
-        const double prev[2] = {rz, rr};
-        ok = grid_allreduce_fx<2>(acc2, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
-                                  red, &s_ok, &s_fb, s_tot, a.spin_limit, a.count, target, fin2);
-      } else {
-        ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
-                                  &s_ok, a.spin_limit, fin2);
-      }
+    constexpr int kW2 = sizeof(T) == 4 ? kResWarps : kP2Warps;  // warps holding partials
+    if (a.fx) {
+      const double prev[2] = {rz, rr};
+      ok = grid_allreduce_fx<2, kW2>(acc2, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
+                                     red, &s_ok, &s_fb, s_tot, a.spin_limit, a.count, target,
+                                     fin2);
     } else {
-      ok = grid_allreduce<T, 2, kP2Warps>(acc2, a.partials, slot, a.count, target, a.abort_flag,
-                                          red, &s_ok, a.spin_limit, fin2);
+      ok = grid_allreduce<T, 2, kW2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
+                                     &s_ok, a.spin_limit, fin2);
     }
     slot ^= 1;
     flags = s_flags;
@@ -1099,7 +1161,7 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   a.partials = P.partials.ptr;
   a.count = P.barrier.ptr;
   // fused reductions: FP32 solve, arrivals counted in 8 bits
-  a.fx = (sizeof(T) == 4 && kFusedReductions && P.ctas <= 255) ? P.fx.ptr : nullptr;
+  a.fx = (kFusedReductions && P.ctas <= 255) ? P.fx.ptr : nullptr;
   if (a.fx)
     VSGB_CUDA(cudaMemsetAsync(P.fx.ptr, 0, sizeof(unsigned long long) * kFxSlots * kFxWords, s));
   // The abort word lives in the solve's scalar record, which the host reads
@@ -1118,6 +1180,9 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   a.err_rel = ctl.err_rel;
   a.diag32 = P.diag32.ptr;
   a.bjd32 = P.bjd32.ptr;
+  a.hist = ctl.hist;
+  a.coef = ctl.coef;
+  a.hist_max = ctl.hist ? ctl.hist_max : 0;
   a.trace = nullptr;
   if (ctl.trace) {
     P.trace.reserve(static_cast<size_t>(kTraceWords) * P.ctas);

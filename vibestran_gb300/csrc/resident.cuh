@@ -53,6 +53,11 @@ struct ResidentCtl {
   long long spin_limit = kDefaultSpinLimit;
   bool block_jacobi = false; // 3x3 block Jacobi instead of the scalar one
   bool trace = false;        // time the phases of every iteration (P.trace)
+  // FP32 solve: Lanczos record (z_k of the first hist_max iterations, node
+  // padded, and alpha_k, beta_k, r_k.z_k); null: off
+  float* hist = nullptr;
+  double* coef = nullptr;
+  int hist_max = 0;
 };
 
 // Plans CTA ranges / windows and allocates the padded vectors; leaves both
