@@ -349,6 +349,36 @@ def extra_bdf(B, C):
     return out
 
 
+def extra_same_operator(B, C, device):
+    """Repeated single-RHS solves with one operator (the second and later
+    solves of a load-case sequence): the coarse correction alone
+    (VSGB_OPT_COARSE 1, the default) against the first inner solve deflated
+    by the recorded Ritz basis (2), on the uniform and the jittered
+    heterogeneous 84k cantilevers, each solve's error against the FP64
+    sparse-direct fingerprint."""
+    out = {}
+    for name in ("cantilever_84k", "cantilever_84k_jitter"):
+        m = getattr(C, name)()
+        eq6, n = B.build_dof_map(m)
+        F = B.apply_forces(m, eq6, n)
+        rel_err = _fingerprint_err(name + "_direct.json")
+        for mode in (1, 2):
+            be = _mixed_backend(B, device)
+            be.set_option(B.OPT_COARSE, mode)
+            asm = B.ChexaAssembler(be)
+            asm.assemble(m, eq6, n)
+            asm.upload_rhs(F)
+            first = asm.solve_resident()
+            runs = [asm.solve_resident() for _ in range(3)]
+            err = rel_err(asm.download())
+            be.close()
+            out[f"{name}_coarse{mode}"] = {
+                "first_solve_s": first.solve_ms / 1e3, "first_iterations": first.iterations,
+                "repeat_solve_s": statistics.median(r.solve_ms for r in runs) / 1e3,
+                "repeat_iterations": runs[-1].iterations, "repeat_rel_err": err}
+    return out
+
+
 def extra_jitter(B, C, device, uniform):
     """Jittered (U(+-0.2 h) interior nodes) heterogeneous (log-uniform E)
     84 000-element cantilever: FP64 and mixed iteration counts against the
@@ -528,7 +558,8 @@ def main():
                          "kernel) of cantilever_84k; solve64 = one FP64 persistent solve of "
                          "cantilever_84k (error target 1e-6); multi = 48 batched iterations "
                          "of the 16-load-case block")
-    ap.add_argument("--extra", choices=["multi_rhs", "adjoint", "stress", "bdf"], default=None,
+    ap.add_argument("--extra", choices=["multi_rhs", "adjoint", "stress", "bdf", "same_operator"],
+                    default=None,
                     help="run one of the additional workloads alone, print its JSON and exit")
     a = ap.parse_args()
     if a.profile:
@@ -541,7 +572,8 @@ def main():
         fn = {"multi_rhs": lambda: extra_multi_rhs(B, C, 0),
               "adjoint": lambda: extra_adjoint(B, C, 0),
               "stress": lambda: extra_stress(B, C, 0),
-              "bdf": lambda: extra_bdf(B, C)}[a.extra]
+              "bdf": lambda: extra_bdf(B, C),
+              "same_operator": lambda: extra_same_operator(B, C, 0)}[a.extra]
         print(json.dumps(fn()))
         return
 
@@ -702,6 +734,7 @@ def main():
                   "adjoint_250k": extra_adjoint(B, C, device),
                   "stress_84k": extra_stress(B, C, device),
                   "bdf_250k": extra_bdf(B, C),
+                  "same_operator_84k": extra_same_operator(B, C, device),
                   "jitter_84k": extra_jitter(B, C, device,
                                              {"fp64": st_fp64.iterations, "mixed": it_mixed})}
     line = {

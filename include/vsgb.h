@@ -122,7 +122,11 @@ extern "C" {
                                      Galerkin correction in the span of the lowest Ritz
                                      vectors of the operator's first inner solve after
                                      every FP64 residual (the smooth modes the FP32 inner
-                                     solves resolve last); 0: off. */
+                                     solves resolve last); 2 also deflates the first FP32
+                                     inner solve of later single-RHS solves with the same
+                                     operator by that basis (scalar Jacobi; faster, but
+                                     the error target can be missed when the basis lacks
+                                     a low mode the load excites); 0: off. */
 
 #define VSGB_PRECOND_JACOBI 0
 #define VSGB_PRECOND_BLOCK_JACOBI 1

@@ -530,7 +530,9 @@ int vsgb_set_option(vsgb_ctx* c, int option, double value) {
         c->eng->set_batch_tiles(c->batch_tiles);
         break;
       case VSGB_OPT_COARSE:
-        c->eng->set_coarse(value != 0.0);
+        if (!(value == 0.0 || value == 1.0 || value == 2.0))
+          throw Error(VSGB_ERR_INVALID, "VSGB_OPT_COARSE: 0, 1 or 2");
+        c->eng->set_coarse(static_cast<int>(value));
         break;
       case VSGB_OPT_PHASE_TRACE:
         c->eng->set_phase_trace(value != 0.0);

@@ -472,6 +472,57 @@ k_coarse_update_panel(int n, const int* __restrict__ meff, const double* __restr
   if (threadIdx.x == 0) *counter = 0u;
 }
 
+// FP32 deflation arrays: W (node-padded, 4 x 4 nb, pad slot zero), A W
+// (4 x n), vectors past meff zero; per-block partials of sum (A w_i)^2 dinv.
+__global__ void __launch_bounds__(kCT)
+k_defl_convert(int n, int nb, const int* __restrict__ meff, const double* __restrict__ Z,
+               const double* __restrict__ KZ, const double* __restrict__ dinv,
+               float* __restrict__ w32, float* __restrict__ aw32, double* __restrict__ part) {
+  __shared__ double sm[4 * (kCT / 32)];
+  const int m = *meff;
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int g = blockIdx.x * kCT + threadIdx.x; g < n; g += gridDim.x * kCT) {
+    const int R = g / 3, q = g - 3 * R;
+    const double di = dinv[g];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const double z = i < m ? Z[static_cast<size_t>(i) * n + g] : 0.0;
+      const double kz = i < m ? KZ[static_cast<size_t>(i) * n + g] : 0.0;
+      w32[(static_cast<size_t>(i) * nb + R) * 4 + q] = static_cast<float>(z);
+      if (q == 0) w32[(static_cast<size_t>(i) * nb + R) * 4 + 3] = 0.f;
+      aw32[static_cast<size_t>(i) * n + g] = static_cast<float>(kz);
+      v[i] = fma(kz * kz, di, v[i]);
+    }
+  }
+  block_sums<4>(v, sm);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) part[static_cast<size_t>(i) * gridDim.x + blockIdx.x] = v[i];
+  }
+}
+
+// (W^T A W)^-1 from the Cholesky factor (zero past meff) and the bounds c_i.
+__global__ void __launch_bounds__(kCT)
+k_defl_finish(int nblk, const int* __restrict__ meff, const double* __restrict__ L,
+              const double* __restrict__ part, float* __restrict__ ginv32,
+              double* __restrict__ cbound) {
+  __shared__ double tot[4];
+  last_block_sums(part, 4, nblk, tot);
+  if (threadIdx.x != 0) return;
+  const int m = min(*meff, 4);
+  for (int i = 0; i < 4; ++i) {
+    // a zero vector gets bound 1: any positive scale (its dots are zero)
+    cbound[i] = (i < m && tot[i] > 0.0) ? sqrt(tot[i]) : 1.0;
+    for (int j = 0; j < 4; ++j) ginv32[i * 4 + j] = 0.f;
+  }
+  for (int j = 0; j < m; ++j) {
+    double x[kCoarseMax] = {};
+    x[j] = 1.0;
+    chol_solve(L, m, x);
+    for (int i = 0; i < m; ++i) ginv32[i * 4 + j] = static_cast<float>(x[i]);
+  }
+}
+
 int coarse_grid(int num_sms) { return num_sms; }
 
 }  // namespace
@@ -552,6 +603,7 @@ bool coarse_basis(CoarseSpace& cs, const float* hist, bool padded,
                   const std::vector<double>& coef, int K, int nb, int m, int num_sms,
                   cudaStream_t s) {
   cs.valid = false;
+  cs.defl_ready = false;
   cs.m = 0;
   if (K < 8 || m <= 0) return false;
   m = std::min(m, kCoarseMax);
@@ -646,6 +698,23 @@ void coarse_apply_panel(const CoarseSpace& cs, double* U, double* R, const doubl
                                               R, dinv, active, norm_f, rel, scale, uD2,
                                               cs.part.ptr, cs.counter.ptr + 1);
   VSGB_LAUNCH_CHECK();
+}
+
+void coarse_deflation_prep(CoarseSpace& cs, const double* dinv, int num_sms, cudaStream_t s) {
+  cs.defl_ready = false;
+  if (!cs.valid) return;
+  const int n = cs.n, nb = n / 3, grid = coarse_grid(num_sms);
+  cs.w32.reserve(static_cast<size_t>(4) * 4 * nb);
+  cs.aw32.reserve(static_cast<size_t>(4) * n);
+  cs.ginv32.reserve(16);
+  cs.cbound.reserve(4);
+  k_defl_convert<<<grid, kCT, 0, s>>>(n, nb, cs.meff.ptr, cs.Z.ptr, cs.KZ.ptr, dinv, cs.w32.ptr,
+                                       cs.aw32.ptr, cs.part.ptr);
+  VSGB_LAUNCH_CHECK();
+  k_defl_finish<<<1, kCT, 0, s>>>(grid, cs.meff.ptr, cs.L.ptr, cs.part.ptr, cs.ginv32.ptr,
+                                   cs.cbound.ptr);
+  VSGB_LAUNCH_CHECK();
+  cs.defl_ready = true;
 }
 
 }  // namespace vsgb

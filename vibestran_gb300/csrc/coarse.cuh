@@ -40,7 +40,16 @@ struct CoarseSpace {
   DevBuf<float> W;           // K x m combination weights of the Lanczos vectors
   std::vector<float> Wh;     // their host copy (pinned by the next copy only)
   std::vector<double> ritz;  // the Ritz values used (smallest first)
+  // deflated FP32 inner solves (resident.cu, 4 vectors, the unused ones
+  // zero): W node-padded, A W, (W^T A W)^-1 and the bounds c_i
+  bool defl_ready = false;
+  DevBuf<float> w32, aw32, ginv32;
+  DevBuf<double> cbound;
 };
+
+// Prepares the FP32 deflation arrays of a built basis (dinv: the Jacobi
+// inverse diagonal, for the bounds c_i^2 = sum_g (A w_i)_g^2 dinv_g).
+void coarse_deflation_prep(CoarseSpace& cs, const double* dinv, int num_sms, cudaStream_t s);
 
 // Lowest m eigenpairs of the symmetric tridiagonal (diag d, off-diagonal e,
 // size k): values ascending in w, vectors column-major in Y (k x m).  Ritz

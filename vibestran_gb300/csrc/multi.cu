@@ -1131,7 +1131,7 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
       // Coarse correction (coarse.cuh) after every FP64 residual; without a
       // basis for this operator the first active column's first inner solve
       // (launch-per-kernel path) records its Lanczos vectors for one.
-      const bool coarse = err_control && coarse_on_;
+      const bool coarse = err_control && coarse_mode_ > 0;
       if (coarse && coarse_.gen != generation_) coarse_.valid = false;
       MultiRecord rec;
       if (coarse && coarse_.gen != generation_ && !tiled)

@@ -1030,9 +1030,30 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
   if (err_control) ensure_diag32(s);
   // Coarse correction (coarse.cuh): the first inner solve on this operator
   // records its Lanczos vectors for the basis.
-  const bool coarse = err_control && coarse_on_ && use_bsr_;
+  const bool coarse = err_control && coarse_mode_ > 0 && use_bsr_;
   const bool record = coarse && coarse_.gen != generation_;
   if (record) coarse_.valid = false;  // a basis of an earlier operator
+  // Deflated first inner solve (coarse_mode_ 2, scalar Jacobi) when an
+  // earlier solve built the basis of this operator: it starts from a residual
+  // the correction made orthogonal to the basis, so u = 0 is corrected first.
+  // Only the first, residual-stopped solve is deflated (deflating the later
+  // steps as well saved no iterations on the 265k-equation cantilever, and a
+  // deflated iteration costs ~10 % more).  Not the default: a basis recorded
+  // from one load can miss a low mode (one of the two near-degenerate bending
+  // modes of a square section, which that load barely excited), and after a
+  // deflated first step the error can sit in that mode, where the estimate
+  // of the next step does not see it: 2 of 19 load cases of the 40x16x16
+  // heterogeneous block ended at 1e-6 and 3e-6 for a 1e-6 target.
+  const bool deflate =
+      coarse && coarse_mode_ == 2 && !bj && res_.win32 && res_.defl32 && coarse_.valid;
+  if (deflate) {
+    if (!coarse_.defl_ready) {
+      coarse_deflation_prep(coarse_, op_->dinv.ptr, num_sms_, s);
+      launches_ += 2;
+    }
+    coarse_apply(coarse_, u_.ptr, r_.ptr, op_->dinv.ptr, scal_.ptr + 1, num_sms_, s);
+    launches_ += 2;
+  }
   const int hist_max = std::min(kCoarseHistMax, max_iters + 1);
   if (record) {
     hist_.reserve(static_cast<size_t>(hist_max) * 4 * (n_ / 3));
@@ -1065,6 +1086,12 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
         ctl.hist = hist_.ptr;
         ctl.coef = coef_.ptr;
         ctl.hist_max = hist_max;
+      }
+      if (deflate && step == 0) {
+        ctl.defl_w = coarse_.w32.ptr;
+        ctl.defl_aw = coarse_.aw32.ptr;
+        ctl.defl_ginv = coarse_.ginv32.ptr;
+        ctl.defl_c = coarse_.cbound.ptr;
       }
       if (err_control && step > 0) {
         // refinement step: the correction's error must fall below

@@ -117,9 +117,12 @@ class PcgEngine {
     coords_ = xyz;
     pattern_key_ = pattern_key;
   }
-  // Coarse (Ritz) correction of error-controlled mixed solves (coarse.cuh):
-  // on by default; off for comparisons.
-  void set_coarse(bool on) { coarse_on_ = on; }
+  // Coarse (Ritz) space of error-controlled mixed solves (coarse.cuh): 0
+  // off, 1 (default) the Galerkin correction after every FP64 residual, 2
+  // that and, in later solves with the same operator, a first FP32 inner
+  // solve deflated by the basis (single right-hand sides, scalar Jacobi; the
+  // batched solve takes the correction only).
+  void set_coarse(int mode) { coarse_mode_ = mode; }
   int coarse_size() const { return coarse_.valid ? coarse_.m : 0; }
   // Tiled batched FP32 solve: 0 off (default: the launch-per-kernel path
   // measured faster), 1 automatic (tile size timed on first use of a
@@ -175,7 +178,7 @@ class PcgEngine {
   MultiWork* multi_ = nullptr;  // batched-solve buffers (multi.cu)
   // coarse correction: the basis, and the Lanczos record it is built from
   CoarseSpace coarse_;
-  bool coarse_on_ = true;
+  int coarse_mode_ = 1;
   DevBuf<float> hist_;
   DevBuf<double> coef_;
   DevBuf<PcgScalars> coarse_scal_;  // scratch record of the basis SpMVs

@@ -77,6 +77,14 @@ struct ResArgs {
   float* hist;
   double* coef;
   int hist_max;
+  // deflated FP32 solve (kDM > 0): W (node-padded, kDM x 4 nb), A W (kDM x
+  // n), (W^T A W)^-1 (kDM x kDM) and bounds c_i with |(A w_i).z| <= c_i
+  // sqrt(r.z) (the fixed-point scales of those dots)
+  const float* __restrict__ defl_w;
+  const float* __restrict__ defl_aw;  // staged for the own rows in shared memory behind the window
+  int win_words;                      // 4 x the largest window: start of that copy
+  const float* __restrict__ defl_ginv;
+  const double* __restrict__ defl_c;
 };
 
 // Cost of a slice beyond its steps, in steps, when slice ranges are split
@@ -94,8 +102,21 @@ struct ResArgs {
 // 4 / 8 / 12.
 constexpr int kSliceWeight = 8;
 
-// Window kernels keep p over the window in shared memory between iterations.
+// Window kernels keep p (the deflated solve: q) over the window in shared
+// memory between iterations.
 constexpr bool kKeepWindowP = true;
+
+// Deflated solves (coarse.cuh): kDeflVecs coarse vectors, FP32 mixed
+// solves with the window only.
+constexpr int kDeflVecs = 4;
+constexpr int kDeflThread = 32;  // lane 0 of warp 1 forms the deflation scalars
+template <typename T, bool kWindow, bool kMixed>
+constexpr bool kDeflatable = sizeof(T) == 4 && kWindow && kMixed && kKeepWindowP;
+// Shared memory the deflated solve takes beyond the plan's: A W and W of the
+// own rows.
+inline size_t defl_smem(int rows_max) {
+  return 2 * static_cast<size_t>(kDeflVecs) * rows_max * sizeof(float);
+}
 
 // FP32 solve: alpha and beta divided in FP32 (they are applied as floats), the
 // stopping test as r.r < (tol |b|)^2 with the relative residual formed once
@@ -204,11 +225,11 @@ __device__ bool grid_allreduce(A (&v)[NV], double* partials, int slot, unsigned*
 // (a drop of more than 64x, where the fixed point has too few digits).
 constexpr bool kFusedReductions = true;
 constexpr int kFxSlots = 4;          // reductions in flight before a word is reused
-constexpr int kFxWords = 4;          // words per slot (2 values, 2 words each in the FP64 solve)
+constexpr int kFxWords = 8;          // words per slot (6 values in the deflated FP32 solve)
 constexpr int kFxScaleBits = 36;
 constexpr double kFxPartMax = 549755813888.0;   // 2^39
 constexpr long long kFxTotalMin = 1LL << 30;
-constexpr int kFxPartSlot = 64;      // sm[64..65]: the CTA's FP64 partials (sm holds 96)
+constexpr int kFxPartSlot = 96;      // sm[96..103]: the CTA's FP64 partials (sm holds 112)
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
   unsigned long long v;
@@ -258,6 +279,33 @@ __device__ __forceinline__ int fx_scale(double prev, bool& usable) {
   return usable ? kFxScaleBits - (ex - 1023) : 0;
 }
 
+// Warp totals of NV <= 8 values with 9 shuffles instead of 5 NV: a butterfly
+// that halves the values each lane carries (8 -> 4 -> 2 -> 1 at offsets 16,
+// 8, 4), then two plain steps.  Lane L ends with the total of value
+// 4 b4 + 2 b3 + b2 (bits of L); the lanes with L % 4 == 0 store it to out.
+// The order of the additions is fixed, so the totals are reproducible.
+template <int NV, typename TV>
+__device__ __forceinline__ void warp_sums_to(const TV (&v)[NV], TV* out) {
+  static_assert(NV <= 8, "at most 8 values");
+  const int lane = threadIdx.x & 31;
+  TV a8[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a8[k] = k < NV ? v[k] : TV(0);
+  const bool h4 = (lane & 16) != 0, h3 = (lane & 8) != 0, h2 = (lane & 4) != 0;
+  TV a4[4], a2[2];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    a4[k] = (h4 ? a8[k + 4] : a8[k]) + __shfl_xor_sync(0xffffffffu, h4 ? a8[k] : a8[k + 4], 16);
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    a2[k] = (h3 ? a4[k + 2] : a4[k]) + __shfl_xor_sync(0xffffffffu, h3 ? a4[k] : a4[k + 2], 8);
+  TV a1 = (h2 ? a2[1] : a2[0]) + __shfl_xor_sync(0xffffffffu, h2 ? a2[0] : a2[1], 4);
+  a1 += __shfl_xor_sync(0xffffffffu, a1, 2);
+  a1 += __shfl_xor_sync(0xffffffffu, a1, 1);
+  const int k = (h4 ? 4 : 0) + (h3 ? 2 : 0) + (h2 ? 1 : 0);
+  if ((lane & 3) == 0 && k < NV) out[k] = a1;
+}
+
 // grid_allreduce for the FP32 solve over the fused words of reduction `red`
 // (ring slot red % kFxSlots of kFxWords words, NV of them used): prev[k] > 0 is the previous total
 // of value k (<= 0: none, fall back).  CTA 0 clears the slot two reductions
@@ -276,7 +324,10 @@ __device__ __forceinline__ int fx_scale(double prev, bool& usable) {
 // at most 255 CTAs stays below 2^40), so the total carries ~68 bits below
 // the previous total's leading bit and no FP64 partial sum is needed after
 // the barrier.
-template <int NV, int kW = kResWarps, bool kRelease = true, typename TV, typename Fin>
+// Values from kMinChk on may fall far below their scale (the deflation dots,
+// scaled by a bound): they skip the "total fell more than 64x" fallback.
+template <int NV, int kW = kResWarps, bool kRelease = true, int kMinChk = NV, typename TV,
+          typename Fin>
 __device__ bool grid_allreduce_fx(TV (&v)[NV], const double (&prev)[NV], double* partials,
                                   int slot, unsigned long long* fx, int red, int* abort_flag,
                                   double* sm, int* s_ok, int* s_fb, double* s_tot,
@@ -288,11 +339,15 @@ __device__ bool grid_allreduce_fx(TV (&v)[NV], const double (&prev)[NV], double*
   TV* smv = reinterpret_cast<TV*>(sm);
   if (kW > 0) {
     if (wid < kW) {
+      if constexpr (NV > 2 && sizeof(TV) == 4) {
+        warp_sums_to(v, smv + wid * NV);  // the deflated solve's 6 values
+      } else {
 #pragma unroll
-      for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
-      if (lane == 0)
+        for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+        if (lane == 0)
 #pragma unroll
-        for (int k = 0; k < NV; ++k) smv[wid * NV + k] = v[k];
+          for (int k = 0; k < NV; ++k) smv[wid * NV + k] = v[k];
+      }
     }
     __syncthreads();
   }
@@ -394,7 +449,8 @@ __device__ bool grid_allreduce_fx(TV (&v)[NV], const double (&prev)[NV], double*
       for (int k = 0; k < NV; ++k) {
         const unsigned long long g = got[kWpv * k];
         const long long q = static_cast<long long>(g) >> 16;
-        if (((g >> 8) & 0xFFull) != 0ull || (q < kFxTotalMin && q > -kFxTotalMin)) fb = 1;
+        if (((g >> 8) & 0xFFull) != 0ull || (k < kMinChk && q < kFxTotalMin && q > -kFxTotalMin))
+          fb = 1;
         double t = static_cast<double>(q);
         if (kSplit)
           t += static_cast<double>(got[kWpv * k + 1] >> 16) * (1.0 / 4294967296.0);
@@ -500,13 +556,22 @@ __device__ __forceinline__ void bj_apply(const T* __restrict__ b, const T (&r)[3
 // kBJ: 3x3 block Jacobi (z = B_I r_I per node) instead of the scalar one; the
 // fourth own-row vector then holds z itself instead of diag^-1, and the row
 // loops of the init and of phase 2 run over nodes.
-template <typename T, bool kWindow, bool kMixed, bool kBJ>
+// kDM > 0 (FP32 mixed, scalar Jacobi, window): deflated PCG (Saad, Yeung,
+// Erhel & Guyomarc'h 2000) with kDM coarse vectors W: the start residual is
+// W-orthogonal (the coarse correction before the solve) and every direction
+// is made A-orthogonal to W, p = z + beta p - W mu, mu = (W^T A W)^-1 (A W)^T z.
+// The window carries the undeflated recurrence q = z + beta q instead, so
+// that no CTA needs W beyond its own rows: p = q - W nu with nu = mu + beta nu
+// (kDM scalars), and A p = A q - (A W) nu on the own rows, whose W and A W
+// sit in shared memory.  The dots (A W)^T z ride on the second reduction.
+template <typename T, bool kWindow, bool kMixed, bool kBJ, int kDM>
 __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double red[96];
+  __shared__ double red[112];
   __shared__ int s_ok;
   __shared__ int s_fb;         // fused reduction fell back to the partials
-  __shared__ double s_tot[2];  // totals of a fused reduction
+  __shared__ double s_tot[6];  // totals of a fused reduction
+  __shared__ float s_nu[kDM > 0 ? kDM : 1];  // deflation coefficients of the direction
   __shared__ int s_next;  // next slice handed to a warp in phase 1
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int c = blockIdx.x;
@@ -524,6 +589,9 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   T* SL = D + (a.u_glob ? 1 : 2) * a.rows_max;  // per-slice p.Ap sums (slices are handed out dynamically)
   T* SLm = SL + slot_half(a.rows_max);           // per-slice p.Mp sums (error-controlled solve)
   T* win = SL + slot_count(a.rows_max);  // 4 per node when kWindow
+  // deflated solve: A W and W of the own rows (kDM x rows_max each)
+  float* AWs = reinterpret_cast<float*>(win + a.win_words);
+  float* WOs = AWs + kDM * a.rows_max;
   const bool err_on = a.err_mode != kErrOff;
   // Phase 2 (u, r, z and the r.z, r.r partials): all warps in the FP32
   // solve; in the FP64 solve kP2Warps of them, which keep the FP64 pipe as
@@ -538,7 +606,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   const double scale = kMixed ? a.O->scale : 1.0;
 
   // ── init: r = rhs, u = 0, z = r / diag, p = 0 ──
-  T acc2[2] = {T(0), T(0)};
+  T acc2[2 + kDM] = {};
   if (kBJ) {
     for (int ln = tid; 3 * ln < nrows; ln += kResThreads) {
       const int lr = 3 * ln, R = 8 * s0 + ln;
@@ -581,6 +649,15 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     D[lr] = dv;
     a.z4[4 * R + q] = zv;
     if (kMixed && a.hist) a.hist[4 * R + q] = static_cast<float>(zv);
+    if constexpr (kDM > 0) {
+#pragma unroll
+      for (int i = 0; i < kDM; ++i) {
+        const float w = __ldg(a.defl_aw + static_cast<size_t>(i) * a.n + g);
+        AWs[i * a.rows_max + lr] = w;
+        WOs[i * a.rows_max + lr] = __ldg(a.defl_w + (static_cast<size_t>(i) * a.nb + R) * 4 + q);
+        acc2[2 + i] = rfma(w, zv, acc2[2 + i]);
+      }
+    }
     a.p4a[4 * R + q] = T(0);
     a.p4b[4 * R + q] = T(0);
     acc2[0] = rfma(rv, rv, acc2[0]);
@@ -600,6 +677,42 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   // targets, thread 0 only (every CTA computes the same values).
   __shared__ ErrEst s_err;
   __shared__ double s_err_t2, s_err_rel2;
+  // Deflation: (W^T A W)^-1, the bounds c_i and the dots (A W)^T z of the
+  // last reduction, which thread 0 leaves for kDeflThread
+  __shared__ float s_ginv[kDM > 0 ? kDM * kDM : 1];
+  __shared__ float s_dc[kDM > 0 ? kDM : 1];
+  __shared__ double s_dt[kDM > 0 ? kDM : 1];
+  __shared__ double s_dsc[kDM > 0 ? kDM : 1];  // c_i sqrt(r.z): scales of the next dots
+  if constexpr (kDM > 0) {
+    if (tid == kDeflThread) {
+      for (int i = 0; i < kDM * kDM; ++i) s_ginv[i] = a.defl_ginv[i];
+      for (int i = 0; i < kDM; ++i) {
+        s_dc[i] = static_cast<float>(a.defl_c[i]);
+        s_nu[i] = 0.f;
+      }
+    }
+  }
+  // kDeflThread, in phase 1 (off thread 0's scalar path; the SpMV that needs
+  // nu follows the phase's barrier): mu = (W^T A W)^-1 (A W)^T z,
+  // nu = mu + beta nu (the direction is p = q - W nu) and the scales of the
+  // next dots from r.z
+  auto defl_next = [&]() {
+    if constexpr (kDM > 0) {
+      float tf[kDM];
+#pragma unroll
+      for (int j = 0; j < kDM; ++j) tf[j] = static_cast<float>(s_dt[j]);
+      const float sr = sqrtf(fabsf(static_cast<float>(rz)));
+      const float tbn = static_cast<float>(s_sc[1]);
+#pragma unroll
+      for (int i = 0; i < kDM; ++i) {
+        float mu = 0.f;
+#pragma unroll
+        for (int j = 0; j < kDM; ++j) mu = fmaf(s_ginv[i * kDM + j], tf[j], mu);
+        s_nu[i] = fmaf(tbn, s_nu[i], mu);
+        s_dsc[i] = static_cast<double>(s_dc[i] * sr);
+      }
+    }
+  };
   if (tid == 0) {
     norm_b = rz = pAp = rr = beta = alpha = rr_stop = pMp = 0.0;
     rel = 1.0;
@@ -618,8 +731,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   int fx_red = 0;  // fused reductions done (FP32)
   T* p_old = a.p4a;
   T* p_new = a.p4b;
-  ok = grid_allreduce<T, 2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red, &s_ok,
-                            a.spin_limit, [&](const double (&t)[2], bool good) {
+  ok = grid_allreduce<T, 2 + kDM>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
+                                  &s_ok, a.spin_limit, [&](const double (&t)[2 + kDM], bool good) {
+                              if constexpr (kDM > 0) {
+                                for (int j = 0; j < kDM; ++j) s_dt[j] = t[2 + j];
+                              }
                               norm_b = sqrt(fabs(t[0]));
                               rz = t[1];
                               rr = t[0];
@@ -670,6 +786,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     tick(-1);
     const T tb = static_cast<T>(s_sc[1]);
     if (tid == 0) s_next = kResWarps;
+    if (kDM > 0 && tid == kDeflThread) defl_next();
     if (!kWindow) __syncthreads();
     if (kWindow) {
       // kFill nodes per thread per round: all their loads are in flight
@@ -796,11 +913,23 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         const int lr = 24 * ls + 3 * r + q;
         const T yq = q == 0 ? y0 : (q == 1 ? y1 : y2);
         // z = r diag^-1 (or the stored block Jacobi z), as in z4
-        const T pn = rfma(tb, P[lr], kBJ ? D[lr] : RR[lr] * D[lr]);
+        T pn, apn = yq;
+        if constexpr (kDM > 0) {
+          // the window holds q (own rows lie in it): p = q - W nu, Ap = Aq - (A W) nu
+          pn = win[4 * (R - wb) + q];
+#pragma unroll
+          for (int i = 0; i < kDM; ++i) {
+            const float nu = s_nu[i];
+            pn = fmaf(-nu, WOs[i * a.rows_max + lr], pn);
+            apn = fmaf(-nu, AWs[i * a.rows_max + lr], apn);
+          }
+        } else {
+          pn = rfma(tb, P[lr], kBJ ? D[lr] : RR[lr] * D[lr]);
+        }
         P[lr] = pn;
-        AP[lr] = yq;
+        AP[lr] = apn;
         if (!(kWindow && kKeepWindowP)) p_new[4 * R + q] = pn;
-        part = pn * yq;
+        part = pn * apn;
         pf = static_cast<float>(pn);
       }
       // p.Mp for the error estimate, in FP32 (an estimate needs no more):
@@ -921,7 +1050,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
     if (flags & kFlagDone) break;
     const T ta = static_cast<T>(s_sc[0]);
     // ── phase 2: u, r, z updates on the own rows ──
-    acc2[0] = acc2[1] = T(0);
+#pragma unroll
+    for (int k = 0; k < 2 + kDM; ++k) acc2[k] = T(0);
     if (kBJ) {
       for (int ln = tid; tid < kP2Threads && 3 * ln < nrows; ln += kP2Threads) {
         const int lr = 3 * ln, R = 8 * s0 + ln;
@@ -947,7 +1077,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         }
       }
     }
-    for (int lr = tid; !kBJ && tid < kP2Threads && lr < nrows; lr += kP2Threads) {
+    auto p2row = [&](int lr) {
       const int g = g0 + lr;
       const int R = g / 3, q = g - 3 * R;
       U[lr] = rfma(ta, P[lr], U[lr]);
@@ -957,12 +1087,23 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       a.z4[4 * R + q] = zv;
       if (kMixed && a.hist && it + 1 < a.hist_max)
         a.hist[static_cast<size_t>(it + 1) * 4 * a.nb + 4 * R + q] = static_cast<float>(zv);
+      if constexpr (kDM > 0) {
+#pragma unroll
+        for (int i = 0; i < kDM; ++i) acc2[2 + i] = rfma(AWs[i * a.rows_max + lr], zv, acc2[2 + i]);
+      }
       acc2[0] = rfma(rv, zv, acc2[0]);
       acc2[1] = rfma(rv, rv, acc2[1]);
+    };
+    // (the deflated form is kept rolled: unrolled, its extra dots spill)
+    if constexpr (kDM > 0) {
+#pragma unroll 1
+      for (int lr = tid; lr < nrows; lr += kP2Threads) p2row(lr);
+    } else {
+      for (int lr = tid; !kBJ && tid < kP2Threads && lr < nrows; lr += kP2Threads) p2row(lr);
     }
     ++it;
     tick(5);
-    auto fin2 = [&](const double (&t)[2], bool good) {
+    auto fin2 = [&](const double (&t)[2 + kDM], bool good) {
       if (!good) {
         flags |= kFlagDone | kFlagAbort;
       } else {
@@ -1001,19 +1142,27 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
           a.coef[3 * it + 2] = t[0];
         }
         rz = t[0];
+        if constexpr (kDM > 0) {
+          for (int j = 0; j < kDM; ++j) s_dt[j] = t[2 + j];
+        }
       }
       s_flags = flags;
       s_sc[1] = beta;
     };
     constexpr int kW2 = sizeof(T) == 4 ? kResWarps : kP2Warps;  // warps holding partials
     if (a.fx) {
-      const double prev[2] = {rz, rr};
-      ok = grid_allreduce_fx<2, kW2>(acc2, prev, a.partials, slot, a.fx, fx_red++, a.abort_flag,
-                                     red, &s_ok, &s_fb, s_tot, a.spin_limit, a.count, target,
-                                     fin2);
+      double prev[2 + kDM];
+      prev[0] = rz;
+      prev[1] = rr;
+      // the deflation dots: |(A w_i).z| <= c_i sqrt(r.z) sets their scale
+#pragma unroll
+      for (int i = 0; i < kDM; ++i) prev[2 + i] = s_dsc[i];
+      ok = grid_allreduce_fx<2 + kDM, kW2, true, 2>(acc2, prev, a.partials, slot, a.fx, fx_red++,
+                                                    a.abort_flag, red, &s_ok, &s_fb, s_tot,
+                                                    a.spin_limit, a.count, target, fin2);
     } else {
-      ok = grid_allreduce<T, 2, kW2>(acc2, a.partials, slot, a.count, target, a.abort_flag, red,
-                                     &s_ok, a.spin_limit, fin2);
+      ok = grid_allreduce<T, 2 + kDM, kW2>(acc2, a.partials, slot, a.count, target, a.abort_flag,
+                                           red, &s_ok, a.spin_limit, fin2);
     }
     slot ^= 1;
     flags = s_flags;
@@ -1193,17 +1342,33 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   VSGB_CUDA(cudaMemsetAsync(P.barrier.ptr, 0, sizeof(unsigned), s));
   VSGB_CUDA(cudaMemsetAsync(&S->abort, 0, sizeof(int), s));
   void* args[] = {&a};
-  const void* fn = bj ? reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, true>)
-                      : reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false>);
+  a.defl_w = ctl.defl_w;
+  a.defl_aw = ctl.defl_aw;
+  a.win_words = 4 * P.max_win;
+  a.defl_ginv = ctl.defl_ginv;
+  a.defl_c = ctl.defl_c;
+  const void* fn = bj ? reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, true, 0>)
+                      : reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false, 0>);
+  if (ctl.defl_w && (bj || !P.defl32))
+    throw Error(VSGB_ERR_STATE, "deflated solve: needs the FP32 windowed plan, scalar Jacobi");
+  if constexpr (kDeflatable<T, kWindow, kMixed>) {
+    if (ctl.defl_w) {
+      fn = reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false, kDeflVecs>);
+      smem += defl_smem(a.rows_max);
+    }
+  } else {
+    if (ctl.defl_w) throw Error(VSGB_ERR_STATE, "deflated solve: needs the FP32 windowed plan");
+  }
   VSGB_CUDA(cudaLaunchCooperativeKernel(fn, dim3(P.ctas), dim3(kResThreads), args, smem, s));
 }
 
 // Both preconditioner forms of a kernel take the same shared memory; the plan
-// holds when both fit one CTA per SM.
+// holds when both fit one CTA per SM.  The deflated form (more shared memory)
+// is optional: *defl says whether it fits too.
 template <typename T, bool kWindow, bool kMixed>
-bool configure(size_t smem, int* blocks) {
-  const void* fns[2] = {reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false>),
-                        reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, true>)};
+bool configure(size_t smem, int rows, int* blocks, bool* defl) {
+  const void* fns[2] = {reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false, 0>),
+                        reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, true, 0>)};
   for (const void* fn : fns) {
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem)) != cudaSuccess) {
@@ -1217,6 +1382,19 @@ bool configure(size_t smem, int* blocks) {
       return false;
     }
   }
+  *defl = false;
+  if constexpr (kDeflatable<T, kWindow, kMixed>) {
+    const void* fn =
+        reinterpret_cast<const void*>(k_resident_pcg<T, kWindow, kMixed, false, kDeflVecs>);
+    int b = 0;
+    const size_t sd = smem + defl_smem(rows);
+    *defl = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sd)) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, kResThreads, sd) ==
+                cudaSuccess &&
+            b >= 1;
+    if (!*defl) cudaGetLastError();
+  }
   return true;
 }
 
@@ -1225,6 +1403,7 @@ bool configure(size_t smem, int* blocks) {
 void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, ResidentPlan& P,
                       cudaStream_t s) {
   P.ok32 = P.ok64 = false;
+  P.defl32 = false;
   if (!B.valid || B.nslices < num_sms) return;
   int coop = 0;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess ||
@@ -1282,13 +1461,14 @@ void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, Re
   P.ctas = G;
   P.threads = kResThreads;
   P.max_slices = max_slices;
+  P.max_win = max_win;
   P.cta_slice.reserve(static_cast<size_t>(G) + 1);
   P.cta_win.reserve(2 * static_cast<size_t>(G));
   VSGB_CUDA(cudaMemcpyAsync(P.cta_slice.ptr, cs.data(), sizeof(int) * (G + 1),
                             cudaMemcpyHostToDevice, s));
   VSGB_CUDA(cudaMemcpyAsync(P.cta_win.ptr, win.data(), sizeof(int) * 2 * G,
                             cudaMemcpyHostToDevice, s));
-  P.partials.reserve(2 * static_cast<size_t>(G) * 2);
+  P.partials.reserve(2 * static_cast<size_t>(G) * (2 + kDeflVecs));  // 2 slots x CTAs x values
   P.fx.reserve(kFxSlots * kFxWords);
   P.barrier.reserve(1);
   const size_t rows = 24 * static_cast<size_t>(max_slices);
@@ -1299,7 +1479,7 @@ void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, Re
   // order: window with u in shared memory, window with u in global memory,
   // then the same two without the window.
   auto plan = [&](size_t elem, auto cfg_win, auto cfg_nowin, bool& ok, bool& win, bool& ug,
-                  size_t& smem) {
+                  bool& defl, size_t& smem) {
     const size_t slots = slot_count(static_cast<int>(rows));
     const size_t w = 4 * static_cast<size_t>(max_win) * elem;
     int blocks = 0;
@@ -1307,15 +1487,18 @@ void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, Re
       const bool want_win = mode < 2, u_global = (mode & 1) != 0;
       const size_t bytes = ((u_global ? 4 : 5) * rows + slots) * elem + (want_win ? w : 0);
       if (!fit(bytes)) continue;
-      if (!(want_win ? cfg_win(bytes, &blocks) : cfg_nowin(bytes, &blocks))) continue;
+      const int r = static_cast<int>(rows);
+      if (!(want_win ? cfg_win(bytes, r, &blocks, &defl) : cfg_nowin(bytes, r, &blocks, &defl)))
+        continue;
       ok = true;
       win = want_win;
       ug = u_global;
       smem = bytes;
     }
   };
+  bool defl64 = false, defl32 = false;
   plan(sizeof(double), configure<double, true, false>, configure<double, false, false>, P.ok64,
-       P.win64, P.ug64, P.smem64);
+       P.win64, P.ug64, defl64, P.smem64);
   if (P.ok64) {
     P.z4d.reserve(nodes4);
     P.p4da.reserve(nodes4);
@@ -1326,7 +1509,8 @@ void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, Re
   }
   if (need32 && B.has32) {
     plan(sizeof(float), configure<float, true, true>, configure<float, false, true>, P.ok32,
-         P.win32, P.ug32, P.smem32);
+         P.win32, P.ug32, defl32, P.smem32);
+    P.defl32 = P.win32 && defl32;
     if (P.ok32) {
       P.z4f.reserve(nodes4);
       P.p4fa.reserve(nodes4);

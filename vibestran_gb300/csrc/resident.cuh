@@ -15,13 +15,15 @@ struct ResidentPlan {
   bool ok32 = false, ok64 = false;  // usable for FP32 inner / FP64 solves
   bool win32 = false, win64 = false;  // x window staged in shared memory
   bool ug32 = false, ug64 = false;    // solution accumulator in global memory
+  bool defl32 = false;                // the deflated FP32 solve fits the plan too
   int ctas = 0, threads = 0;
   size_t smem32 = 0, smem64 = 0;
   int max_slices = 0;               // slices of the largest CTA range
+  int max_win = 0;                  // nodes of the largest x window
   DevBuf<int> cta_slice;            // ctas + 1: slice range of each CTA
   DevBuf<int> cta_win;              // 2 * ctas: [first, last] block column per CTA
   DevBuf<int> slice_mm;             // 2 * nslices: column range per slice (planning scratch)
-  DevBuf<double> partials;          // 2 barrier slots x ctas x up to 4 values
+  DevBuf<double> partials;          // 2 barrier slots x ctas x up to 6 values
   DevBuf<unsigned> barrier;         // monotonic arrival counter
   DevBuf<unsigned long long> fx;    // FP32 solve: fused reduction words
   DevBuf<float> u32g;                       // FP32 solution accumulator when ug32
@@ -58,6 +60,13 @@ struct ResidentCtl {
   float* hist = nullptr;
   double* coef = nullptr;
   int hist_max = 0;
+  // FP32 solve deflated by 4 coarse vectors (null: off; coarse.cuh): W
+  // node-padded (4 x 4 nb), A W (4 x n), (W^T A W)^-1 (4 x 4) and bounds c_i
+  // with |(A w_i).z| <= c_i sqrt(r.z)
+  const float* defl_w = nullptr;
+  const float* defl_aw = nullptr;
+  const float* defl_ginv = nullptr;
+  const double* defl_c = nullptr;
 };
 
 // Plans CTA ranges / windows and allocates the padded vectors; leaves both
