@@ -29,6 +29,35 @@ int sturm_count(const std::vector<double>& d, const std::vector<double>& e, doub
   return cnt;
 }
 
+// The same count for ns shifts at once (e2 = e^2): the recurrences of kSturmW
+// shifts advance together, so their divisions overlap instead of forming one
+// serial chain per count (a count is latency-bound: K dependent divisions).
+// Each count equals sturm_count's for the same shift.
+constexpr int kSturmW = 8;
+void sturm_counts(const std::vector<double>& d, const std::vector<double>& e2,
+                  const double* sig, int ns, int* cnt) {
+  const size_t k = d.size();
+  for (int g = 0; g < ns; g += kSturmW) {
+    double s[kSturmW], q[kSturmW];
+    int c[kSturmW];
+    for (int u = 0; u < kSturmW; ++u) {
+      s[u] = sig[g + (g + u < ns ? u : 0)];
+      q[u] = d[0] - s[u];
+      c[u] = 0;
+    }
+    for (size_t j = 0;; ++j) {
+      for (int u = 0; u < kSturmW; ++u) c[u] += q[u] < 0.0 ? 1 : 0;
+      if (j + 1 == k) break;
+      const double dj = d[j + 1], ej = e2[j];
+      for (int u = 0; u < kSturmW; ++u) {
+        const double qq = q[u] == 0.0 ? 1e-300 : q[u];
+        q[u] = dj - s[u] - ej / qq;
+      }
+    }
+    for (int u = 0; u < kSturmW && g + u < ns; ++u) cnt[g + u] = c[u];
+  }
+}
+
 // Solves (T - sigma I) x = b for a tridiagonal T by Gaussian elimination
 // with partial pivoting (x overwrites b); zero pivots are replaced by a tiny
 // value, as inverse iteration wants.
@@ -88,38 +117,83 @@ void tridiag_shifted_solve(const std::vector<double>& d, const std::vector<doubl
 
 // Z[i][g] = sum_k W[k][i] hist[k][g'] (g' = 4 R + q for g = 3 R + q when
 // the record is node-padded, else g), i < m.
+// FP32 sums: Z only has to span the low modes to the Ritz vectors' accuracy
+// (~1e-2); the Galerkin correction is exact for whatever Z holds, as K Z is
+// formed from it in FP64.  GB300's FP64 rate would make this pass (K x m FMAs
+// per DOF) the most expensive part of the basis.
+// The pass streams the whole record (K x 16 bytes per node: 0.4 GB for 285
+// iterations at 88 560 nodes), so it is HBM-bound: the node-padded form reads
+// one 16-byte record entry per node and iteration (a thread per node, kRitzAhead
+// entries in flight) with the weights in shared memory.
+constexpr int kRitzAhead = 8;
 __global__ void __launch_bounds__(kCT)
-k_ritz_combine(int n, int nb, int K, int m, const float* __restrict__ hist, int padded,
-               const float* __restrict__ W, double* __restrict__ Z) {
-  const size_t stride = padded ? 4 * static_cast<size_t>(nb) : static_cast<size_t>(n);
-  // FP32 sums: Z only has to span the low modes to the Ritz vectors'
-  // accuracy (~1e-2); the Galerkin correction is exact for whatever Z holds,
-  // as K Z is formed from it in FP64.  GB300's FP64 rate would make this
-  // pass (K x m FMAs per DOF) the most expensive part of the basis.
+k_ritz_combine4(int nb, int K, int m, const float4* __restrict__ hist,
+                const float* __restrict__ W, double* __restrict__ Z) {
+  __shared__ float sw[kCoarseHistMax * kCoarseMax];
+  for (int t = threadIdx.x; t < K * m; t += kCT) sw[t] = W[t];
+  __syncthreads();
+  const size_t n = 3 * static_cast<size_t>(nb);
+  for (int R = blockIdx.x * kCT + threadIdx.x; R < nb; R += gridDim.x * kCT) {
+    float acc[kCoarseMax][3];
+#pragma unroll
+    for (int i = 0; i < kCoarseMax; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
+    const float4* h = hist + R;
+    for (int k0 = 0; k0 < K; k0 += kRitzAhead) {
+      float4 v[kRitzAhead];
+#pragma unroll
+      for (int u = 0; u < kRitzAhead; ++u)
+        v[u] = k0 + u < K ? __ldcs(h + static_cast<size_t>(k0 + u) * nb)
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < kRitzAhead; ++u) {
+        if (k0 + u >= K) break;
+        const float* wk = sw + (k0 + u) * m;
+#pragma unroll
+        for (int i = 0; i < kCoarseMax; ++i)
+          if (i < m) {
+            const float w = wk[i];
+            acc[i][0] = fmaf(w, v[u].x, acc[i][0]);
+            acc[i][1] = fmaf(w, v[u].y, acc[i][1]);
+            acc[i][2] = fmaf(w, v[u].z, acc[i][2]);
+          }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kCoarseMax; ++i)
+      if (i < m)
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+          Z[static_cast<size_t>(i) * n + 3 * static_cast<size_t>(R) + q] =
+              static_cast<double>(acc[i][q]);
+  }
+}
+
+// The same for a record of n floats per iteration (the batched solve's):
+// a thread per DOF.
+__global__ void __launch_bounds__(kCT)
+k_ritz_combine(int n, int K, int m, const float* __restrict__ hist, const float* __restrict__ W,
+               double* __restrict__ Z) {
+  __shared__ float sw[kCoarseHistMax * kCoarseMax];
+  for (int t = threadIdx.x; t < K * m; t += kCT) sw[t] = W[t];
+  __syncthreads();
   for (int g = blockIdx.x * kCT + threadIdx.x; g < n; g += gridDim.x * kCT) {
-    const int R = g / 3, q = g - 3 * R;
     float acc[kCoarseMax];
 #pragma unroll
     for (int i = 0; i < kCoarseMax; ++i) acc[i] = 0.f;
-    const float* h = hist + (padded ? 4 * static_cast<size_t>(R) + q : static_cast<size_t>(g));
-    // eight records in flight per thread (one load each would leave the
-    // pass bound by memory latency)
-    int k = 0;
-    for (; k + 8 <= K; k += 8) {
-      float v[8];
+    const float* h = hist + g;
+    for (int k0 = 0; k0 < K; k0 += kRitzAhead) {
+      float v[kRitzAhead];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = __ldg(h + static_cast<size_t>(k + u) * stride);
+      for (int u = 0; u < kRitzAhead; ++u)
+        v[u] = k0 + u < K ? __ldcs(h + static_cast<size_t>(k0 + u) * n) : 0.f;
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
+      for (int u = 0; u < kRitzAhead; ++u) {
+        if (k0 + u >= K) break;
+        const float* wk = sw + (k0 + u) * m;
 #pragma unroll
         for (int i = 0; i < kCoarseMax; ++i)
-          if (i < m) acc[i] = fmaf(__ldg(W + (k + u) * m + i), v[u], acc[i]);
-    }
-    for (; k < K; ++k) {
-      const float v = __ldg(h + static_cast<size_t>(k) * stride);
-#pragma unroll
-      for (int i = 0; i < kCoarseMax; ++i)
-        if (i < m) acc[i] = fmaf(__ldg(W + k * m + i), v, acc[i]);
+          if (i < m) acc[i] = fmaf(wk[i], v[u], acc[i]);
+      }
     }
 #pragma unroll
     for (int i = 0; i < kCoarseMax; ++i)
@@ -540,13 +614,54 @@ int tridiag_lowest(const std::vector<double>& d, const std::vector<double>& e, i
     hi = std::max(hi, d[i] + r);
   }
   const double span = std::max(std::fabs(lo), std::fabs(hi));
-  // Each value: bisection on Sturm counts to 1e-4 of the value (a serial
-  // chain of divisions per count: the host's cost), then inverse iteration
-  // with Rayleigh-quotient shifts, cubically convergent from there; the
-  // copies of a converged value (finite-precision Lanczos) are skipped with
-  // one count.
+  auto open = [span](double a, double b) {
+    return b - a > 1e-4 * std::max(std::fabs(a), std::fabs(b)) && b - a > 1e-16 * span;
+  };
+  // Each value: bisection on Sturm counts to 1e-4 of the value, then inverse
+  // iteration with Rayleigh-quotient shifts, cubically convergent from there;
+  // the copies of a converged value (finite-precision Lanczos) are skipped
+  // with one count.
+  // The brackets of the L = 2m lowest eigenvalues (by index) are bisected
+  // together: a round counts at every open bracket's midpoint with the
+  // recurrences interleaved (sturm_counts), and every count narrows every
+  // bracket (count > j: eigenvalue j lies below the shift).  A serial
+  // bisection per value spent ~0.5 ms of host time here for m = 4 at K = 285.
+  const int L = std::min(k, 2 * m);
+  std::vector<double> e2(e.size());
+  for (size_t j = 0; j < e.size(); ++j) e2[j] = e[j] * e[j];
+  std::vector<double> ba(static_cast<size_t>(L), lo), bb(static_cast<size_t>(L), hi), mids;
+  std::vector<int> cnts;
+  for (int round = 0; round < 200; ++round) {
+    // the distinct open brackets (indices j share one until a count splits
+    // them), each cut at p interior points so that a round counts at about
+    // kSturmW shifts
+    mids.clear();
+    int nopen = 0;
+    for (int j = 0; j < L; ++j)
+      if (open(ba[j], bb[j]) && (j == 0 || ba[j] != ba[j - 1] || bb[j] != bb[j - 1])) ++nopen;
+    if (nopen == 0) break;
+    const int p = std::max(1, kSturmW / nopen);
+    for (int j = 0; j < L; ++j)
+      if (open(ba[j], bb[j]) && (j == 0 || ba[j] != ba[j - 1] || bb[j] != bb[j - 1]))
+        for (int i = 1; i <= p; ++i) mids.push_back(ba[j] + (bb[j] - ba[j]) * i / (p + 1));
+    cnts.resize(mids.size());
+    sturm_counts(d, e2, mids.data(), static_cast<int>(mids.size()), cnts.data());
+    for (size_t t = 0; t < mids.size(); ++t)
+      for (int j = 0; j < L; ++j) {
+        if (cnts[t] > j)
+          bb[j] = std::min(bb[j], mids[t]);
+        else
+          ba[j] = std::max(ba[j], mids[t]);
+      }
+  }
   std::vector<double> vals;
-  for (int idx = 0; idx < k && static_cast<int>(vals.size()) < m;) {
+  int idx = 0;
+  while (idx < L && static_cast<int>(vals.size()) < m) {
+    vals.push_back(0.5 * (ba[idx] + bb[idx]));
+    idx = std::max(idx + 1, sturm_count(d, e, bb[idx] + 1e-6 * std::fabs(bb[idx])));
+  }
+  // (more copies than the L brackets held: the rest one value at a time)
+  while (idx < k && static_cast<int>(vals.size()) < m) {
     double a = vals.empty() ? lo : vals.back(), b = hi;
     if (sturm_count(d, e, a) > idx) a = lo;
     for (int it = 0; it < 200 && b - a > 1e-4 * std::max(std::fabs(a), std::fabs(b)) &&
@@ -579,7 +694,11 @@ int tridiag_lowest(const std::vector<double>& d, const std::vector<double>& e, i
         if (i + 1 < k) t += e[i] * y[i + 1];
         rq += y[i] * t;
       }
+      // cubic convergence: once the shift stands still, more solves only
+      // polish y below what the FP32 record resolves
+      const bool settled = rep > 0 && std::fabs(rq - th) <= 1e-12 * std::fabs(th);
       th = rq;
+      if (settled) break;
     }
     // orthogonalise against the vectors kept (a near-duplicate pair)
     const size_t cols = w.size();
@@ -650,8 +769,12 @@ bool coarse_basis(CoarseSpace& cs, const float* hist, bool padded,
   cs.W.reserve(static_cast<size_t>(kCoarseHistMax) * kCoarseMax);
   VSGB_CUDA(cudaMemcpyAsync(cs.W.ptr, cs.Wh.data(), sizeof(float) * cs.Wh.size(),
                             cudaMemcpyHostToDevice, s));
-  k_ritz_combine<<<coarse_grid(num_sms) * 2, kCT, 0, s>>>(n, nb, K, found, hist, padded ? 1 : 0,
-                                                          cs.W.ptr, cs.Z.ptr);
+  if (padded)
+    k_ritz_combine4<<<(nb + kCT - 1) / kCT, kCT, 0, s>>>(nb, K, found,
+                                                       reinterpret_cast<const float4*>(hist),
+                                                       cs.W.ptr, cs.Z.ptr);
+  else
+    k_ritz_combine<<<(n + kCT - 1) / kCT, kCT, 0, s>>>(n, K, found, hist, cs.W.ptr, cs.Z.ptr);
   VSGB_LAUNCH_CHECK();
   return true;
 }

@@ -60,12 +60,13 @@ int tridiag_lowest(const std::vector<double>& d, const std::vector<double>& e, i
 
 // Builds the basis from a Lanczos record: hist (K slots of 4 * nb floats,
 // node-padded, or of n = 3 nb floats), coef (alpha_k, beta_k, r_k.z_k for
-// k < K).  spmv64(x, y) applies the FP64 operator.  False (and cs.valid
+// k < K).  spmm64(Z, KZ, m) applies the FP64 operator to the m basis
+// vectors (vector i at i * n, m <= 4).  False (and cs.valid
 // false) when fewer than 8 iterations were recorded, the recurrence is not
 // that of an SPD solve, or no positive-definite coarse matrix resulted.
-template <typename SpMV>
+template <typename SpMM>
 bool coarse_build(CoarseSpace& cs, const float* hist, bool padded,
-                  const std::vector<double>& coef, int K, int nb, int m, SpMV&& spmv64,
+                  const std::vector<double>& coef, int K, int nb, int m, SpMM&& spmm64,
                   int num_sms, cudaStream_t s);
 
 // Galerkin correction of one FP64 iterate: u += Z c, r -= K Z c with
@@ -87,13 +88,12 @@ bool coarse_basis(CoarseSpace& cs, const float* hist, bool padded,
                   const std::vector<double>& coef, int K, int nb, int m, int num_sms,
                   cudaStream_t s);
 
-template <typename SpMV>
+template <typename SpMM>
 bool coarse_build(CoarseSpace& cs, const float* hist, bool padded,
-                  const std::vector<double>& coef, int K, int nb, int m, SpMV&& spmv64,
+                  const std::vector<double>& coef, int K, int nb, int m, SpMM&& spmm64,
                   int num_sms, cudaStream_t s) {
   if (!coarse_basis(cs, hist, padded, coef, K, nb, m, num_sms, s)) return false;
-  for (int i = 0; i < cs.m; ++i)
-    spmv64(cs.Z.ptr + static_cast<size_t>(i) * cs.n, cs.KZ.ptr + static_cast<size_t>(i) * cs.n);
+  spmm64(cs.Z.ptr, cs.KZ.ptr, cs.m);
   return coarse_finish(cs, num_sms, s);
 }
 

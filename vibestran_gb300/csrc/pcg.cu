@@ -497,6 +497,53 @@ k_bsr_spmv64(BsrView B, const double* __restrict__ vals, const double* __restric
   }
 }
 
+// K X for M vectors at once (vector v at X + v n, result at Y + v n): the
+// coarse basis products K Z.  The FP64 operator is read once for all M
+// vectors; per vector the arithmetic and its order are those of
+// bsr_row_block, so each column equals a k_bsr_spmv64 product bit for bit.
+template <int M>
+__global__ void __launch_bounds__(kSpmvThreads)
+k_bsr_spmm64_cols(BsrView B, const double* __restrict__ vals, const double* __restrict__ X,
+                  double* __restrict__ Y, int n) {
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  for (int sl = blockIdx.x * wpb + (threadIdx.x >> 5); sl < B.nslices; sl += gridDim.x * wpb) {
+    const int base = B.slice_ptr[sl], steps = B.slice_ptr[sl + 1] - base;
+    const int* cp = B.cols + static_cast<size_t>(base) * 32 + lane;
+    const double* vp = vals + static_cast<size_t>(base) * 288 + lane;
+    double y[M][3];
+#pragma unroll
+    for (int v = 0; v < M; ++v) y[v][0] = y[v][1] = y[v][2] = 0.0;
+    for (int t = 0; t < steps; ++t) {
+      const int c = __ldcg(cp + 32 * t);
+      double a[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a[k] = __ldcg(vp + 288 * t + 32 * k);
+#pragma unroll
+      for (int v = 0; v < M; ++v) {
+        const double* x = X + static_cast<size_t>(v) * n + 3 * static_cast<size_t>(c);
+        const double x0 = __ldg(x), x1 = __ldg(x + 1), x2 = __ldg(x + 2);
+        y[v][0] = fma(a[0], x0, fma(a[1], x1, fma(a[2], x2, y[v][0])));
+        y[v][1] = fma(a[3], x0, fma(a[4], x1, fma(a[5], x2, y[v][1])));
+        y[v][2] = fma(a[6], x0, fma(a[7], x1, fma(a[8], x2, y[v][2])));
+      }
+    }
+    const int R = sl * 8 + (lane >> 2), q = lane & 3;
+#pragma unroll
+    for (int v = 0; v < M; ++v) {
+#pragma unroll
+      for (int o = 1; o <= 2; o <<= 1) {
+        y[v][0] += __shfl_xor_sync(0xffffffffu, y[v][0], o);
+        y[v][1] += __shfl_xor_sync(0xffffffffu, y[v][1], o);
+        y[v][2] += __shfl_xor_sync(0xffffffffu, y[v][2], o);
+      }
+      if (R < B.nb && q < 3)
+        Y[static_cast<size_t>(v) * n + 3 * static_cast<size_t>(R) + q] =
+            q == 0 ? y[v][0] : (q == 1 ? y[v][1] : y[v][2]);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kSpmvThreads)
 k_bsr_spmv32_fused(BsrView B, const float* __restrict__ vals, const float* __restrict__ z,
                    const float* __restrict__ p_old, float* __restrict__ p_new,
@@ -898,20 +945,17 @@ void PcgEngine::coarse_from_record(int count, cudaStream_t s, bool padded) {
   VSGB_CUDA(cudaMemcpyAsync(coef_h_.data(), coef_.ptr, sizeof(double) * coef_h_.size(),
                             cudaMemcpyDeviceToHost, s));
   VSGB_CUDA(cudaStreamSynchronize(s));
-  // K z with a scratch record (the SpMV kernel skips its work once the
-  // record it is given reports done, as the inner record now does)
-  coarse_scal_.reserve(1);
-  VSGB_CUDA(cudaMemsetAsync(coarse_scal_.ptr, 0, sizeof(PcgScalars), s));
   coarse_build(coarse_, hist_.ptr, padded, coef_h_, count, n_ / 3, 4,
-               [&](const double* x, double* y) {
-                 k_bsr_spmv64<<<bsr_grid_, kSpmvThreads, 0, s>>>(
-                     view_of(bsr_), bsr_.val64.ptr, x, y, coarse_scal_.ptr, partials_.ptr,
-                     counters_.ptr + 1);
+               [&](const double* X, double* Y, int m) {
+                 // the basis has at most 4 vectors here (m requested above)
+                 auto fn = m <= 2 ? (m <= 1 ? k_bsr_spmm64_cols<1> : k_bsr_spmm64_cols<2>)
+                                  : (m <= 3 ? k_bsr_spmm64_cols<3> : k_bsr_spmm64_cols<4>);
+                 fn<<<bsr_grid_, kSpmvThreads, 0, s>>>(view_of(bsr_), bsr_.val64.ptr, X, Y, n_);
                  VSGB_LAUNCH_CHECK();
                  ++launches_;
                },
                num_sms_, s);
-  launches_ += 2;
+  launches_ += 3;  // k_ritz_combine*, k_gram, k_coarse_chol
 }
 
 void PcgEngine::ensure_diag32(cudaStream_t s) {

@@ -181,7 +181,6 @@ class PcgEngine {
   int coarse_mode_ = 1;
   DevBuf<float> hist_;
   DevBuf<double> coef_;
-  DevBuf<PcgScalars> coarse_scal_;  // scratch record of the basis SpMVs
   std::vector<double> coef_h_;
   // the first inner solve of an operator records its Lanczos vectors; this
   // builds the basis from them (count = iterations recorded)
