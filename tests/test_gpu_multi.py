@@ -148,3 +148,33 @@ def test_batched_error_controlled_defaults(vsgb, multi_model):
     for k in range(N_CASES):
         assert _rel(U64[:, k], U[:, k]) <= 1e-6, k
     be.close()
+
+
+def test_batched_single_launch_loop_matches_host_batches(vsgb, multi_model):
+    """Each batched inner solve is one graph launch whose WHILE node runs the
+    iterations on the device (k_mloop); without graphs the host launches
+    batches of check_every iterations and reads the state after each.  The
+    kernels and their order are the same, so the solutions are the same bits,
+    FP64 and mixed, for any batch size; max_iters still bounds the loop."""
+    m, eq6, n, F, U = multi_model
+    G = F[:, :16]
+    for mixed, tol in ((False, 1e-10), (True, 1e-8)):
+        be, asm = _assembled(vsgb, m, eq6, n, mixed, tol, True, inner=1e-3 if mixed else 0.0)
+        U_loop = asm.solve(G)
+        it_loop = [be.rhs_stats(k)["iterations"] for k in range(16)]
+        be.set_option(vsgb.OPT_CHECK_EVERY, 6)
+        assert np.array_equal(asm.solve(G), U_loop), mixed
+        be.set_option(vsgb.OPT_USE_GRAPH, 0)
+        U_host = asm.solve(G)
+        assert np.array_equal(U_host, U_loop), mixed
+        assert [be.rhs_stats(k)["iterations"] for k in range(16)] == it_loop
+        for k in range(16):
+            assert _rel(U_loop[:, k], U[:, k]) <= (1e-6 if mixed else 1e-8), (mixed, k)
+        be.close()
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-12, 7)
+    be.set_option(vsgb.OPT_BATCHED, 2)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    with pytest.raises(vsgb.SolverError, match="did not converge after 7 iterations"):
+        asm.solve(G[:, :4])
+    be.close()

@@ -751,6 +751,17 @@ k_maccumulate(int n, double* __restrict__ u64, const float* __restrict__ d32,
     u64[i] = fma(static_cast<double>(d32[i]), inv, u64[i]);
 }
 
+// Loop control of the single-launch batched inner solve: the kernel that
+// closes each body (check_every iterations) of the solve graph's WHILE node.
+// The body runs again while a column is active (S->done, set by k_mupdate at
+// max_iters at the latest), and never more than max_rounds times: the round
+// count, zeroed by the graph before the loop, bounds the loop by itself.
+__global__ void k_mloop(MultiState* S, unsigned max_rounds, cudaGraphConditionalHandle h) {
+  const unsigned r = S->loop_rounds + 1u;
+  S->loop_rounds = r;
+  cudaGraphSetConditional(h, (S->done == 0 && r < max_rounds) ? 1u : 0u);
+}
+
 }  // namespace
 
 }  // namespace vsgb
@@ -780,11 +791,20 @@ struct MultiWork {
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   unsigned exec_epoch[2] = {0, 0};
   int exec_batch[2] = {0, 0};
+  // single-launch inner solves: graph of a WHILE node around check_every
+  // iterations (FP64 / FP32), its key, and whether the driver refused one
+  cudaGraphExec_t lexec[2] = {nullptr, nullptr};
+  unsigned lexec_epoch[2] = {0, 0};
+  int lexec_batch[2] = {0, 0};
+  long long lexec_rounds[2] = {0, 0};
+  bool loop_off = false;
   unsigned epoch = 1;     // bumped whenever a buffer moves or the operator changes
   unsigned op_gen = 0;    // operator generation the buffers were sized for
 
   ~MultiWork() {
     for (auto& g : exec)
+      if (g) cudaGraphExecDestroy(g);
+    for (auto& g : lexec)
       if (g) cudaGraphExecDestroy(g);
     if (hS) cudaFreeHost(hS);
     if (hO) cudaFreeHost(hO);
@@ -1016,7 +1036,7 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
     VSGB_CUDA(cudaMemcpyAsync(W.hO, W.O.ptr, sizeof(MultiOuter), cudaMemcpyDeviceToHost, s));
     VSGB_CUDA(cudaStreamSynchronize(s));
   };
-  auto batch = [&](bool fp32, const MultiRecord& rec) {
+  auto iters = [&](bool fp32, const MultiRecord& rec) {
     for (int k = 0; k < check_every_; ++k) {
       if (fp32)
         launch_multi_iter<float, 16>(B, bsr_.val32.ptr, dinv32_.ptr, diag32, W.r32.ptr,
@@ -1027,7 +1047,82 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
                                      W.u64.ptr, W.p64.ptr, W.Ap64.ptr, W, n_, g64, vgrid, s);
     }
     VSGB_LAUNCH_CHECK();
+  };
+  auto batch = [&](bool fp32, const MultiRecord& rec) {
+    iters(fp32, rec);
     VSGB_CUDA(cudaMemcpyAsync(W.hS, W.S.ptr, sizeof(MultiState), cudaMemcpyDeviceToHost, s));
+  };
+  // The whole inner solve as one graph launch: a memset of the round count,
+  // then a WHILE node whose body is check_every iterations and k_mloop, which
+  // keeps the body running on the device while a column is active (no host
+  // round trip inside a solve).  Cached per key, buffers, batch size and round
+  // bound; false (and the batch loop below from then on) when the driver
+  // refuses any part of it.
+  auto ensure_loop_graph = [&](int key, bool fp32, long long max_rounds) -> bool {
+    if (W.lexec[key] && W.lexec_epoch[key] == W.epoch && W.lexec_batch[key] == check_every_ &&
+        W.lexec_rounds[key] == max_rounds)
+      return true;
+    if (W.lexec[key]) {
+      cudaGraphExecDestroy(W.lexec[key]);
+      W.lexec[key] = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    bool ok = false, capturing = false;
+    try {
+      do {
+        if (cudaGraphCreate(&g, 0) != cudaSuccess) break;
+        cudaGraphConditionalHandle h;
+        if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+          break;
+        cudaMemsetParams mp = {};
+        mp.dst = &W.S.ptr->loop_rounds;
+        mp.value = 0;
+        mp.elementSize = sizeof(unsigned);
+        mp.width = 1;
+        mp.height = 1;
+        mp.pitch = sizeof(unsigned);
+        cudaGraphNode_t n0 = nullptr, n1 = nullptr;
+        if (cudaGraphAddMemsetNode(&n0, g, nullptr, 0, &mp) != cudaSuccess) break;
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        if (cudaGraphAddNode(&n1, g, &n0, nullptr, 1, &cp) != cudaSuccess) break;
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        if (cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+          break;
+        capturing = true;
+        iters(fp32, MultiRecord{});
+        k_mloop<<<1, 1, 0, s>>>(W.S.ptr, static_cast<unsigned>(max_rounds), h);
+        cudaGraph_t done_body = nullptr;
+        capturing = false;
+        if (cudaStreamEndCapture(s, &done_body) != cudaSuccess) break;
+        if (cudaGraphInstantiate(&W.lexec[key], g, 0) != cudaSuccess) {
+          W.lexec[key] = nullptr;
+          break;
+        }
+        ok = true;
+      } while (false);
+    } catch (...) {
+      if (capturing) {
+        cudaGraph_t t = nullptr;
+        cudaStreamEndCapture(s, &t);
+      }
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+      cudaGetLastError();  // the refusal is not sticky: fall back
+      W.loop_off = true;
+      return false;
+    }
+    W.lexec_epoch[key] = W.epoch;
+    W.lexec_batch[key] = check_every_;
+    W.lexec_rounds[key] = max_rounds;
+    return true;
   };
   // Batches of check_every iterations (a cached CUDA graph) until every
   // column reports done; the device stops itself at max_iters.
@@ -1035,6 +1130,16 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
   auto iterate_all = [&](bool fp32, const MultiRecord& rec = MultiRecord{}) {
     const int key = fp32 ? 1 : 0;
     const bool graph = use_graph_ && rec.hist == nullptr;
+    const long long max_rounds = (static_cast<long long>(max_iters) + check_every_ - 1) /
+                                     check_every_ + 4;
+    if (graph && !W.loop_off && ensure_loop_graph(key, fp32, max_rounds)) {
+      VSGB_CUDA(cudaGraphLaunch(W.lexec[key], s));
+      read_state();
+      launches_ += (3LL * check_every_ + 1) * W.hS->loop_rounds;
+      if (!W.hS->done)
+        throw Error(VSGB_ERR_CUDA, "batched PCG device state did not report completion");
+      return;
+    }
     if (graph && (W.exec[key] == nullptr || W.exec_epoch[key] != W.epoch ||
                        W.exec_batch[key] != check_every_)) {
       if (W.exec[key]) {
@@ -1098,10 +1203,15 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
           W.partials.ptr, W.counters.ptr);
       VSGB_LAUNCH_CHECK();
       ++launches_;
+      if (!use_graph_ || W.loop_off) {
+        read_state();
+        check_start();
+        if (!W.hS->done) iterate_all(false);
+      } else {
+        iterate_all(false);  // one launch, also when init finished every column
+      }
       read_state();
       check_start();
-      if (!W.hS->done) iterate_all(false);
-      read_state();
       if (err_control) read_est();
       for (int k = 0; k < nc; ++k) {
         SolveResult& R = res[static_cast<size_t>(k0 + k)];
@@ -1230,10 +1340,15 @@ void PcgEngine::solve_multi(const double* d_F, int nrhs, double* d_U, bool mixed
               inner_tol, outer, max_iters, W.partials.ptr, W.counters.ptr, r0);
           VSGB_LAUNCH_CHECK();
           ++launches_;
+          if (!use_graph_ || W.loop_off || r0.hist) {
+            read_state();
+            check_start();
+            if (!W.hS->done) iterate_all(true, r0);
+          } else {
+            iterate_all(true, r0);  // one launch, also when init finished every column
+          }
           read_state();
           check_start();
-          if (!W.hS->done) iterate_all(true, r0);
-          read_state();
           if (r0.hist && (W.hS->flags[r0.col] & kFlagConverged))
             coarse_from_record(std::min(W.hS->iters[r0.col], r0.max), s, false);
         }

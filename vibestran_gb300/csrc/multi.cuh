@@ -32,6 +32,8 @@ struct MultiState {
   double err_t2[kP];
   double err_rel2;
   double err_norm2[kP];
+  // bodies run by the device-side loop of the single-launch inner solve
+  unsigned loop_rounds;
 };
 
 struct MultiOuter {
