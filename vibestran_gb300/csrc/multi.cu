@@ -121,6 +121,108 @@ __device__ __forceinline__ bool mcol_sum_last(double (&acc)[Q][R], int cb, doubl
   return true;
 }
 
+// The FP32 solve's form of mcol_sum_last: acc holds FP32 sums, the warp and
+// block sums stay in FP32 and the block partials are stored as FP32; the last
+// block adds each column's partials as a double-float pair (Knuth's TwoSum,
+// ~48 significant bits) and converts once per column.  On GB300 a warp-wide
+// FP64 instruction costs the SM ~16 cycles whatever its active lanes, so the
+// FP64 form spent ~260 FP64 warp instructions per block on its shuffle sums
+// and conversions and ~1 400 in the last block (1 216 partials x 32
+// columns), all at the end of the kernel, where the blocks finish together.
+// Same fixed order everywhere: reproducible bit for bit.
+__device__ __forceinline__ void two_sum_acc(float& s, float& e, float x) {
+  const float t = __fadd_rn(s, x);
+  const float bp = __fsub_rn(t, s);
+  const float er = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+  s = t;
+  e = __fadd_rn(e, er);
+}
+
+template <int Q, int R, int BT>
+__device__ __forceinline__ bool mcol_sum_last32(float (&acc)[Q][R], int cb, double* partials,
+                                                unsigned* counter, float* s_red /* BT */,
+                                                double* s_tot /* Q * kP */) {
+  constexpr int QM = Q * kP;
+  constexpr int NW = BT / 32;
+  static_assert(2 * QM <= BT && NW * QM <= BT, "reduction shape");
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < Q; ++q)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      float v = acc[q][r];
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 8);
+      v += __shfl_xor_sync(0xffffffffu, v, 16);
+      acc[q][r] = v;
+    }
+  for (int t = threadIdx.x; t < NW * QM; t += BT) s_red[t] = 0.f;
+  __syncthreads();
+  if (lane < 4)
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+      for (int r = 0; r < R; ++r) s_red[(wid * Q + q) * kP + cb + r] = acc[q][r];
+  __syncthreads();
+  const int nblk = gridDim.x * gridDim.y;
+  const int b = blockIdx.y * gridDim.x + blockIdx.x;
+  float* pf = reinterpret_cast<float*>(partials);  // column t at pf + t * nblk
+  if (threadIdx.x < QM) {
+    float sum = 0.f;
+    for (int w = 0; w < NW; ++w) sum += s_red[w * QM + threadIdx.x];
+    pf[static_cast<size_t>(threadIdx.x) * nblk + b] = sum;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == static_cast<unsigned>(nblk - 1));
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  for (int col = wid; col < QM; col += NW) {
+    const float* pc = pf + static_cast<size_t>(col) * nblk;
+    float sum = 0.f, err = 0.f;
+    for (int b0 = lane; b0 < nblk; b0 += 256) {
+      float v[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) v[m] = (b0 + 32 * m < nblk) ? __ldcg(pc + b0 + 32 * m) : 0.f;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) two_sum_acc(sum, err, v[m]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float so = __shfl_xor_sync(0xffffffffu, sum, o);
+      const float eo = __shfl_xor_sync(0xffffffffu, err, o);
+      two_sum_acc(sum, err, so);
+      err = __fadd_rn(err, eo);
+    }
+    if (lane == 0) {
+      s_red[col] = sum;
+      s_red[QM + col] = err;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < QM)
+    s_tot[threadIdx.x] = static_cast<double>(s_red[threadIdx.x]) +
+                         static_cast<double>(s_red[QM + threadIdx.x]);
+  __syncthreads();
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+// mcol_sum_last in the accumulators' precision
+template <int Q, int R, int BT, typename A>
+__device__ __forceinline__ bool mcol_sum(A (&acc)[Q][R], int cb, double* partials,
+                                         unsigned* counter, double* s_red /* BT */,
+                                         double* s_tot /* Q * kP */) {
+  if constexpr (sizeof(A) == 4) {
+    return mcol_sum_last32<Q, R, BT>(acc, cb, partials, counter, reinterpret_cast<float*>(s_red),
+                                     s_tot);
+  } else {
+    return mcol_sum_last<Q, R, BT>(acc, cb, partials, counter, s_red, s_tot);
+  }
+}
+
 __device__ __forceinline__ void all_done(MultiState* S) {
   int all = 1;
   for (int k = 0; k < kP; ++k) all &= (S->flags[k] & kFlagDone) ? 1 : 0;
@@ -290,7 +392,7 @@ __device__ __forceinline__ void mspmm_slice(const MView& B, const T* __restrict_
 // Ap = K p for the columns of block row group blockIdx.y; p.Ap per column,
 // then alpha = rz / p.Ap (breakdown when p.Ap <= 0, as cuda_pcg_backend_impl.hpp:688-694).
 template <typename T, int G>
-__global__ void __launch_bounds__(kMT)
+__global__ void __launch_bounds__(kMT, sizeof(T) == 4 ? 3 : 1)
 k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restrict__ Ap,
         const float* __restrict__ diag32, MultiState* S, ErrEst* est, double* partials,
         unsigned* counter) {
@@ -338,13 +440,13 @@ k_mspmm(MView B, const T* __restrict__ vals, const T* __restrict__ p, T* __restr
       }
     }
   }
-  double a[2][RN];
+  T a[2][RN];
 #pragma unroll
   for (int r = 0; r < RN; ++r) {
-    a[0][r] = static_cast<double>(pap[r]);
-    a[1][r] = static_cast<double>(pmp[r]);
+    a[0][r] = pap[r];
+    a[1][r] = static_cast<T>(pmp[r]);
   }
-  if (mcol_sum_last<2, RN, kMT>(a, cb, partials, counter, s_red, s_tot)) {
+  if (mcol_sum<2, RN, kMT>(a, cb, partials, counter, s_red, s_tot)) {
     if (threadIdx.x < kP) {
       const int k = threadIdx.x;
       int f = S->flags[k];
@@ -555,13 +657,13 @@ k_minit(int n, int ncols, const double* __restrict__ src, const MultiOuter* O,
     st4(u + o, zero);
     st4(p + o, zv);
   }
-  double a[2][4];
+  T a[2][4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    a[0][j] = static_cast<double>(rz[j]);
-    a[1][j] = static_cast<double>(rr[j]);
+    a[0][j] = rz[j];
+    a[1][j] = rr[j];
   }
-  if (mcol_sum_last<2, 4, kVT>(a, cb, partials, counter, s_red, s_tot)) {
+  if (mcol_sum<2, 4, kVT>(a, cb, partials, counter, s_red, s_tot)) {
     if (threadIdx.x < kP) {
       const int k = threadIdx.x;
       const double rzk = s_tot[k], rrk = s_tot[kP + k], nb = sqrt(fabs(rrk));
@@ -653,13 +755,13 @@ k_mupdate(int n, T* __restrict__ u, T* __restrict__ r, const T* __restrict__ p,
     st4(u + o, uv);
     st4(r + o, rv);
   }
-  double a[2][4];
+  T a[2][4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    a[0][j] = static_cast<double>(rz[j]);
-    a[1][j] = static_cast<double>(rr[j]);
+    a[0][j] = rz[j];
+    a[1][j] = rr[j];
   }
-  if (mcol_sum_last<2, 4, kVT>(a, cb, partials, counter, s_red, s_tot)) {
+  if (mcol_sum<2, 4, kVT>(a, cb, partials, counter, s_red, s_tot)) {
     if (threadIdx.x < kP) {
       const int k = threadIdx.x;
       int fl = S->flags[k];
