@@ -41,6 +41,7 @@ struct ResArgs {
   const T* __restrict__ vals;
   const int* __restrict__ cta_slice;
   const int* __restrict__ cta_win;
+  const int* __restrict__ cta_runs;  // kRunStride per CTA: referenced runs of the window
   const double* __restrict__ dinv;
   const T* __restrict__ bj;  // 3x3 block Jacobi: inverse diagonal blocks, 6 per node
   const double* __restrict__ rhs;
@@ -105,6 +106,12 @@ constexpr int kSliceWeight = 8;
 // Window kernels keep p (the deflated solve: q) over the window in shared
 // memory between iterations.
 constexpr bool kKeepWindowP = true;
+
+// Window gather over the referenced runs of the window (k_window_runs): at
+// most kWinRuns runs per CTA, gaps under kRunGap nodes merged.
+constexpr int kWinRuns = 16;
+constexpr int kRunGap = 32;
+constexpr int kRunStride = 1 + 2 * kWinRuns;
 
 // Deflated solves (coarse.cuh): kDeflVecs coarse vectors, FP32 mixed
 // solves with the window only.
@@ -600,6 +607,20 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   constexpr int kP2Warps = sizeof(T) == 8 ? 4 : kResWarps;
   constexpr int kP2Threads = 32 * kP2Warps;
   const int wb = a.cta_win[2 * c], we = a.cta_win[2 * c + 1];
+  // referenced runs of the window: starts and cumulative lengths
+  __shared__ int s_rs[kWinRuns], s_rc[kWinRuns + 1], s_nrun;
+  if (kWindow && tid == 0) {
+    const int* rr = a.cta_runs + static_cast<size_t>(c) * kRunStride;
+    const int nr = min(max(rr[0], 0), kWinRuns);
+    int acc = 0;
+    s_rc[0] = 0;
+    for (int i = 0; i < nr; ++i) {
+      s_rs[i] = rr[1 + 2 * i];
+      acc += rr[2 + 2 * i] - rr[1 + 2 * i];
+      s_rc[i + 1] = acc;
+    }
+    s_nrun = nr;
+  }
   unsigned target = 0;
   int slot = 0;
   bool ok = true;
@@ -794,13 +815,25 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
       // With kKeepWindowP the window already holds p_k of every window node
       // (each CTA forms p = z + beta p for them with the operands and order of
       // the owner, so the copies are bitwise the owner's): only z is read.
+      // Only the runs of the window that the CTA's columns reference
+      // (k_window_runs): entry t of their concatenation is node
+      // s_rs[i] + t - s_rc[i] of run i.
       constexpr int kFill = 4;
-      for (int j0 = wb + tid; j0 <= we; j0 += kFill * kResThreads) {
+      const int total = s_rc[s_nrun];
+      for (int t0 = tid; t0 < total; t0 += kFill * kResThreads) {
         T z[kFill][3], q[kFill][3];
+        int jj[kFill];
 #pragma unroll
         for (int u = 0; u < kFill; ++u) {
-          const int j = j0 + u * kResThreads;
-          if (j <= we) {
+          const int t = t0 + u * kResThreads;
+          int j = -1;
+          if (t < total) {
+            int i = 0;
+            while (t >= s_rc[i + 1]) ++i;
+            j = s_rs[i] + (t - s_rc[i]);
+          }
+          jj[u] = j;
+          if (j >= 0) {
             ld3(a.z4 + 4 * static_cast<size_t>(j), z[u][0], z[u][1], z[u][2]);
             if (kKeepWindowP)
               lds3(win + 4 * (j - wb), q[u][0], q[u][1], q[u][2]);
@@ -810,8 +843,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
         }
 #pragma unroll
         for (int u = 0; u < kFill; ++u) {
-          const int j = j0 + u * kResThreads;
-          if (j <= we)
+          const int j = jj[u];
+          if (j >= 0)
             st3(win + 4 * (j - wb), rfma(tb, q[u][0], z[u][0]), rfma(tb, q[u][1], z[u][1]),
                 rfma(tb, q[u][2], z[u][2]));
         }
@@ -1238,6 +1271,78 @@ __global__ void k_slice_minmax(int nslices, const int* __restrict__ slice_ptr,
   }
 }
 
+// The runs of a CTA's window that its columns reference: one block per CTA
+// marks every column of its slices (padding included: it points at the
+// slice's own rows) in a shared-memory bitmap over [wb, we], then thread 0
+// turns the bitmap into at most kWinRuns runs, merging runs less than kRunGap
+// nodes apart.  On a structured mesh a CTA's rows are a contiguous node range
+// that reaches one node plane up and down, so the runs are the three plane
+// bands (~2 150 of a 5 700-node window at 84k); the window gather then loads
+// only those.  More runs than kWinRuns: the whole window as one run.
+// runs[c * kRunStride]: count, then (start, end) node pairs, end exclusive.
+__global__ void __launch_bounds__(512)
+k_window_runs(const int* __restrict__ slice_ptr, const int* __restrict__ cols,
+              const int* __restrict__ cta_slice, const int* __restrict__ cta_win,
+              int* __restrict__ runs) {
+  extern __shared__ unsigned bm[];
+  const int c = blockIdx.x;
+  const int wb = cta_win[2 * c], we = cta_win[2 * c + 1];
+  const int nw = (we - wb + 1 + 31) >> 5;
+  for (int w = threadIdx.x; w < nw; w += blockDim.x) bm[w] = 0u;
+  __syncthreads();
+  const long long t0 = static_cast<long long>(slice_ptr[cta_slice[c]]) * 32;
+  const long long t1 = static_cast<long long>(slice_ptr[cta_slice[c + 1]]) * 32;
+  for (long long t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+    const int o = cols[t] - wb;
+    if (o >= 0 && o <= we - wb) atomicOr(&bm[o >> 5], 1u << (o & 31));
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  int* out = runs + static_cast<size_t>(c) * kRunStride;
+  int nr = 0, cs = -1, ce = -1;
+  bool over = false;
+  for (int w = 0; w < nw && !over; ++w) {
+    unsigned b = bm[w];
+    while (b) {
+      const int lo = __ffs(static_cast<int>(b)) - 1;
+      const unsigned above = b | ((1u << lo) - 1u);  // ones through the run
+      const int hi = ~above ? __ffs(static_cast<int>(~above)) - 1 : 32;
+      const int rs = wb + 32 * w + lo, re = wb + 32 * w + hi;
+      if (ce >= 0 && rs - ce <= kRunGap) {
+        ce = re;
+      } else {
+        if (ce >= 0) {
+          if (nr == kWinRuns) {
+            over = true;
+            break;
+          }
+          out[1 + 2 * nr] = cs;
+          out[2 + 2 * nr] = ce;
+          ++nr;
+        }
+        cs = rs;
+        ce = re;
+      }
+      b = hi == 32 ? 0u : (b & ~((1u << hi) - 1u));
+    }
+  }
+  if (!over && ce >= 0) {
+    if (nr == kWinRuns) {
+      over = true;
+    } else {
+      out[1 + 2 * nr] = cs;
+      out[2 + 2 * nr] = ce;
+      ++nr;
+    }
+  }
+  if (over || nr == 0) {
+    nr = 1;
+    out[1] = wb;
+    out[2] = we + 1;
+  }
+  out[0] = nr;
+}
+
 // Thread per node: finds the diagonal block among the node's stored blocks
 // (entries 4t+q < rowlen of its slice row; padding comes after them), and
 // inverts its symmetric part (upper triangle) by cofactors in FP64.  A block
@@ -1300,6 +1405,7 @@ void launch_resident(const BsrSell& B, ResidentPlan& P, const T* vals, const dou
   a.vals = vals;
   a.cta_slice = P.cta_slice.ptr;
   a.cta_win = P.cta_win.ptr;
+  a.cta_runs = P.cta_runs.ptr;
   a.dinv = dinv;
   a.bj = bj;
   a.rhs = rhs;
@@ -1468,6 +1574,26 @@ void resident_prepare(const BsrSell& B, bool need32, int device, int num_sms, Re
                             cudaMemcpyHostToDevice, s));
   VSGB_CUDA(cudaMemcpyAsync(P.cta_win.ptr, win.data(), sizeof(int) * 2 * G,
                             cudaMemcpyHostToDevice, s));
+  P.cta_runs.reserve(static_cast<size_t>(kRunStride) * G);
+  {
+    const size_t bm_bytes = sizeof(unsigned) * ((static_cast<size_t>(max_win) + 31) / 32);
+    if (bm_bytes <= 48 * 1024) {
+      k_window_runs<<<G, 512, bm_bytes, s>>>(B.slice_ptr.ptr, B.cols.ptr, P.cta_slice.ptr,
+                                            P.cta_win.ptr, P.cta_runs.ptr);
+      VSGB_LAUNCH_CHECK();
+    } else {
+      // (a window of more than 393 216 nodes: gather it whole)
+      std::vector<int> whole(static_cast<size_t>(kRunStride) * G, 0);
+      for (int g = 0; g < G; ++g) {
+        whole[static_cast<size_t>(kRunStride) * g] = 1;
+        whole[static_cast<size_t>(kRunStride) * g + 1] = win[2 * g];
+        whole[static_cast<size_t>(kRunStride) * g + 2] = win[2 * g + 1] + 1;
+      }
+      VSGB_CUDA(cudaMemcpyAsync(P.cta_runs.ptr, whole.data(), sizeof(int) * whole.size(),
+                                cudaMemcpyHostToDevice, s));
+      VSGB_CUDA(cudaStreamSynchronize(s));
+    }
+  }
   P.partials.reserve(2 * static_cast<size_t>(G) * (2 + kDeflVecs));  // 2 slots x CTAs x values
   P.fx.reserve(kFxSlots * kFxWords);
   P.barrier.reserve(1);

@@ -22,6 +22,7 @@ struct ResidentPlan {
   int max_win = 0;                  // nodes of the largest x window
   DevBuf<int> cta_slice;            // ctas + 1: slice range of each CTA
   DevBuf<int> cta_win;              // 2 * ctas: [first, last] block column per CTA
+  DevBuf<int> cta_runs;             // per CTA: the runs of its window its columns reference
   DevBuf<int> slice_mm;             // 2 * nslices: column range per slice (planning scratch)
   DevBuf<double> partials;          // 2 barrier slots x ctas x up to 6 values
   DevBuf<unsigned> barrier;         // monotonic arrival counter
