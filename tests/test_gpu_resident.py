@@ -160,3 +160,31 @@ def test_cantilever_84k_jitter_full_size(vsgb, oracle):
         um = asm.solve(F)
         assert rel_err(um) <= 1e-6, l2
     be.close()
+
+
+def test_resident_scrambled_node_numbering(vsgb, oracle):
+    """Randomly numbered nodes: the equations follow the sorted node ids, so a
+    CTA's slices reference columns all over the mesh and its window is nearly
+    every node.  The window gather then takes the whole window (more
+    referenced runs than it keeps) instead of the plane bands of a structured
+    numbering; FP64 and mixed answers as the oracle's."""
+    from vibestran_gb300 import cantilever as C
+    m = C.small_block(24, 8, 8, 0.05, seed=21, jitter=0.15, hetero=True)
+    rng = np.random.default_rng(9)
+    new_ids = (rng.permutation(m.n_nodes) * 3 + 5).astype(np.int32)
+    id_map = dict(zip(m.node_ids.tolist(), new_ids.tolist()))
+    m.node_ids = new_ids
+    m.spc_nodes = np.array([id_map[i] for i in m.spc_nodes.tolist()], np.int32)
+    m.loads = [(np.array([id_map[i] for i in nodes.tolist()], np.int32), s, d)
+               for nodes, s, d in m.loads]
+    eq6, n = vsgb.build_dof_map(m)
+    F = vsgb.apply_forces(m, eq6, n)
+    eq_o, n_o = oracle.dof_map(m)
+    K = oracle.assemble_chexa8(m, eq_o, n_o)
+    uo, _, _ = oracle.pcg_jacobi(K, F, 1e-12, 100000)
+    u64, st64 = _solve(vsgb, m, eq6, n, F, vsgb.FP64, 1, 1e-10)
+    assert st64.kernel_iterations > 0  # the persistent solve ran
+    assert np.linalg.norm(u64 - uo) / np.linalg.norm(uo) <= 1e-8
+    um, stm = _solve(vsgb, m, eq6, n, F, vsgb.MIXED, 1, 1e-8, inner=1e-3)
+    assert stm.kernel_iterations > 0
+    assert np.linalg.norm(um - uo) / np.linalg.norm(uo) <= 1e-6
