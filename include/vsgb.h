@@ -53,11 +53,16 @@ extern "C" {
 #define VSGB_OPT_MAX_ITERS 2      /* max PCG iterations per solve (default 10000) */
 #define VSGB_OPT_PRECISION 3      /* VSGB_FP64 or VSGB_MIXED */
 #define VSGB_OPT_INNER_TOL 4      /* mixed: inner FP32 tolerance (<=0: 1e-3 when error-controlled,
-                                     otherwise clamp(100*tol,1e-4,1e-2) as cuda-pcg-mixed) */
+                                     otherwise clamp(100*tol,1e-4,1e-2) as cuda-pcg-mixed).
+                                     Error-controlled solves should keep the default: below
+                                     1e-3 the bound on the FP32 operator's share of the
+                                     error can miss the target. */
 #define VSGB_OPT_MAX_SOLVES 5     /* mixed: max inner solves (<= 0: default, 3 = 1 + 2
                                      corrections; 5 when error-controlled) */
-#define VSGB_OPT_CHECK_EVERY 6    /* iterations launched between host convergence checks */
-#define VSGB_OPT_USE_GRAPH 7      /* 1: replay iteration batches as CUDA graphs (default 1) */
+#define VSGB_OPT_CHECK_EVERY 6    /* iterations launched between convergence checks (the
+                                     batched solve: per body of its device-side loop) */
+#define VSGB_OPT_USE_GRAPH 7      /* 1: replay iteration batches as CUDA graphs, the batched
+                                     inner solve as one graph launch (default 1) */
 #define VSGB_OPT_FORMAT 8         /* 0 auto, 1 scalar CSR, 2 3x3 node blocks */
 #define VSGB_OPT_RESIDENT 9       /* 1: one persistent launch per PCG solve (default 1) */
 #define VSGB_OPT_BATCHED 10       /* load cases (nrhs > 1) on the 3x3 block operator:
