@@ -932,19 +932,37 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
           }
         }
       }
-#pragma unroll
-      for (int o = 1; o <= 2; o <<= 1) {
-        y0 += __shfl_xor_sync(0xffffffffu, y0, o);
-        y1 += __shfl_xor_sync(0xffffffffu, y1, o);
-        y2 += __shfl_xor_sync(0xffffffffu, y2, o);
-      }
       const int r = lane >> 2, q = lane & 3;
+      T yq;
+      if constexpr (sizeof(T) == 8) {
+        // The row's 4 lanes hold partials of its 3 components.  A butterfly
+        // that halves the values each lane carries leaves lane q with the
+        // total of component q in 3 FP64 adds instead of the 6 of a
+        // reduction of all three (every FP64 warp instruction costs the SM
+        // ~16 cycles whatever its active lanes): over lanes xor 2, lanes 0-1
+        // keep components 0-1 and lanes 2-3 component 2 (and a zero), then
+        // over lanes xor 1 each lane keeps one.
+        const bool h = (lane & 2) != 0, b = (lane & 1) != 0;
+        T k0 = h ? y2 : y0, k1 = h ? T(0) : y1;
+        const T s0 = h ? y0 : y2, s1 = h ? y1 : T(0);
+        k0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+        k1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+        yq = b ? k1 : k0;
+        yq += __shfl_xor_sync(0xffffffffu, b ? k0 : k1, 1);
+      } else {
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+          y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+          y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+          y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+        }
+        yq = q == 0 ? y0 : (q == 1 ? y1 : y2);
+      }
       const int R = 8 * sl + r;
       T part = T(0);
       float pf = 0.f;
       if (q < 3 && R < a.nb) {
         const int lr = 24 * ls + 3 * r + q;
-        const T yq = q == 0 ? y0 : (q == 1 ? y1 : y2);
         // z = r diag^-1 (or the stored block Jacobi z), as in z4
         T pn, apn = yq;
         if constexpr (kDM > 0) {
