@@ -348,6 +348,17 @@ __device__ bool grid_allreduce_fx(TV (&v)[NV], const double (&prev)[NV], double*
     if (wid < kW) {
       if constexpr (NV > 2 && sizeof(TV) == 4) {
         warp_sums_to(v, smv + wid * NV);  // the deflated solve's 6 values
+      } else if constexpr (NV == 2 && sizeof(TV) == 8) {
+        // FP64 pair: lanes 16-31 carry value 1 and lanes 0-15 value 0 after
+        // the first step, so the warp adds 5 times instead of 10 (each
+        // warp-wide FP64 add costs the SM ~16 cycles); lane 0 ends with the
+        // total of value 0, lane 16 with that of value 1
+        const bool hi = (lane & 16) != 0;
+        TV keep = hi ? v[1] : v[0];
+        keep += __shfl_xor_sync(0xffffffffu, hi ? v[0] : v[1], 16);
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+        if ((lane & 15) == 0) smv[wid * NV + (hi ? 1 : 0)] = keep;
       } else {
 #pragma unroll
         for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
@@ -604,7 +615,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_resident_pcg(ResArgs<T> a) {
   // solve; in the FP64 solve kP2Warps of them, which keep the FP64 pipe as
   // busy (the phase is bound by it) and leave a quarter of the warp sums for
   // the reduction.
-  constexpr int kP2Warps = sizeof(T) == 8 ? 4 : kResWarps;
+  constexpr int kP2Warps = sizeof(T) == 8 ? 8 : kResWarps;
   constexpr int kP2Threads = 32 * kP2Warps;
   const int wb = a.cta_win[2 * c], we = a.cta_win[2 * c + 1];
   // referenced runs of the window: starts and cumulative lengths
