@@ -127,8 +127,9 @@ __device__ __forceinline__ bool mcol_sum_last(double (&acc)[Q][R], int cb, doubl
 // ~48 significant bits) and converts once per column.  On GB300 a warp-wide
 // FP64 instruction costs the SM ~16 cycles whatever its active lanes, so the
 // FP64 form spent ~260 FP64 warp instructions per block on its shuffle sums
-// and conversions and ~1 400 in the last block (1 216 partials x 32
-// columns), all at the end of the kernel, where the blocks finish together.
+// and conversions and ~1 400 in the last block (32 columns of one partial per
+// block, 1 216 blocks at 8 per SM), all at the end of the kernel, where the
+// blocks finish together.
 // Same fixed order everywhere: reproducible bit for bit.
 __device__ __forceinline__ void two_sum_acc(float& s, float& e, float x) {
   const float t = __fadd_rn(s, x);
