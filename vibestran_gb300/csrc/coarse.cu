@@ -113,6 +113,74 @@ void tridiag_shifted_solve(const std::vector<double>& d, const std::vector<doubl
   }
 }
 
+// tridiag_shifted_solve for ns shifts at once (vectors b[s], shifts sig[s]):
+// the same operations for each shift, in the same order, with the shifts'
+// elimination chains interleaved row by row so that their divisions overlap.
+void tridiag_shifted_solve_multi(const std::vector<double>& d, const std::vector<double>& e,
+                                 const double* sig, std::vector<double>* const* b, int ns) {
+  const int k = static_cast<int>(d.size());
+  if (k == 1) {
+    for (int t = 0; t < ns; ++t) tridiag_shifted_solve(d, e, sig[t], *b[t]);
+    return;
+  }
+  std::vector<double> a0(static_cast<size_t>(ns) * k), a1(static_cast<size_t>(ns) * k, 0.0),
+      a2(static_cast<size_t>(ns) * k, 0.0);
+  std::vector<double> diag(ns), sup(ns), sup2(ns), tiny(ns);
+  for (int t = 0; t < ns; ++t) {
+    diag[t] = d[0] - sig[t];
+    sup[t] = e[0];
+    sup2[t] = 0.0;
+    double scale = 0.0;
+    for (int i = 0; i < k; ++i) scale = std::max(scale, std::fabs(d[i] - sig[t]));
+    tiny[t] = 1e-300 + 1e-15 * scale;
+  }
+  for (int i = 0; i < k - 1; ++i) {
+    for (int t = 0; t < ns; ++t) {
+      std::vector<double>& bb = *b[t];
+      double* A0 = a0.data() + static_cast<size_t>(t) * k;
+      double* A1 = a1.data() + static_cast<size_t>(t) * k;
+      double* A2 = a2.data() + static_cast<size_t>(t) * k;
+      const double nl = e[i], nd = d[i + 1] - sig[t], nu = (i + 1 < k - 1) ? e[i + 1] : 0.0;
+      if (std::fabs(nl) > std::fabs(diag[t])) {
+        const double f = diag[t] / nl;
+        A0[i] = nl;
+        A1[i] = nd;
+        A2[i] = nu;
+        const double bi = bb[i];
+        bb[i] = bb[i + 1];
+        diag[t] = sup[t] - f * nd;
+        sup[t] = sup2[t] - f * nu;
+        sup2[t] = 0.0;
+        bb[i + 1] = bi - f * bb[i];
+      } else {
+        const double piv = diag[t] != 0.0 ? diag[t] : tiny[t];
+        const double f = nl / piv;
+        A0[i] = piv;
+        A1[i] = sup[t];
+        A2[i] = sup2[t];
+        diag[t] = nd - f * sup[t];
+        sup[t] = nu - f * sup2[t];
+        sup2[t] = 0.0;
+        bb[i + 1] -= f * bb[i];
+      }
+    }
+  }
+  for (int t = 0; t < ns; ++t)
+    a0[static_cast<size_t>(t) * k + k - 1] = diag[t] != 0.0 ? diag[t] : tiny[t];
+  for (int i = k - 1; i >= 0; --i) {
+    for (int t = 0; t < ns; ++t) {
+      std::vector<double>& bb = *b[t];
+      const double* A0 = a0.data() + static_cast<size_t>(t) * k;
+      const double* A1 = a1.data() + static_cast<size_t>(t) * k;
+      const double* A2 = a2.data() + static_cast<size_t>(t) * k;
+      double v = bb[i];
+      if (i + 1 < k) v -= A1[i] * bb[i + 1];
+      if (i + 2 < k) v -= A2[i] * bb[i + 2];
+      bb[i] = v / (A0[i] != 0.0 ? A0[i] : tiny[t]);
+    }
+  }
+}
+
 // ── device kernels ────────────────────────────────────────────────────────
 
 // Z[i][g] = sum_k W[k][i] hist[k][g'] (g' = 4 R + q for g = 3 R + q when
@@ -677,15 +745,36 @@ int tridiag_lowest(const std::vector<double>& d, const std::vector<double>& e, i
     // skip the copies of this value (within 1e-6 past the bracket)
     idx = std::max(idx + 1, sturm_count(d, e, b + 1e-6 * std::fabs(b)));
   }
-  for (double th : vals) {
-    std::vector<double> y(static_cast<size_t>(k));
+  // Inverse iteration with Rayleigh-quotient shifts, the values' solves
+  // interleaved (tridiag_shifted_solve_multi); each value follows the same
+  // sequence of operations it would alone.
+  const int nv = static_cast<int>(vals.size());
+  std::vector<std::vector<double>> ys(static_cast<size_t>(nv), std::vector<double>(static_cast<size_t>(k)));
+  std::vector<double> ths(vals);
+  std::vector<char> live(static_cast<size_t>(nv), 1);
+  for (auto& y : ys)
     for (int i = 0; i < k; ++i) y[i] = 1.0 + 0.001 * ((i * 7919) % 101);  // deterministic start
-    for (int rep = 0; rep < 4; ++rep) {
-      tridiag_shifted_solve(d, e, th, y);
+  for (int rep = 0; rep < 4; ++rep) {
+    std::vector<int> act;
+    for (int v = 0; v < nv; ++v)
+      if (live[v]) act.push_back(v);
+    if (act.empty()) break;
+    std::vector<double> sh(act.size());
+    std::vector<std::vector<double>*> yp(act.size());
+    for (size_t t = 0; t < act.size(); ++t) {
+      sh[t] = ths[act[t]];
+      yp[t] = &ys[act[t]];
+    }
+    tridiag_shifted_solve_multi(d, e, sh.data(), yp.data(), static_cast<int>(act.size()));
+    for (int v : act) {
+      std::vector<double>& y = ys[v];
       double nrm = 0.0;
       for (double x : y) nrm += x * x;
       nrm = std::sqrt(nrm);
-      if (!(nrm > 0.0) || !std::isfinite(nrm)) break;
+      if (!(nrm > 0.0) || !std::isfinite(nrm)) {
+        live[v] = 0;
+        continue;
+      }
       for (double& x : y) x /= nrm;
       double rq = 0.0;  // Rayleigh quotient y^T T y: the next shift
       for (int i = 0; i < k; ++i) {
@@ -696,10 +785,14 @@ int tridiag_lowest(const std::vector<double>& d, const std::vector<double>& e, i
       }
       // cubic convergence: once the shift stands still, more solves only
       // polish y below what the FP32 record resolves
-      const bool settled = rep > 0 && std::fabs(rq - th) <= 1e-12 * std::fabs(th);
-      th = rq;
-      if (settled) break;
+      const bool settled = rep > 0 && std::fabs(rq - ths[v]) <= 1e-12 * std::fabs(ths[v]);
+      ths[v] = rq;
+      if (settled) live[v] = 0;
     }
+  }
+  for (int v = 0; v < nv; ++v) {
+    std::vector<double>& y = ys[v];
+    const double th = ths[v];
     // orthogonalise against the vectors kept (a near-duplicate pair)
     const size_t cols = w.size();
     for (size_t c = 0; c < cols; ++c) {
