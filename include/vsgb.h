@@ -284,6 +284,29 @@ int vsgb_adjoint_gradients(vsgb_ctx* ctx, const double* F, const double* dJdu, d
 int vsgb_solid_stress(vsgb_ctx* ctx, const double* u, int k, double* centroid_out,
                       double* nodal_out, double* kernel_ms);
 
+/* Nodal displacements of the resident mesh (LinearStaticSolver::recover_results,
+ * displacement part, src/solver/linear_static.cpp:574-587): disp_out[6 i + d]
+ * = T1 T2 T3 R1 R2 R3 of node i in the uploaded node order, u[eq] where the
+ * DOF is free and 0 where it is constrained (the rotations always are: solid
+ * elements activate T1-T3 only).  u: n_dof host displacements, or NULL for
+ * load case k of the last solve on this context; disp_out: n_nodes*6 doubles.
+ * The deck subset of this path has no CD frames, so the values stay in the
+ * basic frame (the reference rotates only nodes that name one, :589-612);
+ * vsgb_write_node_csv lists them in ascending node-id order as the reference
+ * does. */
+int vsgb_node_displacements(vsgb_ctx* ctx, const double* u, int k, double* disp_out);
+
+/* The nodal CSV of CsvWriter (src/io/csv_writer.cpp:34-57): the header
+ * "# node_id, subcase_id, T1, T2, T3, R1, R2, R3", then for each subcase s in
+ * the order given and each node in ascending id order the line
+ * "id, subcase, d0, ..., d5" with the values in scientific notation with 8
+ * digits after the point.  disp: n_subcases blocks of n_nodes*6 doubles in
+ * the node order of node_ids (vsgb_node_displacements' output).  Host only.
+ * Returns VSGB_ERR_INVALID with the reference's "Cannot write CSV: <path>"
+ * when the file cannot be opened. */
+int vsgb_write_node_csv(const char* path, int n_nodes, const int* node_ids, int n_subcases,
+                        const int* subcase_ids, const double* disp, char* err, size_t errlen);
+
 /* ── BDF decks (host only, no GPU needed) ────────────────────────────────── */
 
 /* Reader of the deck subset of the SOL 101 CHEXA8 path, in place of

@@ -132,3 +132,60 @@ def test_deck_to_stresses_on_gpu(vsgb, oracle):
     assert sel.sum() == 96
     assert np.all(np.abs(cen[sel, 0] / beam[sel] - 1.0) < 5e-3)
     be.close()
+
+
+@pytest.mark.parametrize("isop", [0, 1])
+def test_node_displacements_axial_single_hex(vsgb, known, isop, tmp_path):
+    """recover_results' displacement part (linear_static.cpp:574-587) on the
+    reference's axial deck: the top-face nodes rise 1e-3 m, node 6 contracts
+    -3e-4 m in x, node 1 stays at 0 in z, and every rotation is 0 (the
+    expectations of chexa8_axial_force.expected.json); the node CSV lists
+    them as CsvWriter does."""
+    spec = known["hexa_bar_axial_extension"]
+    ex = spec["expect"]
+    m = model_from_spec(spec, isop)
+    eq6, n = vsgb.build_dof_map(m)
+    F = vsgb.apply_forces(m, eq6, n)
+    be = vsgb.Gb300PcgSolverBackend.try_create(1e-12, 1000)
+    asm = vsgb.ChexaAssembler(be)
+    asm.assemble(m, eq6, n)
+    u = asm.solve(F)
+    d = asm.node_displacements()  # load case 0 of the last solve
+    assert np.array_equal(d, asm.node_displacements(u))
+    row = {int(nid): i for i, nid in enumerate(m.node_ids)}
+    for nid in ex["uz_top_nodes"]:
+        assert abs(d[row[nid], 2] - ex["uz"]) <= ex["e2e_rel_tol"] * ex["uz"]
+    assert abs(d[row[6], 0] - ex["ux_node6"]) <= ex["e2e_rel_tol"] * abs(ex["ux_node6"])
+    assert d[row[1], 2] == 0.0 and np.all(d[:, 3:] == 0.0)
+    # the free DOFs are the solution itself
+    eq = np.asarray(eq6)[:, :3]
+    assert np.array_equal(d[:, :3][eq >= 0], u[eq[eq >= 0]])
+    path = tmp_path / "axial.node.csv"
+    vsgb.write_node_csv(str(path), m.node_ids, d, [1])
+    lines = path.read_text().splitlines()
+    assert lines[0] == "# node_id, subcase_id, T1, T2, T3, R1, R2, R3" and len(lines) == 9
+    top = [ln for ln in lines[1:] if ln.startswith("5, 1, ")][0]
+    assert abs(float(top.split(", ")[4]) - ex["uz"]) <= 1e-6 * ex["uz"]
+    be.close()
+
+
+def test_node_displacements_match_the_solution_84k(vsgb):
+    """Full-size: every free DOF of the 84 000-element cantilever's nodal
+    output equals its equation's entry of the resident solution, bit for bit,
+    and the constrained ones are 0."""
+    from vibestran_gb300 import cantilever as C
+    m = C.cantilever_84k()
+    eq6, n = vsgb.build_dof_map(m)
+    F = vsgb.apply_forces(m, eq6, n)
+    be = vsgb.Gb300MixedPcgSolverBackend.try_create()
+    asm = vsgb.ChexaAssembler(be)
+    asm.upload(m, eq6, n)
+    asm.assemble_resident()
+    asm.upload_rhs(F)
+    asm.solve_resident()
+    u = asm.download()
+    d = asm.node_displacements()
+    eq = np.asarray(eq6)[:, :3]
+    assert np.array_equal(d[:, :3][eq >= 0], u[eq[eq >= 0]])
+    assert np.all(d[:, :3][eq < 0] == 0.0) and np.all(d[:, 3:] == 0.0)
+    be.close()

@@ -78,7 +78,7 @@ EXPORTS = (
     "vsgb_host_alloc", "vsgb_host_free",
     "vsgb_solution_download", "vsgb_element_sensitivity", "vsgb_timer_start",
     "vsgb_timer_stop", "vsgb_time_spmv", "vsgb_kernel_launches", "vsgb_phase_times",
-    "vsgb_pcg_solve_noalloc",
+    "vsgb_pcg_solve_noalloc", "vsgb_node_displacements", "vsgb_write_node_csv",
 )
 NOALLOC_MAX_N = 65536  # VSGB_NOALLOC_MAX_N
 
@@ -167,6 +167,8 @@ def load_library(build_if_missing: bool = False):
     L.vsgb_phase_times.argtypes = [vp, _f64p]
     L.vsgb_adjoint_gradients.argtypes = [vp, _f64p, vp, vp, vp, vp, vp, ctypes.POINTER(VsgbStats)]
     L.vsgb_solid_stress.argtypes = [vp, vp, c_int, _f64p, vp, ctypes.POINTER(c_dbl)]
+    L.vsgb_node_displacements.argtypes = [vp, vp, c_int, _f64p]
+    L.vsgb_write_node_csv.argtypes = [cp, c_int, _i32p, c_int, _i32p, _f64p, cp, sz]
     L.vsgb_bdf_read.argtypes = [cp, c_int, ctypes.POINTER(vp), cp, sz]
     L.vsgb_bdf_parse.argtypes = [cp, sz, c_int, ctypes.POINTER(vp), cp, sz]
     L.vsgb_bdf_free.argtypes = [vp]
@@ -399,6 +401,7 @@ class ChexaAssembler:
         self.n = 0
         self.nnz_lower = 0
         self.n_elem = 0
+        self.n_nodes = 0
 
     def upload(self, model, eq6, n):
         L = load_library()
@@ -415,6 +418,7 @@ class ChexaAssembler:
         self.backend.context.check(rc)
         self.n = int(n)
         self.n_elem = model.n_elem
+        self.n_nodes = model.n_nodes
 
     def assemble_resident(self) -> int:
         nnz = ctypes.c_longlong()
@@ -490,6 +494,18 @@ class ChexaAssembler:
             None if u_in is None else u_in.ctypes.data_as(ctypes.c_void_p), k, cen,
             None if nod is None else nod.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ms)))
         return cen, nod, ms.value
+
+    def node_displacements(self, u=None, k=0) -> np.ndarray:
+        """Nodal displacements (recover_results, linear_static.cpp:574-587):
+        (n_nodes, 6) T1 T2 T3 R1 R2 R3 in the uploaded node order, 0 for
+        constrained DOFs.  u: host displacements, or None for load case k of
+        the last solve."""
+        out = np.zeros((self.n_nodes, 6))
+        u_in = None if u is None else np.ascontiguousarray(u, np.float64)
+        self.backend.context.check(load_library().vsgb_node_displacements(
+            self.backend.context.ptr,
+            None if u_in is None else u_in.ctypes.data_as(ctypes.c_void_p), k, out.reshape(-1)))
+        return out
 
     def adjoint_gradients(self, F, dJdu=None, with_adjoint=False):
         """Compliance and linear-response gradients w.r.t. every element's E
@@ -659,6 +675,21 @@ class BdfDeck:
         return C.SolidModel(node_ids=ids, xyz=xyz, conn=conn, elem_ids=eids, E=E, nu=nu,
                             form=form, spc_nodes=spc_nodes, spc_mask=spc_mask, loads=loads,
                             name=name)
+
+
+def write_node_csv(path, node_ids, disp, subcase_ids=(1,)):
+    """CsvWriter's nodal CSV (csv_writer.cpp:34-57) of disp ((n_subcases,)
+    n_nodes, 6) in the node order of node_ids, listed in ascending id order."""
+    ids = np.ascontiguousarray(node_ids, np.int32)
+    d = np.ascontiguousarray(disp, np.float64).reshape(-1, ids.size, 6)
+    sc = np.ascontiguousarray(subcase_ids, np.int32)
+    if sc.size != d.shape[0]:
+        raise SolverError("one subcase id per displacement block")
+    err = ctypes.create_string_buffer(512)
+    rc = load_library().vsgb_write_node_csv(os.fsencode(path), ids.size, ids, sc.size, sc,
+                                            d.reshape(-1), err, 512)
+    if rc != VSGB_OK:
+        raise SolverError(err.value.decode(), rc)
 
 
 def read_bdf(path=None, text=None, threads=0) -> BdfDeck:

@@ -55,6 +55,7 @@ struct vsgb_ctx {
   int u_cases = 0;                     // load cases held in u by the last solve
   DevBuf<double> f, u;
   DevBuf<double> u_in, stress_c, stress_n;  // stress recovery staging
+  DevBuf<double> node_disp;                  // nodal displacement recovery
   // staging of an uploaded CSR (solve_csr)
   DevBuf<int> in_rp, in_ci;
   DevBuf<double> in_v;
@@ -805,6 +806,34 @@ int vsgb_solve_assembled(vsgb_ctx* c, const double* F, int nrhs, double* u_out,
   rc = vsgb_solve_resident(c, stats);
   if (rc != VSGB_OK) return rc;
   return vsgb_solution_download(c, u_out);
+}
+
+int vsgb_node_displacements(vsgb_ctx* c, const double* u, int k, double* disp_out) {
+  return guarded(c, [&] {
+    if (!c->mesh_ok) throw Error(VSGB_ERR_STATE, "no mesh uploaded");
+    if (!disp_out) throw Error(VSGB_ERR_INVALID, "null output");
+    cudaStream_t s = c->stream;
+    const int n = c->n_dof;
+    const double* du = nullptr;
+    if (u) {
+      c->u_in.reserve(static_cast<size_t>(n > 0 ? n : 1));
+      upload(c->u_in.ptr, u, sizeof(double) * n, s);
+      du = c->u_in.ptr;
+    } else {
+      if (k < 0 || k >= c->u_cases || c->K.n != n)
+        throw Error(VSGB_ERR_STATE, "no solution of load case " + std::to_string(k) +
+                                        " on this context");
+      du = c->u.ptr + static_cast<size_t>(k) * n;
+    }
+    const size_t nn = static_cast<size_t>(c->n_nodes);
+    c->node_disp.reserve(6 * nn + 1);
+    vsgb::launch_node_displacements(c->n_nodes, c->eq3.ptr, du, n, c->node_disp.ptr, c->num_sms,
+                                    s);
+    c->eng->add_launches(1);
+    VSGB_CUDA(cudaMemcpyAsync(disp_out, c->node_disp.ptr, sizeof(double) * 6 * nn,
+                              cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  });
 }
 
 int vsgb_solid_stress(vsgb_ctx* c, const double* u, int k, double* centroid_out,

@@ -26,6 +26,43 @@ void put_err(char* err, size_t len, const std::string& m) {
 
 }  // namespace
 
+extern "C" int vsgb_write_node_csv(const char* path, int n_nodes, const int* node_ids,
+                                   int n_subcases, const int* subcase_ids, const double* disp,
+                                   char* err, size_t errlen) {
+  if (!path || n_nodes < 0 || n_subcases < 0 || (n_nodes > 0 && (!node_ids || !disp)) ||
+      (n_subcases > 0 && !subcase_ids)) {
+    put_err(err, errlen, "vsgb_write_node_csv: invalid argument");
+    return VSGB_ERR_INVALID;
+  }
+  std::FILE* f = std::fopen(path, "w");
+  if (!f) {
+    put_err(err, errlen, std::string("Cannot write CSV: ") + path);
+    return VSGB_ERR_INVALID;
+  }
+  std::vector<int> order(static_cast<size_t>(n_nodes));
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [node_ids](int a, int b) { return node_ids[a] < node_ids[b]; });
+  std::fputs("# node_id, subcase_id, T1, T2, T3, R1, R2, R3\n", f);
+  char line[256];
+  for (int s = 0; s < n_subcases; ++s) {
+    const double* ds = disp + static_cast<size_t>(s) * n_nodes * 6;
+    for (int i : order) {
+      const double* d = ds + static_cast<size_t>(i) * 6;
+      const int len =
+          std::snprintf(line, sizeof(line), "%d, %d, %.8e, %.8e, %.8e, %.8e, %.8e, %.8e\n",
+                        node_ids[i], subcase_ids[s], d[0], d[1], d[2], d[3], d[4], d[5]);
+      std::fwrite(line, 1, static_cast<size_t>(len), f);
+    }
+  }
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) {
+    put_err(err, errlen, std::string("Cannot write CSV: ") + path);
+    return VSGB_ERR_INVALID;
+  }
+  return VSGB_OK;
+}
+
 extern "C" int vsgb_build_dof_map(int n_nodes, const int* node_ids, int n_elem,
                                   const int* conn_ids, int n_spc, const int* spc_node_ids,
                                   const int* spc_masks, int* eq6_out, int* n_free, char* err,

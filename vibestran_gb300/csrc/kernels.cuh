@@ -23,6 +23,8 @@ void launch_lame(int n_elem, const double* E, const double* nu, double* lame, in
                  cudaStream_t s);
 // CHEXA8 centroid (n_elem x 7) and corner (n_elem x 8 x 7, may be null)
 // stresses from the displacements u[n_dof] (stress.cu); lame: 2 * n_elem scratch.
+void launch_node_displacements(int n_nodes, const int* eq3, const double* u, int n_dof,
+                               double* out, int num_sms, cudaStream_t s);
 void launch_solid_stress(int n_elem, const double* xyz, const int* conn, const int* eq3,
                          const double* E, const double* nu, const double* u, int n_dof,
                          double* lame, double* centroid, double* nodal, int num_sms,

@@ -127,6 +127,35 @@ __global__ void k_solid_stress(int n_elem, const double* __restrict__ xyz,
 
 }  // namespace
 
+// Nodal displacements (recover_results, src/solver/linear_static.cpp:581-587):
+// thread per node, out[6 i + d] = u[eq] of its translational DOF d when free,
+// else 0; R1-R3 are 0 (solid elements activate T1-T3 only, so the DOF map
+// constrains the rotations of every node of this path).
+__global__ void k_node_displacements(int n_nodes, const int* __restrict__ eq3,
+                                     const double* __restrict__ u, int n_dof,
+                                     double* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_nodes; i += gridDim.x * blockDim.x) {
+    double d[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int eq = eq3[3 * i + q];
+      if (eq >= 0 && eq < n_dof) d[q] = u[eq];
+    }
+    double2* o = reinterpret_cast<double2*>(out + 6 * static_cast<size_t>(i));
+    o[0] = make_double2(d[0], d[1]);
+    o[1] = make_double2(d[2], d[3]);
+    o[2] = make_double2(d[4], d[5]);
+  }
+}
+
+void launch_node_displacements(int n_nodes, const int* eq3, const double* u, int n_dof,
+                               double* out, int num_sms, cudaStream_t s) {
+  if (n_nodes <= 0) return;
+  const int grid = grid_for(n_nodes, kThreads, num_sms * 8);
+  k_node_displacements<<<grid, kThreads, 0, s>>>(n_nodes, eq3, u, n_dof, out);
+  VSGB_LAUNCH_CHECK();
+}
+
 void launch_solid_stress(int n_elem, const double* xyz, const int* conn, const int* eq3,
                          const double* E, const double* nu, const double* u, int n_dof,
                          double* lame, double* centroid, double* nodal, int num_sms,
