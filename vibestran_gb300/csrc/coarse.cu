@@ -811,13 +811,8 @@ int tridiag_lowest(const std::vector<double>& d, const std::vector<double>& e, i
   return static_cast<int>(w.size());
 }
 
-bool coarse_basis(CoarseSpace& cs, const float* hist, bool padded,
-                  const std::vector<double>& coef, int K, int nb, int m, int num_sms,
-                  cudaStream_t s) {
-  cs.valid = false;
-  cs.defl_ready = false;
-  cs.m = 0;
-  if (K < 8 || m <= 0) return false;
+int coarse_host_basis(CoarseSpace& cs, const std::vector<double>& coef, int K, int m) {
+  if (K < 8 || m <= 0) return 0;
   m = std::min(m, kCoarseMax);
   // Lanczos tridiagonal of the preconditioned CG (Saad, Iterative Methods,
   // sec. 6.7.3): diagonal 1/alpha_k + beta_{k-1}/alpha_{k-1}, off-diagonal
@@ -825,18 +820,18 @@ bool coarse_basis(CoarseSpace& cs, const float* hist, bool padded,
   std::vector<double> d(static_cast<size_t>(K)), e(static_cast<size_t>(K - 1));
   for (int k = 0; k < K; ++k) {
     const double al = coef[3 * k], rz = coef[3 * k + 2];
-    if (!(al > 0.0) || !(rz > 0.0)) return false;
+    if (!(al > 0.0) || !(rz > 0.0)) return 0;
     d[k] = 1.0 / al;
     if (k > 0) {
       const double alp = coef[3 * (k - 1)], bep = coef[3 * (k - 1) + 1];
-      if (!(bep > 0.0)) return false;
+      if (!(bep > 0.0)) return 0;
       d[k] += bep / alp;
       e[k - 1] = std::sqrt(bep) / alp;
     }
   }
   std::vector<double> w, Y;
   const int found = tridiag_lowest(d, e, m, w, Y);
-  if (found == 0) return false;
+  if (found == 0) return 0;
   // weights of the Lanczos vectors v_k = (-1)^k z_k / sqrt(r_k.z_k), each
   // column scaled to unit largest weight (Z's scale is free)
   std::vector<double> Wd(static_cast<size_t>(K) * found);
@@ -853,10 +848,28 @@ bool coarse_basis(CoarseSpace& cs, const float* hist, bool padded,
     for (int k = 0; k < K; ++k)
       cs.Wh[static_cast<size_t>(k) * found + i] = static_cast<float>(Wd[static_cast<size_t>(k) * found + i] * sc);
   }
+  cs.ritz = w;
+  return found;
+}
+
+bool coarse_basis(CoarseSpace& cs, const float* hist, bool padded,
+                  const std::vector<double>& coef, int K, int nb, int m, int num_sms,
+                  cudaStream_t s) {
+  cs.valid = false;
+  cs.defl_ready = false;
+  cs.m = 0;
+  if (K < 8 || m <= 0) return false;
+  // the host part, unless it was computed ahead for this record
+  int found = 0;
+  if (cs.pre_found >= 0 && cs.pre_K == K && cs.pre_gen == cs.gen)
+    found = cs.pre_found;
+  else
+    found = coarse_host_basis(cs, coef, K, m);
+  cs.pre_found = -1;
+  if (found == 0) return false;
   const int n = 3 * nb;
   cs.n = n;
   cs.m = found;
-  cs.ritz = w;
   cs.Z.reserve(static_cast<size_t>(kCoarseMax) * n);
   cs.KZ.reserve(static_cast<size_t>(kCoarseMax) * n);
   cs.W.reserve(static_cast<size_t>(kCoarseHistMax) * kCoarseMax);

@@ -40,6 +40,11 @@ struct CoarseSpace {
   DevBuf<float> W;           // K x m combination weights of the Lanczos vectors
   std::vector<float> Wh;     // their host copy (pinned by the next copy only)
   std::vector<double> ritz;  // the Ritz values used (smallest first)
+  // host part of a basis computed ahead (coarse_host_basis): the Ritz pairs
+  // of a record of pre_K iterations for operator generation pre_gen, found
+  // vectors (Wh, ritz); pre_found < 0: none
+  int pre_found = -1, pre_K = 0;
+  unsigned pre_gen = ~0u;
   // deflated FP32 inner solves (resident.cu, 4 vectors, the unused ones
   // zero): W node-padded, A W, (W^T A W)^-1 and the bounds c_i
   bool defl_ready = false;
@@ -81,6 +86,11 @@ void coarse_apply(const CoarseSpace& cs, double* u, double* r, const double* din
 void coarse_apply_panel(const CoarseSpace& cs, double* U, double* R, const double* dinv,
                         const int* active, const double* norm_f, double* rel, double* scale,
                         double* uD2, int num_sms, cudaStream_t s);
+
+// The host part of coarse_basis alone (the Ritz pairs of the record's
+// tridiagonal and the weights Wh): returns the vectors found (0: no basis),
+// without any CUDA call, so that it can run while the GPU works.
+int coarse_host_basis(CoarseSpace& cs, const std::vector<double>& coef, int K, int m);
 
 // Host part of coarse_build (the template forwards to it after K Z).
 bool coarse_finish(CoarseSpace& cs, int num_sms, cudaStream_t s);

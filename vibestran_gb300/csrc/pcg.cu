@@ -940,11 +940,19 @@ void PcgEngine::trace_add(cudaStream_t s) {
 void PcgEngine::coarse_from_record(int count, cudaStream_t s, bool padded) {
   coarse_.gen = generation_;  // built (or found unusable) once per operator
   coarse_.valid = false;
-  if (count < 8) return;
-  coef_h_.resize(static_cast<size_t>(3) * count);
-  VSGB_CUDA(cudaMemcpyAsync(coef_h_.data(), coef_.ptr, sizeof(double) * coef_h_.size(),
-                            cudaMemcpyDeviceToHost, s));
-  VSGB_CUDA(cudaStreamSynchronize(s));
+  if (count < 8) {
+    coarse_.pre_found = -1;
+    return;
+  }
+  // the host part may have been computed from this record already (while
+  // the residual ran); otherwise read the record now
+  if (!(coarse_.pre_found >= 0 && coarse_.pre_K == count && coarse_.pre_gen == generation_)) {
+    coarse_.pre_found = -1;
+    coef_h_.resize(static_cast<size_t>(3) * count);
+    VSGB_CUDA(cudaMemcpyAsync(coef_h_.data(), coef_.ptr, sizeof(double) * coef_h_.size(),
+                              cudaMemcpyDeviceToHost, s));
+    VSGB_CUDA(cudaStreamSynchronize(s));
+  }
   coarse_build(coarse_, hist_.ptr, padded, coef_h_, count, n_ / 3, 4,
                [&](const double* X, double* Y, int m) {
                  // the basis has at most 4 vectors here (m requested above)
@@ -1154,6 +1162,26 @@ void PcgEngine::solve_mixed(const double* d_f, double tol, double inner_tol, int
       launch_residual64(s, d_f);
       VSGB_LAUNCH_CHECK();
       ++launches_;
+      // The coarse basis' host part (the Ritz pairs of the recorded
+      // tridiagonal, ~0.1 ms) runs while the FP64 residual does: the record
+      // is read on a copy stream that waits for the inner solve only.
+      if (coarse && record && step == 0 && !coarse_.valid) {
+        if (!copy_s_) VSGB_CUDA(cudaStreamCreateWithFlags(&copy_s_, cudaStreamNonBlocking));
+        VSGB_CUDA(cudaStreamWaitEvent(copy_s_, rev_[1], 0));
+        coef_h_.resize(static_cast<size_t>(3) * hist_max);
+        VSGB_CUDA(cudaMemcpyAsync(host, scal_.ptr, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                  copy_s_));
+        VSGB_CUDA(cudaMemcpyAsync(coef_h_.data(), coef_.ptr, sizeof(double) * coef_h_.size(),
+                                  cudaMemcpyDeviceToHost, copy_s_));
+        VSGB_CUDA(cudaStreamSynchronize(copy_s_));
+        const int K = std::min(host->iter, hist_max);
+        coarse_.pre_found = -1;
+        if ((host->flags & kFlagConverged) && K >= 8) {
+          coarse_.pre_found = coarse_host_basis(coarse_, coef_h_, K, 4);
+          coarse_.pre_K = K;
+          coarse_.pre_gen = generation_;
+        }
+      }
       // Galerkin correction in the coarse space right behind the residual
       // (the next inner solve reads the refreshed outer record on the device;
       // after a failed inner solve the iterate is not used)
@@ -1334,6 +1362,7 @@ PcgEngine::~PcgEngine() {
     if (g) cudaGraphExecDestroy(g);
   for (auto& e : rev_)
     if (e) cudaEventDestroy(e);
+  if (copy_s_) cudaStreamDestroy(copy_s_);
   destroy_multi(multi_);
 }
 

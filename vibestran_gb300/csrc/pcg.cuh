@@ -198,6 +198,7 @@ class PcgEngine {
   // Events around each persistent launch; the host syncs after every launch
   // anyway to read the scalar record.
   cudaEvent_t rev_[2] = {nullptr, nullptr};
+  cudaStream_t copy_s_ = nullptr;  // reads a finished solve's record while later kernels run
   double resident_ms_ = 0.0;
   long long resident_iters_ = 0;
   void resident_begin(cudaStream_t s, const void* hot, size_t hot_bytes);  // before the launch
