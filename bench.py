@@ -782,11 +782,14 @@ def main():
         "speedup_mixed_vs_fp64_solve": statistics.median(fp64_solve) / statistics.median(mixed_solve),
         # The FP32 block operator (94 MB) stays in the 126 MB L2 across the
         # iterations of one launch, so DRAM carries ~1 % of the algorithmic
-        # bytes (ncu); the kernel is bound by L2 streaming and the per-
-        # iteration critical path of two grid reductions, not by HBM.  frac
-        # is the algorithmic rate against HBM (an effective rate).
+        # bytes (ncu); the kernel is bound by the operator loads a warp keeps
+        # in flight from L2 (ncu's L2 throughput stays under half its peak in
+        # the SpMV phase) and the per-iteration critical path of two grid
+        # reductions, not by HBM.  frac is the algorithmic rate against HBM
+        # (an effective rate).
         "roofline": {"kernel": "k_resident_pcg<float> (persistent FP32 inner solve)",
-                     "bound": "l2+grid-sync", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "bound": "l2-latency+grid-sync", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
                      "frac_meaning": "algorithmic bytes per second against the HBM copy rate",
                      "traffic": (_traffic_per_iteration("k_resident_pcg_f32") * res_it
